@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 phonon particle-advance path.
+
+Workload (one GPU): the in-plane thin film -- 100 nm thick, periodic along
+the film, diffuse top and bottom walls, 1 K/um gradient, silicon-like
+LA + 2 TA material at 300 K (1000 frequency bins), 1e7 phonons, 100 cells,
+dt = 0.5 ps, 4000 steps, FP32 flight with FP64 tallies. One bench step is
+one complete solve: emission of all phonons, every dt-step to the 2 ns
+horizon, the FP64 tally. Inputs are synthetic (analytic material tables,
+seeded Philox4x32-10 streams).
+
+value      phonon-steps/s of the device-resident solve (tables and state
+           already on the device, CUDA events on the session stream).
+e2e        the same metric through the public C ABI call mc_solve() with
+           host buffers: device allocation, table upload, emission, all
+           launches and the copy of the field back to host memory.
+roofline   the advance kernel, HBM bound: algorithmic bytes = 48 B of FP32
+           phonon state read per live phonon plus 48 B written per
+           survivor, per launch, over the average launch duration.
+cpu_baseline  the FP64 oracle (C++ restatement of the reference's event
+           loop, OpenMP over phonons, all host cores) on a bounded sample.
+
+--impl reference times that CPU implementation alone on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+WORKLOAD = dict(thickness=1e-7, length=1e-7, cells=100, nemit=10_000_000, dt=0.5e-12, nsteps=4000,
+                maxscat=1_000_000, T=300.0)
+WORKLOAD_NAME = ("in-plane film 100 nm, periodic x / diffuse y / specular z, 1 K/um, Si-like LA+2TA 300 K "
+                 "(1000 bins), 1e7 phonons, 100 cells, dt 0.5 ps x 4000 steps, FP32 flight / FP64 tally")
+METRIC = "phonon-steps/s"
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        load = [x for x in sm if x > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_phonon():
+    """DRAM bytes per live phonon per advance launch from the committed ncu
+    summary (profiles/advance_traffic.json), if present."""
+    p = os.path.join(HERE, "profiles", "advance_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_live_phonon"]), d.get("source", "")
+    return None, None
+
+
+def cpu_baseline(W, sample_phonons, threads=0):
+    """Oracle (FP64, OpenMP) on a bounded sample of the workload."""
+    from oracle import oracle as O
+    from montecarlocpp_gb300 import FilmDomain, silicon_tables
+    disp, relax = silicon_tables()
+    m = O.OMaterial(disp, relax, W["T"])
+    dom = FilmDomain.from_cli(W["length"], W["thickness"], W["cells"])
+    d = O.ODomain(dom)
+    t0 = time.perf_counter()
+    _, st, _ = O.solve(m, d, O.MULTI, nemit=sample_phonons, maxscat=W["maxscat"], dt=W["dt"],
+                       horizon=W["dt"] * W["nsteps"], rng=O.RNG_PHILOX, seed=1, nthreads=threads)
+    el = time.perf_counter() - t0
+    cores = threads or os.cpu_count()
+    return {"value": st["phonon_steps"] / el, "unit": "phonon-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{st['nemit']} phonons of the same workload (full 4000-step horizon), "
+                      f"{st['phonon_steps']:.3g} phonon-steps, {st['events']} events in {el:.2f} s",
+            "events_per_s": st["events"] / el}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    W = dict(WORKLOAD)
+    sample = int(os.environ.get("MC_REF_SAMPLE", 200_000))
+    for _ in range(args.warmup):
+        cpu_baseline(W, sample)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(W, sample))
+    el = time.perf_counter() - t0
+    v = statistics.median(x["value"] for x in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "phonon-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "sample_phonons": sample},
+            "cpu_baseline": {"value": v, "unit": "phonon-steps/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "phonon-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference needs Eigen 3 and Boost, absent here; its event loop is timed through the "
+                    "C++ oracle restatement (oracle/mc_oracle.cpp)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nemit", type=int, default=WORKLOAD["nemit"])
+    ap.add_argument("--nsteps", type=int, default=WORKLOAD["nsteps"])
+    ap.add_argument("--k", type=int, default=0, help="dt-steps per launch (0: tuned)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import montecarlocpp_gb300 as M
+    from montecarlocpp_gb300 import autotune
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    W = dict(WORKLOAD, nemit=args.nemit, nsteps=args.nsteps)
+    mat = M.Material.silicon(W["T"])
+    dom = M.FilmDomain.from_cli(W["length"], W["thickness"], W["cells"])
+    prob = M.MultiProblem(mat, dom, W["nemit"], W["maxscat"])
+    stream = torch.cuda.Stream()
+    K = args.k or autotune.best_steps_per_launch(prob, W, stream)
+    seed = 1000 + rank
+    common = dict(dt=W["dt"], nsteps=W["nsteps"], precision=32, steps_per_launch=K, seed=seed,
+                  stream=stream.cuda_stream)
+    sess = prob.session(**common)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up
+    for _ in range(args.warmup):
+        sess.run()
+        sess.result(field=False)
+
+    # timed: device-resident solves, per-launch events
+    per_launch = []  # (ms, live_in, live_out)
+    totals = []
+    steps_done = 0.0
+    launches_total = 0
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_all0 = torch.cuda.Event(enable_timing=True)
+        t_all1 = torch.cuda.Event(enable_timing=True)
+        t_all0.record(stream)
+        for it in range(args.steps):
+            sess.emit()
+            done = False
+            evs = []
+            while not done:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                done = sess.advance(1)
+                e1.record(stream)
+                evs.append((e0, e1))
+            _, st = sess.result(field=False)
+            steps_done += st["phonon_steps"]
+            launches_total += st["launches"]
+            per_launch.extend(e0.elapsed_time(e1) for e0, e1 in evs)
+        t_all1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    total_ms = t_all0.elapsed_time(t_all1)
+    if world > 1:
+        t = torch.tensor([total_ms, steps_done], dtype=torch.float64, device="cuda")
+        tm = t.clone()
+        torch.distributed.all_reduce(tm[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        total_ms, steps_all = float(tm[0]), float(t[1])
+    else:
+        steps_all = steps_done
+    value = steps_all / (total_ms * 1e-3)
+
+    # roofline of the advance kernel: phonon state bytes per launch
+    live = W["nemit"]  # C1 phonons only stop at the horizon: every launch sees all of them
+    nl = len(per_launch) // max(args.steps, 1)
+    avg_ms = statistics.mean(per_launch)
+    bytes_launch = 48.0 * live * 2 if nl > 1 else 48.0 * live
+    peak, peak_kind = measured_peak()
+    achieved = bytes_launch / (avg_ms * 1e-3) / 1e9
+    tpp, tsrc = traffic_per_phonon()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": (tpp * live if tpp else None), "peak_source": peak_kind,
+            "kernel": "k_advance<float>", "launch_ms": avg_ms, "launches_per_solve": nl,
+            "algorithmic_bytes_per_launch": bytes_launch}
+
+    # e2e through mc_solve (host buffers)
+    e2e_steps, e2e_t = 0.0, 0.0
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        out = prob.solve(dt=W["dt"], nsteps=W["nsteps"], precision=32, steps_per_launch=K, seed=seed)
+        e2e_t += time.perf_counter() - t0
+        e2e_steps += prob.stats["phonon_steps"]
+    h2d = 8 * (mat.nw * mat.np * 2) + 8 * (mat.nw * (mat.np + 1) * 2) + 4096
+    d2h = out.size * 8 + 8 * 18
+    kappa = M.kappa_from_flux(out, dom, 0, flux_row0=1)
+
+    line = {"metric": METRIC, "value": value, "unit": "phonon-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: analytic Si-like dispersion/relaxation tables, Philox4x32-10 keyed by phonon id",
+            "config": {"workload": WORKLOAD_NAME, "nemit": W["nemit"], "cells": W["cells"], "dt": W["dt"],
+                       "nsteps": W["nsteps"], "steps_per_launch": K, "precision": "fp32 flight, fp64 tally",
+                       "l2": "phonon state 2 x 480 MB > L2 (129 MB)"},
+            "e2e": {"value": e2e_steps / e2e_t, "unit": "phonon-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_total,
+            "roofline": roof,
+            "clocks": clk.summary(),
+            "kappa_W_per_mK": kappa}
+
+    if not args.no_plain:
+        line["plain_kernel"] = plain_kernel(prob, W, stream, peak, peak_kind)
+    if rank == 0 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(W, int(os.environ.get("MC_CPU_SAMPLE", 400_000)))
+        except Exception as e:  # the oracle is only a reported baseline
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def plain_kernel(prob, W, stream, peak, peak_kind, nsteps=64):
+    """The per-dt-step kernel (K = 1): 48 B read + 48 B written per phonon
+    per launch; first `nsteps` steps of the same workload."""
+    import torch
+    s = prob.session(dt=W["dt"], nsteps=nsteps, precision=32, steps_per_launch=1, seed=7,
+                     stream=stream.cuda_stream)
+    s.emit()
+    s.advance(4)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.advance(nsteps - 4 - 1)
+    e1.record(stream)
+    s.advance(1)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / (nsteps - 5)
+    n = W["nemit"]
+    ach = 96.0 * n / (ms * 1e-3) / 1e9
+    _, st = s.result(field=False)
+    s.close()
+    return {"steps_per_launch": 1, "launch_ms": ms, "phonon_steps_per_s": n / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": 96.0 * n}}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

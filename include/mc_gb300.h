@@ -1,0 +1,172 @@
+/*
+ * mc_gb300.h -- C ABI of the GB300 (sm_103a) phonon particle-advance library.
+ *
+ * The library replaces the run loop of montecarlocpp's field problems,
+ * `ArrayXXd FieldProblem::solve(Rng& gen, Progress* prog) const`
+ * (montecarlo/problem.h:141, montecarlo/problem.cpp:370-445), with
+ * hand-written CUDA kernels. Plain pointers and sizes only; all device memory
+ * is owned by the library; every entry point returns an int status
+ * (MC_OK = 0, negative on error, message from mc_last_error()) where the
+ * reference aborts on BOOST_ASSERT_MSG. There is no CPU fallback: without a
+ * CUDA device the compute entry points return MC_ERR_NO_DEVICE.
+ *
+ * Array layouts: matrices are row-major (M[3*r + c], columns of M are the
+ * edge vectors as in the reference's Parallelepiped(o, mat, ...)); field
+ * results are rows x cols in COLUMN-major order, i.e. the memory layout of
+ * the reference's Eigen::ArrayXXd, so a C++ caller can wrap the buffer with
+ * Eigen::Map<ArrayXXd>(out, rows, cols).
+ */
+#ifndef MC_GB300_H
+#define MC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define MC_OK 0
+#define MC_ERR_ARG (-1)          /* invalid argument (reference: assert)  */
+#define MC_ERR_CUDA (-2)         /* CUDA runtime error                     */
+#define MC_ERR_NO_DEVICE (-3)    /* no CUDA device: no CPU fallback        */
+#define MC_ERR_UNSUPPORTED (-4)  /* geometry outside the kernels' limits   */
+#define MC_ERR_IO (-5)           /* file could not be read                 */
+#define MC_ERR_REPLAY (-6)       /* replay stream exhausted                */
+#define MC_ERR_NONFINITE (-7)    /* non-finite phonon state                */
+#define MC_ERR_BUSY (-8)         /* admission refused (serving)            */
+
+/* Message of the last error on the calling thread. */
+const char* mc_last_error(void);
+/* Library version string. */
+const char* mc_version(void);
+
+/* ------------------------------------------------------------- material */
+typedef struct mc_material_s* mc_material_h;
+
+/* Material(disp, relax, T) from the parsed file contents
+ * (montecarlo/material.cpp:154-234): disp is nw rows of
+ * (omega, domega, (vel_p, dos_p) x np) row-major; relax is np rows of 8
+ * coefficients (two terms c0 w^c1 T^c2 exp(-c3/T)). */
+int mc_material_create(const double* disp, long nw, long np, const double* relax, double T,
+                       mc_material_h* out);
+/* Material(disp, relax, T) reading the two files
+ * (montecarlo/material.cpp:158-186). */
+int mc_material_load(const char* disp_path, const char* relax_path, double T, mc_material_h* out);
+/* energySum, fluxSum, scatSum, cond (montecarlo/material.h:55,62-64). */
+int mc_material_sums(mc_material_h m, double out[4]);
+/* vel and tau tables, nw x np row-major (montecarlo/material.cpp:246-256). */
+int mc_material_tables(mc_material_h m, double* vel, double* tau);
+void mc_material_destroy(mc_material_h m);
+
+/* --------------------------------------------------------------- domain */
+typedef struct mc_domain_s* mc_domain_h;
+
+enum { MC_SPEC = 0, MC_DIFF = 1, MC_ISOT = 2, MC_PERI = 3, MC_INTER = 4 };
+
+/* Parallelepiped<Bac, Lef, Bot, Fro, Rig, Top>(o, mat, div, gradT, T)
+ * (montecarlo/subdomain.h:145-158); faces in bdry<0..5>() order. */
+typedef struct {
+    double o[3];
+    double M[9];
+    long div[3];
+    double gradT[3];
+    int kind[6];
+    double T[6];
+} mc_pped_desc;
+
+/* makePair(bdry1, bdry2[, transl, rot]) (montecarlo/boundary.cpp:361-369
+ * for Inter, montecarlo/boundary.cpp:524-550 for Peri). */
+typedef struct {
+    int kind;
+    int sdom1, face1;
+    int sdom2, face2;
+    double transl[3];
+    double rot[9];
+} mc_pair_desc;
+
+/* Domain assembly (montecarlo/domain.cpp:88-102 addSdom and the
+ * init() of each domain). Limits: <= 32 subdomains, <= 512 cells per axis
+ * per subdomain, one pair per Inter face. */
+int mc_domain_create(const mc_pped_desc* ppeds, int n, const mc_pair_desc* pairs, int npairs,
+                     mc_domain_h* out);
+/* Number of field columns (montecarlo/field.cpp:93-113). */
+long mc_domain_cols(mc_domain_h d);
+/* Cell volumes, one per column (CellVolF, montecarlo/problem.cpp:302-306). */
+int mc_domain_cell_volumes(mc_domain_h d, double* out);
+void mc_domain_destroy(mc_domain_h d);
+
+/* -------------------------------------------------------------- problem */
+enum { MC_TEMP = 0, MC_FLUX = 1, MC_MULTI = 2 };
+enum { MC_TALLY_AUTO = -1, MC_TALLY_SHARED = 0, MC_TALLY_GLOBAL = 1 };
+
+typedef struct {
+    int problem;            /* MC_TEMP (1 row), MC_FLUX (3), MC_MULTI (4)   */
+    long nemit;             /* requested phonons (montecarlo/problem.cpp:329-337 rounding) */
+    long maxscat;
+    long maxloop;           /* 0 -> 100 * maxscat (montecarlo/problem.cpp:339) */
+    double dt;              /* step length, s                              */
+    long nsteps;            /* time horizon = nsteps * dt                  */
+    int precision;          /* 32: FP32 flight, 64: FP64 flight; tallies FP64 */
+    uint64_t seed;          /* Philox key                                  */
+    int steps_per_launch;   /* K dt-steps per advance launch (>= 1)        */
+    int block_size;         /* 0 -> 256                                    */
+    int grid_blocks;        /* 0 -> resident blocks x SMs                  */
+    int tally_mode;         /* MC_TALLY_*                                  */
+    /* replay: per-phonon 32-bit words, offsets has nemit+1 entries (host) */
+    const uint32_t* replay_words;
+    const int64_t* replay_offsets;
+    /* event log (host buffers, may be NULL): log_cap records of 12 doubles
+     * per phonon id < log_phonons: loop index, subdomain, face hit (-1
+     * scatter, -2 horizon, -3 escape), subdomain after, cell, x, y, z,
+     * time, nscat, w, p */
+    double* log;
+    int64_t* log_counts;
+    long log_cap;
+    long log_phonons;
+    void* stream;           /* cudaStream_t; NULL -> library stream        */
+} mc_problem_desc;
+
+typedef struct {
+    long nemit;             /* phonons after rounding                      */
+    double power;           /* montecarlo/problem.cpp:341                  */
+    long rows, cols;
+    double phonon_steps;    /* live phonon x dt-step pairs processed       */
+    long events, scatters, escapes, horizon_stops, maxscat_stops, maxloop_stops, absorbed,
+        nonfinite;
+    unsigned status;        /* MC status bits (replay exhausted, nonfinite) */
+    double kernel_ms;       /* device time of emission + advance launches   */
+    int launches;
+    double checksum[4];     /* per row: sum over every flight of its tally
+                               amount before the cell split (equals the
+                               raw tally summed over cells)                 */
+} mc_stats;
+
+/* Replaces FieldProblem::solve over all phonons of the problem
+ * (montecarlo/problem.cpp:370-445) followed by the caller's reduction
+ * (montecarlo/main.cpp:162-165): out is rows x cols column-major and holds
+ * power * postProc(tally) / cellVol. Host buffers; synchronous. */
+int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st);
+
+/* ---------------------------------------------- device-resident session */
+typedef struct mc_session_s* mc_session_h;
+
+/* Allocate the phonon structure of arrays and tables on the device. */
+int mc_session_create(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, mc_session_h* out);
+/* Emit all phonons (reset tally, counters and time). Asynchronous. */
+int mc_session_emit(mc_session_h s);
+/* Launch up to `nlaunch` advance windows; *done = 1 once the horizon is
+ * reached. Asynchronous on the session stream. */
+int mc_session_advance(mc_session_h s, int nlaunch, int* done);
+/* Synchronise; copy the post-processed field (may be NULL) and stats. */
+int mc_session_result(mc_session_h s, double* out, mc_stats* st);
+/* Bytes the phonon state of this session occupies on the device. */
+size_t mc_session_state_bytes(mc_session_h s);
+void mc_session_destroy(mc_session_h s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MC_GB300_H */

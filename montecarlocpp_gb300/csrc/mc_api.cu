@@ -1,0 +1,879 @@
+// mc_api.cu -- host side of the C ABI declared in include/mc_gb300.h.
+//
+// Builds, in FP64 on the host, everything the kernels read: the material's
+// velocity / relaxation tables and integer inverse-CDF thresholds
+// (montecarlo/material.cpp:51-75,154-234), the subdomains' reduced-coordinate
+// geometry, face normals, rotations and pair maps
+// (montecarlo/subdomain.cpp:41-71, montecarlo/boundary.cpp:28-37,44-56,
+// 361-369,524-550), the emitter list and phonon allocation
+// (montecarlo/domain.cpp:88-102, montecarlo/problem.cpp:315-342), and
+// post-processes the FP64 tallies (montecarlo/problem.cpp:439-551).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/mc_gb300.h"
+#include "mc_launch.h"
+
+using namespace mcg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cudaFail(cudaError_t e, const char* where) {
+    return fail(MC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                                    \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cudaFail(e_, #call);          \
+    } while (0)
+
+const double HBAR = 1.054560652927e-034;  // montecarlo/constants.h:18
+const double KB = 1.380648e-023;          // montecarlo/constants.h:19
+const double DMIN = std::numeric_limits<double>::min();
+const double DEPS = std::numeric_limits<double>::epsilon();
+
+int ensureDevice() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(MC_ERR_NO_DEVICE, "no CUDA device: the GB300 kernels cannot run (no CPU fallback)");
+    return MC_OK;
+}
+
+// ---------------------------------------------------------------- vectors
+struct V3 { double v[3]; double& operator[](int i) { return v[i]; } double operator[](int i) const { return v[i]; } };
+V3 mk(double a, double b, double c) { V3 r; r[0] = a; r[1] = b; r[2] = c; return r; }
+double dot(const V3& a, const V3& b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+V3 cross(const V3& a, const V3& b) {
+    return mk(a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]);
+}
+V3 unit(const V3& a) {
+    double z = dot(a, a);
+    if (!(z > 0.)) return a;
+    double s = std::sqrt(z);
+    return mk(a[0] / s, a[1] / s, a[2] / s);
+}
+struct M3 { double m[9]; };
+M3 eye() { M3 r{}; r.m[0] = r.m[4] = r.m[8] = 1.; return r; }
+M3 mmul(const M3& a, const M3& b) {
+    M3 r{};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = (a.m[3 * i] * b.m[j] + a.m[3 * i + 1] * b.m[3 + j]) + a.m[3 * i + 2] * b.m[6 + j];
+    return r;
+}
+V3 mvec(const M3& a, const V3& x) {
+    return mk((a.m[0] * x[0] + a.m[1] * x[1]) + a.m[2] * x[2], (a.m[3] * x[0] + a.m[4] * x[1]) + a.m[5] * x[2],
+              (a.m[6] * x[0] + a.m[7] * x[1]) + a.m[8] * x[2]);
+}
+M3 transp(const M3& a) { M3 r{}; for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) r.m[3 * i + j] = a.m[3 * j + i]; return r; }
+double det3(const M3& a) {
+    const double* m = a.m;
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+M3 inv3(const M3& a) {
+    const double* m = a.m;
+    double d = det3(a);
+    M3 r{};
+    r.m[0] = (m[4] * m[8] - m[5] * m[7]) / d; r.m[1] = (m[2] * m[7] - m[1] * m[8]) / d; r.m[2] = (m[1] * m[5] - m[2] * m[4]) / d;
+    r.m[3] = (m[5] * m[6] - m[3] * m[8]) / d; r.m[4] = (m[0] * m[8] - m[2] * m[6]) / d; r.m[5] = (m[2] * m[3] - m[0] * m[5]) / d;
+    r.m[6] = (m[3] * m[7] - m[4] * m[6]) / d; r.m[7] = (m[1] * m[6] - m[0] * m[7]) / d; r.m[8] = (m[0] * m[4] - m[1] * m[3]) / d;
+    return r;
+}
+V3 colOf(const M3& a, int c) { return mk(a.m[c], a.m[3 + c], a.m[6 + c]); }
+
+// Rotation taking z-hat to n: half-angle quaternion about z x n, as a
+// matrix; for n = -z the rotation by pi about x.
+M3 rotZTo(const V3& nIn) {
+    V3 v1 = unit(nIn);
+    double c = v1[2];
+    double qw, qx, qy, qz;
+    if (c < -1. + 1e-12) {
+        qw = 0.; qx = 1.; qy = 0.; qz = 0.;
+    } else {
+        V3 axis = cross(mk(0., 0., 1.), v1);
+        double s = std::sqrt((1. + c) * 2.);
+        double invs = 1. / s;
+        qx = axis[0] * invs; qy = axis[1] * invs; qz = axis[2] * invs;
+        qw = s * 0.5;
+    }
+    double tx = 2. * qx, ty = 2. * qy, tz = 2. * qz;
+    double twx = tx * qw, twy = ty * qw, twz = tz * qw;
+    double txx = tx * qx, txy = ty * qx, txz = tz * qx;
+    double tyy = ty * qy, tyz = tz * qy, tzz = tz * qz;
+    M3 r{};
+    r.m[0] = 1. - (tyy + tzz); r.m[1] = txy - twz; r.m[2] = txz + twy;
+    r.m[3] = txy + twz; r.m[4] = 1. - (txx + tzz); r.m[5] = tyz - twx;
+    r.m[6] = txz - twy; r.m[7] = tyz + twx; r.m[8] = 1. - (txx + tyy);
+    return r;
+}
+
+// Integer inverse-CDF thresholds: T_i = ceil(cdf_i * 2^32), so that for a
+// 32-bit word x, x < T_i exactly when x / 2^32 < cdf_i in FP64.
+unsigned long long thrOf(double cdf) {
+    double t = std::ceil(std::ldexp(cdf, 32));
+    if (t < 0.) t = 0.;
+    if (t > 4294967296.0) t = 4294967296.0;
+    return (unsigned long long)t;
+}
+
+// Two-level discrete distribution (montecarlo/material.cpp:123-147) as
+// FP64 cumulative tables.
+void buildThresholds(const std::vector<double>& pdf, long nw, long np, std::vector<unsigned long long>& wthr,
+                     std::vector<unsigned long long>& pthr) {
+    std::vector<double> rowSum(nw), pre(nw);
+    double acc = 0.;
+    for (long w = 0; w < nw; ++w) {
+        double s = 0.;
+        for (long p = 0; p < np; ++p) s += pdf[w * np + p];
+        rowSum[w] = s;
+        acc += s;
+        pre[w] = acc;
+    }
+    wthr.resize(nw);
+    for (long w = 0; w < nw; ++w) wthr[w] = thrOf(pre[w] / acc);
+    pthr.assign(nw * np, 4294967296ull);
+    for (long w = 0; w < nw; ++w) {
+        if (!(rowSum[w] > 0.)) continue;
+        double a = 0.;
+        std::vector<double> pp(np);
+        for (long p = 0; p < np; ++p) { a += pdf[w * np + p]; pp[p] = a; }
+        for (long p = 0; p < np; ++p) pthr[w * np + p] = thrOf(pp[p] / a);
+    }
+}
+
+template <typename R>
+struct DevTables {
+    R* vel = nullptr;
+    R* vt = nullptr;
+    unsigned long long *wthr = nullptr, *pthr = nullptr, *fwthr = nullptr, *fpthr = nullptr;
+};
+
+}  // namespace
+
+struct mc_material_s {
+    long nw = 0, np = 0;
+    double T = 0.;
+    std::vector<double> omega, vel, tau;
+    double energySum = 0., fluxSum = 0., scatSum = 0., cond = 0.;
+    std::vector<unsigned long long> swthr, spthr, fwthr, fpthr;
+};
+
+namespace {
+
+int buildMaterial(const double* disp, long nw, long np, const double* relax, double T, mc_material_s** out) {
+    if (!disp || !relax || nw <= 0 || np <= 0 || np > 255 || nw > 65535)
+        return fail(MC_ERR_ARG, "Invalid dispersion file");
+    if (!(T > 0.)) return fail(MC_ERR_ARG, "temperature must be positive");
+    mc_material_s* m = new mc_material_s;
+    m->nw = nw; m->np = np; m->T = T;
+    m->omega.resize(nw);
+    m->vel.resize(nw * np);
+    m->tau.assign(nw * np, 0.);
+    std::vector<double> domega(nw), dos(nw * np);
+    const long nc = 2 + 2 * np;
+    for (long w = 0; w < nw; ++w) {
+        m->omega[w] = disp[w * nc];
+        domega[w] = disp[w * nc + 1];
+        for (long p = 0; p < np; ++p) {
+            m->vel[w * np + p] = disp[w * nc + 2 + 2 * p];
+            dos[w * np + p] = disp[w * nc + 3 + 2 * p];
+        }
+    }
+    for (long p = 0; p < np; ++p) {
+        std::vector<double> tinv(nw, 0.);
+        for (int j = 0; j < 2; ++j) {
+            const double* c = relax + p * 8 + 4 * j;
+            if (c[0] < 0.) { delete m; return fail(MC_ERR_ARG, "Scattering times cannot be negative"); }
+            if (c[0] <= DMIN) continue;
+            double tp = std::pow(T, c[2]), ex = std::exp(-c[3] / T);
+            for (long w = 0; w < nw; ++w) tinv[w] += c[0] * std::pow(m->omega[w], c[1]) * tp * ex;
+        }
+        for (long w = 0; w < nw; ++w) m->tau[w * np + p] = 1. / tinv[w];
+    }
+    for (long i = 0; i < nw * np; ++i)
+        if (!std::isfinite(m->tau[i])) { delete m; return fail(MC_ERR_ARG, "Scattering time model produced infinite values"); }
+    for (long i = 0; i < nw * np; ++i)
+        if (!(m->vel[i] > DMIN)) { delete m; return fail(MC_ERR_ARG, "Velocity must be nonzero"); }
+    std::vector<double> epdf(nw * np), fpdf(nw * np), spdf(nw * np);
+    double xs = HBAR / (KB * T), es = 0., fs = 0., ss = 0., k = 0.;
+    for (long w = 0; w < nw; ++w) {
+        double x = xs * m->omega[w];
+        double q = x / (2. * std::sinh(x / 2.));
+        double dedT = KB * (std::fabs(x) < DEPS ? 1. - x * x / 12. : q * q);
+        for (long p = 0; p < np; ++p) {
+            long i = w * np + p;
+            epdf[i] = dedT * dos[i] * domega[w];
+            fpdf[i] = m->vel[i] * epdf[i];
+            spdf[i] = epdf[i] / m->tau[i];
+            es += epdf[i]; fs += fpdf[i]; ss += spdf[i];
+            k += m->tau[i] * (m->vel[i] * m->vel[i]) * epdf[i];
+        }
+    }
+    if (!(fs > 0.) || !(ss > 0.)) { delete m; return fail(MC_ERR_ARG, "material has no phonons to draw"); }
+    m->energySum = es; m->fluxSum = fs; m->scatSum = ss; m->cond = k / 3.;
+    buildThresholds(spdf, nw, np, m->swthr, m->spthr);
+    buildThresholds(fpdf, nw, np, m->fwthr, m->fpthr);
+    *out = m;
+    return MC_OK;
+}
+
+bool readAll(const char* path, std::vector<double>& v) {
+    std::ifstream f(path);
+    if (!f) return false;
+    double x;
+    while (f >> x) v.push_back(x);
+    return true;
+}
+
+struct HostFace {
+    int kind;
+    V3 n, o;
+    double area, T;
+    int pairS = -1, pairF = -1;
+    M3 R = eye();
+    V3 t = mk(0, 0, 0);
+    int ninter = 0;
+};
+
+}  // namespace
+
+struct mc_domain_s {
+    std::vector<mc_pped_desc> pp;
+    std::vector<HostFace> faces;          // 6 per subdomain
+    std::vector<EmitterD> em;
+    std::vector<double> emWeight;
+    std::vector<long> colbeg;
+    long cols = 0;
+    std::vector<double> cellVol;
+    std::vector<SdomD<double>> sd;        // FP64 device image
+};
+
+namespace {
+
+int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_s** out) {
+    if (!ps || n <= 0) return fail(MC_ERR_ARG, "Domain setup not complete");
+    if (n > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 32 subdomains");
+    mc_domain_s* D = new mc_domain_s;
+    D->pp.assign(ps, ps + n);
+    D->faces.resize(6 * n);
+    D->sd.resize(n);
+    std::vector<std::vector<int>> faceEmit(n);
+    for (int s = 0; s < n; ++s) {
+        const mc_pped_desc& p = ps[s];
+        M3 M; std::memcpy(M.m, p.M, sizeof(M.m));
+        double vol = det3(M);
+        if (!(vol >= DMIN)) { delete D; return fail(MC_ERR_ARG, "Volume too small, check vector order"); }
+        V3 c0 = colOf(M, 0), c1 = colOf(M, 1), c2 = colOf(M, 2);
+        V3 o = mk(p.o[0], p.o[1], p.o[2]);
+        // faces (montecarlo/subdomain.h:149-154)
+        V3 fo[6] = {o, o, o, mk(o[0] + c0[0], o[1] + c0[1], o[2] + c0[2]),
+                    mk(o[0] + c1[0], o[1] + c1[1], o[2] + c1[2]), mk(o[0] + c2[0], o[1] + c2[1], o[2] + c2[2])};
+        V3 fi[6] = {c1, c2, c0, c2, c0, c1};
+        V3 fj[6] = {c2, c0, c1, c1, c2, c0};
+        for (int f = 0; f < 6; ++f) {
+            HostFace& F = D->faces[6 * s + f];
+            F.kind = p.kind[f];
+            if (F.kind < MC_SPEC || F.kind > MC_INTER) { delete D; return fail(MC_ERR_ARG, "invalid face kind"); }
+            if ((F.kind == MC_SPEC || F.kind == MC_DIFF || F.kind == MC_INTER) && p.T[f] != 0.) {
+                delete D; return fail(MC_ERR_ARG, "Cannot specify temperature");
+            }
+            V3 cr = cross(fi[f], fj[f]);
+            F.n = unit(cr);
+            F.area = std::sqrt(dot(cr, cr));
+            F.o = fo[f];
+            F.T = p.T[f];
+            if ((F.kind == MC_ISOT || F.kind == MC_PERI) && F.area * std::fabs(F.T) != 0.) faceEmit[s].push_back(f);
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (p.div[k] >= MAX_SHAPE) { delete D; return fail(MC_ERR_UNSUPPORTED, "more than 511 cells along an axis"); }
+        }
+    }
+    for (int q = 0; q < nq; ++q) {
+        const mc_pair_desc& P = qs[q];
+        if (P.sdom1 < 0 || P.sdom1 >= n || P.sdom2 < 0 || P.sdom2 >= n || P.face1 < 0 || P.face1 > 5 ||
+            P.face2 < 0 || P.face2 > 5) { delete D; return fail(MC_ERR_ARG, "pair index out of range"); }
+        HostFace& a = D->faces[6 * P.sdom1 + P.face1];
+        HostFace& b = D->faces[6 * P.sdom2 + P.face2];
+        if (a.kind != P.kind || b.kind != P.kind) { delete D; return fail(MC_ERR_ARG, "pair kind does not match faces"); }
+        if (P.kind == MC_PERI) {
+            if (a.pairS >= 0 || b.pairS >= 0) { delete D; return fail(MC_ERR_ARG, "Boundary already paired"); }
+            M3 R; std::memcpy(R.m, P.rot, sizeof(R.m));
+            V3 t = mk(P.transl[0], P.transl[1], P.transl[2]);
+            double T1 = a.T, T2 = b.T;
+            a.T = T1 - T2; b.T = T2 - T1;
+            a.R = R; b.R = transp(R);
+            a.t = t;
+            V3 mt = mvec(transp(R), t);
+            b.t = mk(-mt[0], -mt[1], -mt[2]);
+            a.pairS = P.sdom2; a.pairF = P.face2;
+            b.pairS = P.sdom1; b.pairF = P.face1;
+        } else if (P.kind == MC_INTER) {
+            if (a.ninter > 0 || b.ninter > 0) {
+                delete D; return fail(MC_ERR_UNSUPPORTED, "more than one pair on an Inter face");
+            }
+            a.ninter++; b.ninter++;
+            a.pairS = P.sdom2; a.pairF = P.face2;
+            b.pairS = P.sdom1; b.pairF = P.face1;
+        } else { delete D; return fail(MC_ERR_ARG, "pair kind must be Peri or Inter"); }
+    }
+    for (int s = 0; s < n; ++s)
+        for (int f = 0; f < 6; ++f) {
+            const HostFace& F = D->faces[6 * s + f];
+            if ((F.kind == MC_PERI || F.kind == MC_INTER) && F.pairS < 0) {
+                delete D; return fail(MC_ERR_ARG, "Domain setup not complete: unpaired face");
+            }
+        }
+    // subdomain images, emitters and columns
+    long cols = 0;
+    for (int s = 0; s < n; ++s) {
+        const mc_pped_desc& p = ps[s];
+        SdomD<double>& S = D->sd[s];
+        std::memset(&S, 0, sizeof(S));
+        M3 M; std::memcpy(M.m, p.M, sizeof(M.m));
+        M3 Mi = inv3(M);
+        std::memcpy(S.M, M.m, sizeof(M.m));
+        std::memcpy(S.Minv, Mi.m, sizeof(Mi.m));
+        bool neg = false;
+        int npos = 0;
+        for (int k = 0; k < 3; ++k) {
+            S.o[k] = p.o[k];
+            if (p.div[k] < 0) neg = true;
+            if (p.div[k] > 0) ++npos;
+            S.shape[k] = (int)std::max(p.div[k], 1L);
+            S.S[k] = S.shape[k];
+            S.gradT[k] = p.gradT[k];
+        }
+        // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
+        if (neg) S.accum = -2;
+        else if (npos == 0) S.accum = -1;
+        else if (npos == 1) { int d = 0; for (int k = 1; k < 3; ++k) if (p.div[k] > p.div[d]) d = k; S.accum = d; }
+        else S.accum = npos + 1;
+        M3 gr = rotZTo(unit(mk(p.gradT[0], p.gradT[1], p.gradT[2])));
+        std::memcpy(S.grot, gr.m, sizeof(gr.m));
+        double maxn = 0.;
+        for (int c = 0; c < 3; ++c) { V3 cc = colOf(M, c); maxn = std::max(maxn, std::sqrt(dot(cc, cc))); }
+        S.eps = 100. * DEPS * maxn;  // FP32 images rescale this
+        double vol = det3(M);
+        double gn = std::sqrt(dot(mk(p.gradT[0], p.gradT[1], p.gradT[2]), mk(p.gradT[0], p.gradT[1], p.gradT[2])));
+        double vw = 2. * vol * gn;  // montecarlo/subdomain.cpp:250-253
+        if (vw != 0.) { D->em.push_back(EmitterD{s, -1}); D->emWeight.push_back(vw); }
+        for (int f : faceEmit[s]) {
+            const HostFace& F = D->faces[6 * s + f];
+            D->em.push_back(EmitterD{s, f});
+            D->emWeight.push_back(F.area * std::fabs(F.T));  // montecarlo/boundary.cpp:413-416
+        }
+        long sp = neg ? 0 : (long)S.shape[0] * S.shape[1] * S.shape[2];
+        if (sp == 0) { S.colbeg = -1; D->colbeg.push_back(-1); continue; }
+        S.colbeg = (int)cols;
+        D->colbeg.push_back(cols);
+        for (long c = 0; c < sp; ++c) D->cellVol.push_back(vol / (double)sp);
+        cols += sp;
+    }
+    D->cols = cols;
+    // faces: normals, rotations, pair maps in reduced coordinates
+    for (int s = 0; s < n; ++s) {
+        SdomD<double>& S = D->sd[s];
+        for (int f = 0; f < 6; ++f) {
+            const HostFace& F = D->faces[6 * s + f];
+            FaceD<double>& G = S.f[f];
+            G.kind = F.kind;
+            G.to = -1; G.toface = -1; G.ident = 1;
+            for (int k = 0; k < 3; ++k) G.n[k] = F.n[k];
+            M3 r = rotZTo(F.n);
+            std::memcpy(G.rot, r.m, sizeof(r.m));
+            M3 I = eye();
+            std::memcpy(G.Rd, I.m, sizeof(I.m));
+            std::memcpy(G.A, I.m, sizeof(I.m));
+            G.T = F.T;
+            if (F.kind == MC_PERI || F.kind == MC_INTER) {
+                const int t = F.pairS;
+                G.to = t; G.toface = F.pairF;
+                M3 R = F.kind == MC_PERI ? F.R : eye();
+                V3 tr = F.kind == MC_PERI ? F.t : mk(0, 0, 0);
+                bool id = true;
+                for (int i = 0; i < 9; ++i) if (R.m[i] != eye().m[i]) id = false;
+                G.ident = id ? 1 : 0;
+                std::memcpy(G.Rd, R.m, sizeof(R.m));
+                // u' = diag(S') Minv' (R (o + M diag(1/S) u) + t - o')
+                const SdomD<double>& T2 = D->sd[t];
+                M3 Mi2; std::memcpy(Mi2.m, T2.Minv, sizeof(Mi2.m));
+                M3 M1; std::memcpy(M1.m, S.M, sizeof(M1.m));
+                M3 A = mmul(mmul(Mi2, R), M1);
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) A.m[3 * i + j] = A.m[3 * i + j] * T2.S[i] / S.S[j];
+                V3 Ro = mvec(R, mk(S.o[0], S.o[1], S.o[2]));
+                V3 x0 = mk(Ro[0] + tr[0] - T2.o[0], Ro[1] + tr[1] - T2.o[1], Ro[2] + tr[2] - T2.o[2]);
+                V3 b = mvec(Mi2, x0);
+                std::memcpy(G.A, A.m, sizeof(A.m));
+                for (int k = 0; k < 3; ++k) G.b[k] = T2.S[k] * b[k];
+            }
+        }
+    }
+    *out = D;
+    return MC_OK;
+}
+
+template <typename R>
+void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
+    std::memset(&b, 0, sizeof(b));
+    for (int i = 0; i < 9; ++i) { b.Minv[i] = (R)a.Minv[i]; b.M[i] = (R)a.M[i]; b.grot[i] = (R)a.grot[i]; }
+    for (int i = 0; i < 3; ++i) { b.o[i] = (R)a.o[i]; b.S[i] = (R)a.S[i]; b.gradT[i] = (R)a.gradT[i]; b.shape[i] = a.shape[i]; }
+    // escape tolerance: 100 ulp of the largest edge in the flight precision
+    b.eps = (R)(f32 ? a.eps / DEPS * (double)std::numeric_limits<float>::epsilon() : a.eps);
+    b.accum = a.accum;
+    b.colbeg = a.colbeg;
+    for (int f = 0; f < 6; ++f) {
+        const FaceD<double>& x = a.f[f];
+        FaceD<R>& y = b.f[f];
+        y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident;
+        for (int i = 0; i < 3; ++i) { y.n[i] = (R)x.n[i]; y.b[i] = (R)x.b[i]; }
+        for (int i = 0; i < 9; ++i) { y.rot[i] = (R)x.rot[i]; y.Rd[i] = (R)x.Rd[i]; y.A[i] = (R)x.A[i]; }
+        y.T = (R)x.T;
+    }
+}
+
+}  // namespace
+
+// ================================================================ session
+struct mc_session_s {
+    mc_material_h mat = nullptr;
+    mc_domain_h dom = nullptr;
+    mc_problem_desc desc{};
+    int prec = 32;
+    bool replay = false, logging = false;
+    int tm = TM_SHARED;
+    int block = 256, grid = 0;
+    size_t smem = 0;
+    long nemit = 0;
+    double power = 0.;
+    long maxloop = 0;
+    int rows = 1;
+    int step = 0;         // next window start
+    int launches = 0;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timing = false;
+    // device buffers
+    void* state = nullptr;       // two halves
+    size_t stateBytes = 0;
+    void* tables = nullptr;
+    void* dom_d = nullptr;
+    EmitterD* em_d = nullptr;
+    long long* cdf_d = nullptr;
+    unsigned long long* cnt_d = nullptr;   // counters + 2 live slots
+    unsigned int* status_d = nullptr;
+    double* tally_d = nullptr;
+    double* csum_d = nullptr;
+    uint32_t* rwords_d = nullptr;
+    long long* roff_d = nullptr;
+    uint32_t* rcur_d = nullptr;
+    double* log_d = nullptr;
+    int* logcnt_d = nullptr;
+    int parity = 0;               // which half holds the live phonons
+    Params<float> p32{};
+    Params<double> p64{};
+};
+
+namespace {
+
+template <typename R>
+int setupSession(mc_session_s* S) {
+    const mc_material_s& m = *S->mat;
+    const mc_domain_s& D = *S->dom;
+    const size_t nt = (size_t)m.nw * m.np;
+    // tables
+    size_t tb = 2 * sizeof(R) * nt + sizeof(unsigned long long) * (2 * m.nw + 2 * nt) + 64;
+    CK(cudaMalloc(&S->tables, tb));
+    char* base = (char*)S->tables;
+    std::vector<R> vel(nt), vt(nt);
+    for (size_t i = 0; i < nt; ++i) { vel[i] = (R)m.vel[i]; vt[i] = (R)(m.vel[i] * m.tau[i]); }
+    Params<R> P{};
+    P.vel = (R*)base; base += sizeof(R) * nt;
+    P.vt = (R*)base; base += sizeof(R) * nt;
+    base = (char*)(((uintptr_t)base + 15) & ~(uintptr_t)15);
+    P.wthr = (unsigned long long*)base; base += 8 * m.nw;
+    P.pthr = (unsigned long long*)base; base += 8 * nt;
+    P.fwthr = (unsigned long long*)base; base += 8 * m.nw;
+    P.fpthr = (unsigned long long*)base; base += 8 * nt;
+    CK(cudaMemcpy((void*)P.vel, vel.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)P.vt, vt.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)P.wthr, m.swthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)P.pthr, m.spthr.data(), 8 * nt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)P.fwthr, m.fwthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)P.fpthr, m.fpthr.data(), 8 * nt, cudaMemcpyHostToDevice));
+    // domain
+    std::vector<SdomD<R>> sd(D.sd.size());
+    for (size_t i = 0; i < sd.size(); ++i) castSdom(D.sd[i], sd[i], sizeof(R) == 4);
+    CK(cudaMalloc(&S->dom_d, sizeof(SdomD<R>) * sd.size()));
+    CK(cudaMemcpy(S->dom_d, sd.data(), sizeof(SdomD<R>) * sd.size(), cudaMemcpyHostToDevice));
+    P.sd = (const SdomD<R>*)S->dom_d;
+    P.nsd = (int)sd.size();
+    // emitters: rounded phonon counts (montecarlo/problem.cpp:319-341)
+    const long ne = (long)D.em.size();
+    if (ne == 0) return fail(MC_ERR_ARG, "No phonons to emit");
+    double wsum = 0.;
+    for (double w : D.emWeight) wsum += w;
+    std::vector<long long> cdf(ne);
+    long long tot = 0;
+    for (long i = 0; i < ne; ++i) {
+        double frac = D.emWeight[i] / wsum;
+        double rounded = std::ceil(frac * S->desc.nemit - 0.5);
+        tot += std::max(1LL, (long long)rounded);
+        cdf[i] = tot;
+    }
+    S->nemit = (long)tot;
+    S->power = wsum / (double)tot * m.fluxSum / 4.;
+    for (long i = 0; i < ne; ++i)
+        if (!(D.emWeight[i] > 0.)) return fail(MC_ERR_ARG, "No phonons to emit");
+    CK(cudaMalloc(&S->em_d, sizeof(EmitterD) * ne));
+    CK(cudaMemcpy(S->em_d, D.em.data(), sizeof(EmitterD) * ne, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&S->cdf_d, sizeof(long long) * ne));
+    CK(cudaMemcpy(S->cdf_d, cdf.data(), sizeof(long long) * ne, cudaMemcpyHostToDevice));
+    P.em = S->em_d; P.emitCdf = S->cdf_d; P.nem = (int)ne;
+    P.nw = (int)m.nw; P.np = (int)m.np;
+    // state: two halves of (P0, P1, P2)
+    const size_t n = (size_t)S->nemit;
+    using V4 = typename Vec4<R>::T;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
+    S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
+    CK(cudaMalloc(&S->state, 2 * half));
+    char* sb = (char*)S->state;
+    V4* h0[2]; V4* h1[2]; uint4* h2[2];
+    for (int h = 0; h < 2; ++h) {
+        h0[h] = (V4*)sb; sb += al(sizeof(V4) * n);
+        h1[h] = (V4*)sb; sb += al(sizeof(V4) * n);
+        h2[h] = (uint4*)sb; sb += al(sizeof(uint4) * n);
+    }
+    // counters: C_NCOUNTERS + 2 live counts
+    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 2)));
+    CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
+    S->rows = S->desc.problem == MC_TEMP ? 1 : (S->desc.problem == MC_FLUX ? 3 : 4);
+    CK(cudaMalloc(&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L)));
+    P.problem = S->desc.problem; P.rows = S->rows; P.cols = (int)D.cols;
+    P.nemit = S->nemit;
+    P.maxscat = S->desc.maxscat;
+    P.maxloop = S->maxloop;
+    P.dt = (R)S->desc.dt;
+    P.nsteps = (int)S->desc.nsteps;
+    P.ksteps = S->desc.steps_per_launch;
+    P.key0 = (uint32_t)S->desc.seed;
+    P.key1 = (uint32_t)(S->desc.seed >> 32);
+    P.counters = S->cnt_d;
+    P.status = S->status_d;
+    P.tally = S->tally_d;
+    CK(cudaMalloc(&S->csum_d, sizeof(double) * 4));
+    P.csum = S->csum_d;
+    // replay
+    if (S->replay) {
+        const int64_t* off = S->desc.replay_offsets;
+        long long nw = off[S->nemit];
+        if (off[0] != 0 || nw < 0) return fail(MC_ERR_ARG, "replay offsets must start at 0");
+        for (long i = 0; i < S->nemit; ++i)
+            if (off[i + 1] < off[i]) return fail(MC_ERR_ARG, "replay offsets must not decrease");
+        CK(cudaMalloc(&S->rwords_d, sizeof(uint32_t) * std::max(nw, 1LL)));
+        if (nw) CK(cudaMemcpy(S->rwords_d, S->desc.replay_words, sizeof(uint32_t) * nw, cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&S->roff_d, sizeof(long long) * (S->nemit + 1)));
+        CK(cudaMemcpy(S->roff_d, off, sizeof(long long) * (S->nemit + 1), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&S->rcur_d, sizeof(uint32_t) * S->nemit));
+        P.rwords = S->rwords_d; P.roff = S->roff_d; P.rcur = S->rcur_d;
+    }
+    if (S->logging) {
+        long long ln = std::min<long long>(S->desc.log_phonons, S->nemit);
+        CK(cudaMalloc(&S->log_d, sizeof(double) * 12 * (size_t)ln * S->desc.log_cap + 8));
+        CK(cudaMalloc(&S->logcnt_d, sizeof(int) * (size_t)std::max(ln, 1LL)));
+        P.log = S->log_d; P.logcap = S->desc.log_cap; P.logn = ln; P.logcount = S->logcnt_d;
+    }
+    // launch configuration
+    const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
+    S->tm = S->desc.tally_mode;
+    if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
+    S->smem = smemTableBytes<R>((int)m.nw, (int)m.np) + (S->tm == TM_SHARED ? tallyB : 0);
+    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
+    S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
+    if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int occ = advanceOccupancy<R>(S->replay, S->logging, S->tm, S->block, S->smem);
+    if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
+    S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    // halves
+    Params<R>* dst = nullptr;
+    if (sizeof(R) == 4) dst = (Params<R>*)&S->p32; else dst = (Params<R>*)&S->p64;
+    *dst = P;
+    struct Halves { V4* a[2]; V4* b[2]; uint4* c[2]; };
+    static_assert(sizeof(void*) == 8, "64-bit");
+    dst->P0in = h0[0]; dst->P1in = h1[0]; dst->P2in = h2[0];
+    dst->P0out = h0[1]; dst->P1out = h1[1]; dst->P2out = h2[1];
+    return MC_OK;
+}
+
+template <typename R>
+Params<R>& paramsOf(mc_session_s* S);
+template <> Params<float>& paramsOf<float>(mc_session_s* S) { return S->p32; }
+template <> Params<double>& paramsOf<double>(mc_session_s* S) { return S->p64; }
+
+template <typename R>
+int emitT(mc_session_s* S) {
+    Params<R>& P = paramsOf<R>(S);
+    // emission writes the first half
+    using V4 = typename Vec4<R>::T;
+    V4* a0 = P.P0in; V4* a1 = P.P1in; uint4* a2 = P.P2in;
+    if (S->parity == 1) { a0 = P.P0out; a1 = P.P1out; a2 = P.P2out; }
+    Params<R> E = P;
+    E.P0out = a0; E.P1out = a1; E.P2out = a2;
+    CK(cudaMemsetAsync(S->cnt_d, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 2), S->stream));
+    CK(cudaMemsetAsync(S->status_d, 0, sizeof(unsigned int), S->stream));
+    CK(cudaMemsetAsync(S->csum_d, 0, sizeof(double) * 4, S->stream));
+    CK(cudaMemsetAsync(S->tally_d, 0, sizeof(double) * (size_t)S->rows * std::max(S->dom->cols, 1L), S->stream));
+    if (S->replay) CK(cudaMemsetAsync(S->rcur_d, 0, sizeof(uint32_t) * S->nemit, S->stream));
+    if (S->logging) {
+        CK(cudaMemsetAsync(S->logcnt_d, 0, sizeof(int) * std::min<long long>(S->desc.log_phonons, S->nemit), S->stream));
+        CK(cudaMemsetAsync(S->log_d, 0xFF, sizeof(double) * 12 * (size_t)std::min<long long>(S->desc.log_phonons, S->nemit) * S->desc.log_cap, S->stream));
+    }
+    // live count of the emitted half
+    unsigned long long n = (unsigned long long)S->nemit;
+    CK(cudaMemcpyAsync(S->cnt_d + C_NCOUNTERS + S->parity, &n, sizeof(n), cudaMemcpyHostToDevice, S->stream));
+    CK(launchEmit<R>(E, S->replay, S->stream));
+    CK(cudaStreamSynchronize(S->stream));  // n lives on the host stack
+    S->step = 0;
+    S->launches = 1;
+    return MC_OK;
+}
+
+template <typename R>
+int advanceT(mc_session_s* S, int nl, int* done) {
+    Params<R>& P0 = paramsOf<R>(S);
+    const int nsteps = (int)S->desc.nsteps;
+    for (int l = 0; l < nl && S->step < nsteps; ++l) {
+        Params<R> P = P0;
+        if (S->parity == 1) {
+            std::swap(P.P0in, P.P0out); std::swap(P.P1in, P.P1out); std::swap(P.P2in, P.P2out);
+        }
+        P.nlive_in = S->cnt_d + C_NCOUNTERS + S->parity;
+        P.nlive_out = S->cnt_d + C_NCOUNTERS + (S->parity ^ 1);
+        P.step0 = S->step;
+        CK(cudaMemsetAsync(P.nlive_out, 0, sizeof(unsigned long long), S->stream));
+        CK(launchAdvance<R>(P, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+        S->parity ^= 1;
+        S->step += S->desc.steps_per_launch;
+        S->launches++;
+    }
+    if (done) *done = S->step >= nsteps ? 1 : 0;
+    return MC_OK;
+}
+
+int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
+    CK(cudaStreamSynchronize(S->stream));
+    const mc_domain_s& D = *S->dom;
+    const mc_material_s& m = *S->mat;
+    std::vector<unsigned long long> c(C_NCOUNTERS + 2);
+    unsigned int status = 0;
+    CK(cudaMemcpy(c.data(), S->cnt_d, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&status, S->status_d, sizeof(status), cudaMemcpyDeviceToHost));
+    const size_t nval = (size_t)S->rows * D.cols;
+    if (out) {
+        std::vector<double> t(nval);
+        if (nval) CK(cudaMemcpy(t.data(), S->tally_d, sizeof(double) * nval, cudaMemcpyDeviceToHost));
+        // postProc and / cellVol (montecarlo/problem.cpp:439-444,478-551)
+        for (long col = 0; col < D.cols; ++col)
+            for (int r = 0; r < S->rows; ++r) {
+                double v = t[(size_t)col * S->rows + r];
+                if (S->desc.problem == MC_TEMP || (S->desc.problem == MC_MULTI && r == 0)) v = v / m.energySum;
+                out[(size_t)col * S->rows + r] = S->power * (v / D.cellVol[col]);
+            }
+    }
+    if (S->logging && S->desc.log && S->desc.log_counts) {
+        long long ln = std::min<long long>(S->desc.log_phonons, S->nemit);
+        std::vector<int> lc(ln);
+        CK(cudaMemcpy(S->desc.log, S->log_d, sizeof(double) * 12 * (size_t)ln * S->desc.log_cap, cudaMemcpyDeviceToHost));
+        if (ln) CK(cudaMemcpy(lc.data(), S->logcnt_d, sizeof(int) * ln, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < ln; ++i) S->desc.log_counts[i] = lc[i];
+    }
+    if (st) {
+        std::memset(st, 0, sizeof(*st));
+        st->nemit = S->nemit;
+        st->power = S->power;
+        st->rows = S->rows;
+        st->cols = D.cols;
+        st->phonon_steps = (double)c[C_PHONON_STEPS];
+        st->events = (long)c[C_EVENTS];
+        st->scatters = (long)c[C_SCATTERS];
+        st->escapes = (long)c[C_ESCAPES];
+        st->horizon_stops = (long)c[C_HORIZON];
+        st->maxscat_stops = (long)c[C_MAXSCAT];
+        st->maxloop_stops = (long)c[C_MAXLOOP];
+        st->absorbed = (long)c[C_ABSORBED];
+        st->nonfinite = (long)c[C_BAD];
+        st->status = status;
+        st->launches = S->launches;
+        double cs[4] = {0, 0, 0, 0};
+        CK(cudaMemcpy(cs, S->csum_d, sizeof(cs), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < 4; ++r) st->checksum[r] = cs[r];
+    }
+    if (status & S_REPLAY_EXHAUSTED) return fail(MC_ERR_REPLAY, "replay stream exhausted");
+    if (status & S_NONFINITE) return fail(MC_ERR_NONFINITE, "non-finite phonon state");
+    return MC_OK;
+}
+
+void freeSession(mc_session_s* S) {
+    if (!S) return;
+    void* ps[] = {S->state, S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
+                  S->rwords_d, S->roff_d, S->rcur_d, S->log_d, S->logcnt_d};
+    for (void* p : ps) if (p) cudaFree(p);
+    if (S->ev0) cudaEventDestroy(S->ev0);
+    if (S->ev1) cudaEventDestroy(S->ev1);
+    if (S->ownStream && S->stream) cudaStreamDestroy(S->stream);
+    delete S;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+const char* mc_last_error(void) { return g_err.c_str(); }
+const char* mc_version(void) { return "montecarlocpp_gb300 0.1 (sm_103a)"; }
+
+int mc_material_create(const double* disp, long nw, long np, const double* relax, double T, mc_material_h* out) {
+    if (!out) return fail(MC_ERR_ARG, "null output handle");
+    return buildMaterial(disp, nw, np, relax, T, out);
+}
+
+int mc_material_load(const char* dp, const char* rp, double T, mc_material_h* out) {
+    if (!dp || !rp || !out) return fail(MC_ERR_ARG, "null argument");
+    std::vector<double> a, b;
+    if (!readAll(dp, a)) return fail(MC_ERR_IO, "Error opening dispersion file");
+    if (!readAll(rp, b)) return fail(MC_ERR_IO, "Error opening relaxation time file");
+    if (a.size() < 2) return fail(MC_ERR_ARG, "Invalid dispersion file");
+    long nw = (long)a[0], np = (long)a[1];
+    if (nw <= 0 || np <= 0) return fail(MC_ERR_ARG, "Invalid dispersion file");
+    if ((long)a.size() < 2 + nw * (2 + 2 * np) || (long)b.size() < 8 * np)
+        return fail(MC_ERR_ARG, "Array extraction failed");
+    return buildMaterial(a.data() + 2, nw, np, b.data(), T, out);
+}
+
+int mc_material_sums(mc_material_h m, double out[4]) {
+    if (!m || !out) return fail(MC_ERR_ARG, "null argument");
+    out[0] = m->energySum; out[1] = m->fluxSum; out[2] = m->scatSum; out[3] = m->cond;
+    return MC_OK;
+}
+
+int mc_material_tables(mc_material_h m, double* vel, double* tau) {
+    if (!m) return fail(MC_ERR_ARG, "null argument");
+    if (vel) std::memcpy(vel, m->vel.data(), sizeof(double) * m->vel.size());
+    if (tau) std::memcpy(tau, m->tau.data(), sizeof(double) * m->tau.size());
+    return MC_OK;
+}
+
+void mc_material_destroy(mc_material_h m) { delete m; }
+
+int mc_domain_create(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_h* out) {
+    if (!out) return fail(MC_ERR_ARG, "null output handle");
+    if (nq > 0 && !qs) return fail(MC_ERR_ARG, "null pair list");
+    return buildDomain(ps, n, qs, nq, out);
+}
+
+long mc_domain_cols(mc_domain_h d) { return d ? d->cols : -1; }
+
+int mc_domain_cell_volumes(mc_domain_h d, double* out) {
+    if (!d || !out) return fail(MC_ERR_ARG, "null argument");
+    std::memcpy(out, d->cellVol.data(), sizeof(double) * d->cellVol.size());
+    return MC_OK;
+}
+
+void mc_domain_destroy(mc_domain_h d) { delete d; }
+
+int mc_session_create(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, mc_session_h* out) {
+    if (!m || !d || !p || !out) return fail(MC_ERR_ARG, "null argument");
+    if (p->problem < MC_TEMP || p->problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+    if (p->nemit <= 0 || p->maxscat <= 0 || p->maxloop < 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
+    if (!(p->dt > 0.) || p->nsteps <= 0 || p->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
+    if (p->steps_per_launch <= 0) return fail(MC_ERR_ARG, "steps_per_launch must be >= 1");
+    if (p->precision != 32 && p->precision != 64) return fail(MC_ERR_ARG, "precision must be 32 or 64");
+    if ((p->replay_words == nullptr) != (p->replay_offsets == nullptr)) return fail(MC_ERR_ARG, "replay needs words and offsets");
+    if (p->log && (p->log_cap <= 0 || p->log_phonons <= 0 || !p->log_counts)) return fail(MC_ERR_ARG, "invalid log request");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    mc_session_s* S = new mc_session_s;
+    S->mat = m; S->dom = d; S->desc = *p;
+    S->prec = p->precision;
+    S->replay = p->replay_words != nullptr;
+    S->logging = p->log != nullptr;
+    S->maxloop = p->maxloop != 0 ? p->maxloop : 100 * p->maxscat;
+    if (p->stream) S->stream = (cudaStream_t)p->stream;
+    else {
+        cudaError_t e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete S; return cudaFail(e, "cudaStreamCreate"); }
+        S->ownStream = true;
+    }
+    rc = S->prec == 32 ? setupSession<float>(S) : setupSession<double>(S);
+    if (rc) { std::string msg = g_err; freeSession(S); g_err = msg; return rc; }
+    *out = S;
+    return MC_OK;
+}
+
+int mc_session_emit(mc_session_h s) {
+    if (!s) return fail(MC_ERR_ARG, "null session");
+    s->parity = 0;
+    return s->prec == 32 ? emitT<float>(s) : emitT<double>(s);
+}
+
+int mc_session_advance(mc_session_h s, int nl, int* done) {
+    if (!s || nl < 0) return fail(MC_ERR_ARG, "invalid argument");
+    return s->prec == 32 ? advanceT<float>(s, nl, done) : advanceT<double>(s, nl, done);
+}
+
+int mc_session_result(mc_session_h s, double* out, mc_stats* st) {
+    if (!s) return fail(MC_ERR_ARG, "null session");
+    return resultImpl(s, out, st);
+}
+
+size_t mc_session_state_bytes(mc_session_h s) { return s ? s->stateBytes : 0; }
+
+void mc_session_destroy(mc_session_h s) { freeSession(s); }
+
+int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st) {
+    mc_session_h s = nullptr;
+    int rc = mc_session_create(m, d, p, &s);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s->stream);
+    rc = mc_session_emit(s);
+    int done = 0;
+    while (!rc && !done) rc = mc_session_advance(s, 64, &done);
+    cudaEventRecord(e1, s->stream);
+    if (!rc) rc = mc_session_result(s, out, st);
+    float ms = 0.f;
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (st) st->kernel_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::string msg = g_err;
+    mc_session_destroy(s);
+    g_err = msg;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,24 @@
+// mc_launch.h -- host-side launch wrappers of the sm_103a kernels, one
+// instantiation per precision (mc_f32.cu, mc_f64.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mc_kernels.cuh"
+
+namespace mcg {
+
+template <typename R>
+cudaError_t launchEmit(const Params<R>& p, bool replay, cudaStream_t s);
+
+// tm: TM_SHARED or TM_GLOBAL
+template <typename R>
+cudaError_t launchAdvance(const Params<R>& p, bool replay, bool log, int tm, int grid, int block,
+                          size_t smem, cudaStream_t s);
+
+// Maximum resident blocks per SM of the advance kernel for this
+// configuration (0 if it cannot launch).
+template <typename R>
+int advanceOccupancy(bool replay, bool log, int tm, int block, size_t smem);
+
+}  // namespace mcg

@@ -1,0 +1,88 @@
+// mc_layout.h -- plain-old-data layouts shared by the host library and the
+// sm_103a kernels. No CUDA or torch types: the host side fills these in
+// FP64 and copies them (cast to the kernel's Real) to device memory.
+#pragma once
+
+#include <stdint.h>
+
+namespace mcg {
+
+// Face kinds, in the order of montecarlo/boundary.h:137-281.
+enum FaceKind { F_SPEC = 0, F_DIFF = 1, F_ISOT = 2, F_PERI = 3, F_INTER = 4 };
+
+// Tally problems (montecarlo/problem.h:157-203): rows 1, 3, 4.
+enum Problem { P_TEMP = 0, P_FLUX = 1, P_MULTI = 2 };
+
+// Reason a phonon stopped (device counters).
+enum Counter {
+    C_PHONON_STEPS = 0,  // live phonons x dt steps processed
+    C_EVENTS,            // completed loop iterations (flight + event)
+    C_SCATTERS,          // relaxation-time scatters
+    C_ESCAPES,           // numerical escapes / Inter misses
+    C_HORIZON,           // alive at the time horizon
+    C_MAXSCAT,           // stopped at nscat >= maxscat
+    C_MAXLOOP,           // stopped at maxloop iterations
+    C_ABSORBED,          // absorbed by an isothermal wall
+    C_REPLAY_EXHAUSTED,  // replay stream ran out
+    C_BAD,               // non-finite state (killed)
+    C_LIVE,              // live phonons written by the last launch
+    C_NCOUNTERS = 16
+};
+
+// Status bits returned to the host.
+enum Status {
+    S_OK = 0,
+    S_REPLAY_EXHAUSTED = 1,
+    S_NONFINITE = 2,
+    S_BAD_CELL = 4,
+};
+
+// One face of a Parallelepiped subdomain in reduced coordinates: face f
+// lies on axis f % 3 at u = 0 (f < 3) or u = S (f >= 3).
+template <typename R>
+struct FaceD {
+    int kind;
+    int to;       // destination subdomain (Peri / Inter), else -1
+    int toface;   // face of `to` the phonon arrives on
+    int ident;    // 1 if the Peri rotation is the identity
+    R n[3];       // inward unit normal (Spec reflection)
+    R rot[9];     // rotation z-hat -> n, row-major (Diff, Isot emission)
+    R Rd[9];      // Peri direction rotation, row-major
+    R A[9];       // reduced-coordinate map into subdomain `to`: u' = A u + b
+    R b[3];
+    R T;          // emission temperature after pairing (Isot / Peri)
+};
+
+template <typename R>
+struct SdomD {
+    R Minv[9];    // row-major inverse edge matrix
+    R M[9];       // row-major edge matrix
+    R o[3];       // origin
+    R S[3];       // shape as reals
+    R gradT[3];   // volumetric gradient (EmitSubdomain)
+    R grot[9];    // rotation z-hat -> gradT-hat
+    R eps;        // escape tolerance in path length
+    int shape[3];
+    int accum;    // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
+    int colbeg;   // first field column, -1 if the subdomain has none
+    int pad[3];
+    FaceD<R> f[6];
+};
+
+// Emitter: a volume (face = -1) or a face of a subdomain.
+struct EmitterD {
+    int sdom;
+    int face;
+};
+
+// Packed cell: 5-bit subdomain, three 9-bit cell indices.
+constexpr int CELL_BITS = 9;
+constexpr int MAX_SHAPE = 1 << CELL_BITS;
+constexpr int MAX_SDOM = 32;
+
+// Bytes moved per phonon per launch by the FP32 kernel's state (read once,
+// written once): three 16-byte words.
+constexpr int STATE_BYTES_F32 = 48;
+constexpr int STATE_BYTES_F64 = 80;
+
+}  // namespace mcg

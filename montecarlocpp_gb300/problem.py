@@ -1,0 +1,265 @@
+"""Host-side mirror of montecarlocpp's Material / Problem API over the C ABI.
+
+``Material(disp, relax, T)`` mirrors montecarlo/material.h:51-67;
+``TempProblem`` / ``FluxProblem`` / ``MultiProblem(mat, dom, nemit, maxscat,
+maxloop=0)`` mirror montecarlo/problem.h:157-203, and their ``solve()``
+replaces ``FieldProblem::solve`` (montecarlo/problem.cpp:370-445) for all
+phonons at once on the GPU. Results are rows x cols numpy arrays with the
+reference's row meaning: Temp (1 row), Flux (3 rows x, y, z), Multi (4 rows:
+temperature then flux).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from .domains import Domain
+from .materials import silicon_tables
+
+TEMP, FLUX, MULTI = 0, 1, 2
+TALLY_AUTO, TALLY_SHARED, TALLY_GLOBAL = -1, 0, 1
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Material:
+    """Material(disp, relax, T): dispersion + relaxation files, temperature."""
+
+    def __init__(self, disp=None, relax=None, T=300.0, *, tables=None):
+        L = _lib.lib()
+        h = C.c_void_p()
+        if tables is not None:
+            d, r = (np.ascontiguousarray(x, dtype=np.float64) for x in tables)
+            _lib.check(L.mc_material_create(_dp(d), d.shape[0], (d.shape[1] - 2) // 2, _dp(r), float(T),
+                                            C.byref(h)))
+            self.nw, self.np = d.shape[0], (d.shape[1] - 2) // 2
+        else:
+            if not (os.path.exists(disp) and os.path.exists(relax)):
+                raise FileNotFoundError("Error opening dispersion or relaxation time file")
+            _lib.check(L.mc_material_load(disp.encode(), relax.encode(), float(T), C.byref(h)))
+            with open(disp) as f:
+                nw, np_ = f.readline().split()[:2]
+            self.nw, self.np = int(nw), int(np_)
+        self.h = h
+        self.T = float(T)
+        self._sums = np.zeros(4)
+        _lib.check(L.mc_material_sums(self.h, _dp(self._sums)))
+
+    @classmethod
+    def silicon(cls, T=300.0, model=None):
+        return cls(T=T, tables=silicon_tables(model))
+
+    def temp(self):
+        return self.T
+
+    def cond(self):
+        return float(self._sums[3])
+
+    def energySum(self):
+        return float(self._sums[0])
+
+    def fluxSum(self):
+        return float(self._sums[1])
+
+    def scatSum(self):
+        return float(self._sums[2])
+
+    def tables(self):
+        vel = np.zeros((self.nw, self.np))
+        tau = np.zeros((self.nw, self.np))
+        _lib.check(_lib.lib().mc_material_tables(self.h, _dp(vel), _dp(tau)))
+        return vel, tau
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mc_material_destroy(self.h)
+            self.h = None
+
+
+def domain_descs(dom: Domain):
+    n = len(dom.ppeds)
+    ps = (_lib.PpedDesc * n)()
+    for i, p in enumerate(dom.ppeds):
+        ps[i].o[:] = [float(x) for x in p.o]
+        ps[i].M[:] = [float(x) for x in np.asarray(p.M, dtype=np.float64).reshape(-1)]
+        ps[i].div[:] = [int(x) for x in p.div]
+        ps[i].gradT[:] = [float(x) for x in p.gradT]
+        ps[i].kind[:] = [int(k) for k in p.kinds]
+        ps[i].T[:] = [float(t) for t in p.T]
+    m = len(dom.pairs)
+    qs = (_lib.PairDesc * max(m, 1))()
+    for i, q in enumerate(dom.pairs):
+        qs[i].kind, qs[i].sdom1, qs[i].face1, qs[i].sdom2, qs[i].face2 = q.kind, q.s1, q.f1, q.s2, q.f2
+        qs[i].transl[:] = [float(x) for x in q.transl]
+        qs[i].rot[:] = [float(x) for x in np.asarray(q.rot, dtype=np.float64).reshape(-1)]
+    return ps, n, qs, m
+
+
+class DomainHandle:
+    """The library's image of a Domain description."""
+
+    def __init__(self, dom: Domain):
+        L = _lib.lib()
+        ps, n, qs, m = domain_descs(dom)
+        h = C.c_void_p()
+        _lib.check(L.mc_domain_create(ps, n, qs, m, C.byref(h)))
+        self.h = h
+        self.dom = dom
+        self.cols = L.mc_domain_cols(h)
+
+    def cell_volumes(self):
+        out = np.zeros(self.cols)
+        _lib.check(_lib.lib().mc_domain_cell_volumes(self.h, _dp(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mc_domain_destroy(self.h)
+            self.h = None
+
+
+def _handle(dom):
+    if isinstance(dom, DomainHandle):
+        return dom
+    h = getattr(dom, "_mc_handle", None)
+    if h is None:
+        h = DomainHandle(dom)
+        dom._mc_handle = h
+    return h
+
+
+class FieldProblem:
+    """Common part of Temp/Flux/Multi problems (montecarlo/problem.h:121-147)."""
+
+    kind = MULTI
+    loopFactor = 100  # montecarlo/problem.h:124
+
+    def __init__(self, mat: Material, dom, nemit: int, maxscat: int, maxloop: int = 0):
+        if nemit <= 0 or maxscat <= 0 or maxloop < 0:
+            raise ValueError("Invalid problem arguments")
+        self.mat, self.dom = mat, dom
+        self.handle = _handle(dom)
+        self.nemit_requested, self.maxscat = int(nemit), int(maxscat)
+        self.maxloop = int(maxloop) if maxloop else self.loopFactor * int(maxscat)
+        self.stats = None
+
+    def rows(self):
+        return {TEMP: 1, FLUX: 3, MULTI: 4}[self.kind]
+
+    def desc(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
+             grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0, stream=None):
+        d = _lib.ProblemDesc()
+        d.problem, d.nemit, d.maxscat, d.maxloop = self.kind, self.nemit_requested, self.maxscat, self.maxloop
+        d.dt, d.nsteps, d.precision, d.seed = float(dt), int(nsteps), int(precision), int(seed)
+        d.steps_per_launch = int(steps_per_launch) if steps_per_launch else int(nsteps)
+        d.block_size, d.grid_blocks, d.tally_mode = int(block_size), int(grid_blocks), int(tally_mode)
+        keep = []
+        if replay is not None:
+            words, offsets = replay
+            words = np.ascontiguousarray(words, dtype=np.uint32)
+            offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+            keep += [words, offsets]
+            d.replay_words = words.ctypes.data_as(C.POINTER(C.c_uint32))
+            d.replay_offsets = offsets.ctypes.data_as(C.POINTER(C.c_int64))
+        log = None
+        if log_cap:
+            log = np.zeros((log_phonons, log_cap, 12))
+            counts = np.zeros(log_phonons, dtype=np.int64)
+            keep += [log, counts]
+            d.log = _dp(log)
+            d.log_counts = counts.ctypes.data_as(C.POINTER(C.c_int64))
+            d.log_cap, d.log_phonons = int(log_cap), int(log_phonons)
+            log = (log, counts)
+        d.stream = stream
+        return d, keep, log
+
+    def solve(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
+              grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0):
+        """Run every phonon on the GPU; returns the rows x cols field
+        (power * postProc(tally) / cellVol, montecarlo/problem.cpp:439-444).
+        With log_cap, ``self.log`` holds (records, counts)."""
+        d, keep, log = self.desc(dt=dt, nsteps=nsteps, seed=seed, precision=precision,
+                                 steps_per_launch=steps_per_launch, block_size=block_size,
+                                 grid_blocks=grid_blocks, tally_mode=tally_mode, replay=replay,
+                                 log_cap=log_cap, log_phonons=log_phonons)
+        out = np.zeros(self.rows() * self.handle.cols)
+        st = _lib.Stats()
+        _lib.check(_lib.lib().mc_solve(self.mat.h, self.handle.h, C.byref(d), _dp(out), C.byref(st)))
+        self.stats = st.as_dict()
+        if log is not None:
+            n = min(len(log[1]), st.nemit)
+            self.log = (log[0][:n], log[1][:n])
+        del keep
+        return out.reshape(self.rows(), self.handle.cols, order="F")
+
+    def session(self, **kw):
+        return Session(self, **kw)
+
+
+class TempProblem(FieldProblem):
+    kind = TEMP
+
+
+class FluxProblem(FieldProblem):
+    kind = FLUX
+
+
+class MultiProblem(FieldProblem):
+    kind = MULTI
+
+
+class Session:
+    """Device-resident run: emit once, advance in windows, read back."""
+
+    def __init__(self, prob: FieldProblem, **kw):
+        self.prob = prob
+        d, self._keep, self._log = prob.desc(**kw)
+        self.desc = d
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mc_session_create(prob.mat.h, prob.handle.h, C.byref(d), C.byref(h)))
+        self.h = h
+
+    def emit(self):
+        _lib.check(_lib.lib().mc_session_emit(self.h))
+
+    def advance(self, nlaunch: int) -> bool:
+        done = C.c_int(0)
+        _lib.check(_lib.lib().mc_session_advance(self.h, int(nlaunch), C.byref(done)))
+        return bool(done.value)
+
+    def run(self):
+        self.emit()
+        while not self.advance(1 << 20):
+            pass
+
+    def result(self, field=True):
+        st = _lib.Stats()
+        out = np.zeros(self.prob.rows() * self.prob.handle.cols) if field else None
+        _lib.check(_lib.lib().mc_session_result(self.h, _dp(out) if field else None, C.byref(st)))
+        r = out.reshape(self.prob.rows(), self.prob.handle.cols, order="F") if field else None
+        return r, st.as_dict()
+
+    def state_bytes(self):
+        return _lib.lib().mc_session_state_bytes(self.h)
+
+    def close(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mc_session_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def kappa_from_flux(field: np.ndarray, dom, axis: int = 0, flux_row0: int = 0) -> float:
+    """kappa = -<q_axis> / gradT_axis, volume-weighted over the cells."""
+    vols = _handle(dom).cell_volumes()
+    q = float(np.sum(field[flux_row0 + axis] * vols) / np.sum(vols))
+    g = float(dom.ppeds[0].gradT[axis])
+    return -q / g

@@ -1,0 +1,233 @@
+"""GPU parity tests: the sm_103a kernels, called through the C ABI, against
+the CPU oracle on the same inputs.
+
+Tolerances (stated per test):
+* trajectories, FP64 flight: loop index, subdomains, face hit, cell, nscat,
+  w, p identical; positions within 1e-12 of the domain size; times 1e-12
+  relative;
+* trajectories, FP32 flight: the same discrete fields identical; positions
+  within 1e-5 of the domain size;
+* fields, FP64 flight: within 1e-9 of each row's largest magnitude;
+* statistics: kappa within 3 standard errors of the oracle.
+"""
+
+import numpy as np
+import pytest
+
+import montecarlocpp_gb300 as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DISCRETE = [0, 1, 2, 3, 4, 9, 10, 11]
+
+
+def domains():
+    return {
+        "film": M.FilmDomain.from_cli(1e-7, 1e-7, 100),
+        "cross": M.CrossPlaneFilmDomain(1e-7, 1e-7, 20),
+        "bulk": M.BulkDomain.from_cli(1e-6, 10),
+        "pore": M.PoreCellDomain(5e-7, 2.5e-7),
+    }
+
+
+CASES = {
+    "film": (M.MULTI, 2000, 0.5e-12, 400),
+    "cross": (M.TEMP, 2000, 1e-12, 2000),
+    "bulk": (M.FLUX, 2000, 0.5e-12, 400),
+    "pore": (M.MULTI, 1500, 0.5e-12, 400),
+}
+PROBLEM = {M.TEMP: M.TempProblem, M.FLUX: M.FluxProblem, M.MULTI: M.MultiProblem}
+
+
+def run_pair(gmat, omat, dom, kind, nemit, dt, nsteps, prec, K, seed=7, maxscat=10**6, log_cap=512,
+             nlog=96, rng=O.RNG_PHILOX, replay=None, oracle_kw=None, **kw):
+    od = O.ODomain(dom)
+    o_out, o_st, ex = O.solve(omat, od, kind, nemit=nemit, maxscat=maxscat, dt=dt, horizon=dt * nsteps,
+                              rng=rng, seed=seed, log_cap=log_cap, log_phonons=nlog, **(oracle_kw or {}))
+    P = PROBLEM[kind](gmat, dom, nemit, maxscat)
+    if replay == "from_oracle":
+        replay = O.record_to_replay(ex["record"])
+    g_out = P.solve(dt=dt, nsteps=nsteps, seed=seed, precision=prec, steps_per_launch=K, log_cap=log_cap,
+                    log_phonons=nlog, replay=replay, **kw)
+    return (o_out, o_st, ex["log"]), (g_out, P.stats, P.log)
+
+
+def compare_logs(olog, glog, L, pos_tol, allow_mismatch=0):
+    (a_rec, a_cnt), (b_rec, b_cnt) = olog, glog
+    bad = 0
+    maxdx = 0.0
+    for i in range(min(len(a_cnt), len(b_cnt))):
+        n = int(min(a_cnt[i], b_cnt[i], a_rec.shape[1]))
+        a, b = a_rec[i, :n], b_rec[i, :n]
+        ok = a_cnt[i] == b_cnt[i] and np.array_equal(a[:, DISCRETE], b[:, DISCRETE])
+        if not ok:
+            bad += 1
+            continue
+        if n:
+            maxdx = max(maxdx, float(np.abs(a[:, 5:8] - b[:, 5:8]).max()) / L)
+            assert np.allclose(a[:, 8], b[:, 8], rtol=max(pos_tol, 1e-12), atol=0)
+    assert bad <= allow_mismatch, f"{bad} trajectories differ"
+    assert maxdx <= pos_tol, maxdx
+    return bad, maxdx
+
+
+def field_err(a, b):
+    scale = np.abs(a).max(axis=1, keepdims=True)
+    scale[scale == 0] = 1
+    return float((np.abs(a - b) / scale).max())
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("K", [1, 50, 100000])
+def test_fp64_trajectories_and_field(name, K, gmat, omat):
+    dom = domains()[name]
+    kind, nemit, dt, nsteps = CASES[name]
+    (oo, ost, olog), (go, gst, glog) = run_pair(gmat, omat, dom, kind, nemit, dt, nsteps, 64, K)
+    assert gst["nemit"] == ost["nemit"]
+    assert gst["events"] == ost["events"]
+    assert gst["scatters"] == ost["scatters"]
+    assert gst["absorbed"] == ost["absorbed"]
+    assert gst["horizon_stops"] == ost["horizon_stops"]
+    assert gst["phonon_steps"] == ost["phonon_steps"]
+    compare_logs(olog, glog, dom.max_dim(), 1e-12)
+    assert field_err(oo, go) < 1e-9
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp32_trajectories(name, gmat, omat):
+    dom = domains()[name]
+    kind, nemit, dt, nsteps = CASES[name]
+    (oo, ost, olog), (go, gst, glog) = run_pair(gmat, omat, dom, kind, nemit, dt, nsteps, 32, 50)
+    bad, _ = compare_logs(olog, glog, dom.max_dim(), 1e-5, allow_mismatch=1)
+    # the per-result FP32 error of the field against the FP64 oracle
+    assert field_err(oo, go) < 5e-3
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-12), (32, 1e-5)])
+def test_replay_of_reference_stream(prec, tol, gmat, omat):
+    """The oracle runs the reference's uniform scheme (mt19937 engines over
+    static phonon chunks, montecarlo/main.cpp:29-39,155-160), records the
+    32-bit words each phonon consumed; the GPU replays them."""
+    dom = domains()["film"]
+    (oo, ost, olog), (go, gst, glog) = run_pair(
+        gmat, omat, dom, M.MULTI, 1000, 0.5e-12, 300, prec, 37, seed=0, rng=O.RNG_MT, replay="from_oracle",
+        oracle_kw=dict(nchunk=4, record_cap=8192))
+    assert gst["status"] == 0
+    compare_logs(olog, glog, dom.max_dim(), tol, allow_mismatch=0 if prec == 64 else 1)
+    if prec == 64:
+        assert gst["events"] == ost["events"]
+        assert field_err(oo, go) < 1e-9
+
+
+def test_replay_exhausted_is_an_error(gmat):
+    dom = domains()["film"]
+    P = M.MultiProblem(gmat, dom, 100, 10**6)
+    n = 100
+    words = np.arange(3 * n, dtype=np.uint32) * 2654435761
+    offsets = np.arange(n + 1, dtype=np.int64) * 3
+    with pytest.raises(M.problem._lib.McError) as e:
+        P.solve(dt=0.5e-12, nsteps=200, precision=64, replay=(words, offsets))
+    assert e.value.code == -6
+
+
+def test_tally_layouts_agree(gmat):
+    dom = domains()["film"]
+    P = M.MultiProblem(gmat, dom, 5000, 10**6)
+    a = P.solve(dt=0.5e-12, nsteps=300, precision=64, steps_per_launch=30, tally_mode=0, seed=3)
+    b = P.solve(dt=0.5e-12, nsteps=300, precision=64, steps_per_launch=30, tally_mode=1, seed=3)
+    assert field_err(a, b) < 1e-12
+
+
+def test_launch_shape_does_not_change_results(gmat):
+    dom = domains()["pore"]
+    P = M.MultiProblem(gmat, dom, 3000, 10**6)
+    a = P.solve(dt=0.5e-12, nsteps=200, precision=64, steps_per_launch=200, block_size=256, seed=4)
+    ea = P.stats["events"]
+    b = P.solve(dt=0.5e-12, nsteps=200, precision=64, steps_per_launch=7, block_size=64, grid_blocks=13, seed=4)
+    assert P.stats["events"] == ea
+    assert field_err(a, b) < 1e-12
+
+
+def test_checksum_partition_of_unity_full_size(gmat):
+    """At the full in-plane film size (1e7 phonons, 4000 steps of 0.5 ps)
+    the raw tally summed over cells equals the sum over every flight of its
+    amount (the cell split loses nothing), and no phonon is lost."""
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 100)
+    P = M.MultiProblem(gmat, dom, 10_000_000, 10**6)
+    out = P.solve(dt=0.5e-12, nsteps=4000, precision=32, steps_per_launch=200, seed=11)
+    st = P.stats
+    assert st["horizon_stops"] == st["nemit"] and st["escapes"] == 0 and st["nonfinite"] == 0
+    assert st["phonon_steps"] == 4000 * st["nemit"]
+    vol = P.handle.cell_volumes()
+    raw = out * vol / st["power"]
+    raw[0] *= gmat.energySum()
+    for r in range(4):
+        # FP32 flight: each cell split rounds at 1e-7 of its flight
+        assert raw[r].sum() == pytest.approx(st["checksum"][r], rel=1e-6, abs=1e-6 * abs(raw[r]).sum())
+    kappa = M.kappa_from_flux(out, dom, 0, flux_row0=1)
+    assert 20 < kappa < 120
+
+
+def test_checksum_fp64(gmat):
+    dom = M.PoreCellDomain(5e-7, 2.5e-7)
+    P = M.MultiProblem(gmat, dom, 20000, 10**6)
+    out = P.solve(dt=0.5e-12, nsteps=500, precision=64, steps_per_launch=100, seed=12)
+    st = P.stats
+    raw = out * P.handle.cell_volumes() / st["power"]
+    raw[0] *= gmat.energySum()
+    for r in range(4):
+        assert raw[r].sum() == pytest.approx(st["checksum"][r], rel=1e-11, abs=1e-11 * abs(raw[r]).sum())
+
+
+def test_kappa_statistical_parity(gmat, omat):
+    """FP32 GPU (Philox) against the FP64 oracle run with the reference's
+    mt19937 scheme: kappa of the 100 nm film within 3 standard errors."""
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 20)
+    od = O.ODomain(dom)
+    dt, nsteps = 0.5e-12, 1000
+    ko, kg = [], []
+    for s in range(6):
+        o, _, _ = O.solve(omat, od, O.MULTI, nemit=20000, maxscat=10**6, dt=dt, horizon=dt * nsteps,
+                          rng=O.RNG_MT, nchunk=8, seed=100 * s)
+        ko.append(M.kappa_from_flux(o, dom, 0, flux_row0=1))
+    P = M.MultiProblem(gmat, dom, 20000, 10**6)
+    for s in range(6):
+        g = P.solve(dt=dt, nsteps=nsteps, precision=32, steps_per_launch=100, seed=1000 + s)
+        kg.append(M.kappa_from_flux(g, dom, 0, flux_row0=1))
+    ko, kg = np.array(ko), np.array(kg)
+    se = np.sqrt(ko.var(ddof=1) / len(ko) + kg.var(ddof=1) / len(kg))
+    assert abs(ko.mean() - kg.mean()) < 3 * se
+
+
+def test_edge_cases(gmat, omat):
+    film = domains()["film"]
+    # one requested phonon
+    P = M.TempProblem(gmat, film, 1, 10)
+    P.solve(dt=1e-12, nsteps=5, precision=64)
+    assert P.stats["nemit"] == 1
+    # maxscat = 1 stops every phonon at its first scatter
+    P = M.FluxProblem(gmat, film, 500, 1)
+    P.solve(dt=1e-12, nsteps=10**6, precision=64, steps_per_launch=10**6)
+    st = P.stats
+    assert st["maxscat_stops"] + st["maxloop_stops"] == st["nemit"]
+    # one step only
+    P = M.MultiProblem(gmat, film, 500, 10**6)
+    P.solve(dt=1e-12, nsteps=1, precision=32)
+    assert P.stats["phonon_steps"] == P.stats["nemit"] == P.stats["horizon_stops"]
+    # isothermal walls absorb everything given time
+    cross = domains()["cross"]
+    P = M.TempProblem(gmat, cross, 2000, 10**6)
+    P.solve(dt=1e-12, nsteps=200000, precision=32, steps_per_launch=5000)
+    st = P.stats
+    assert st["absorbed"] + st["horizon_stops"] == st["nemit"] and st["absorbed"] > 0.99 * st["nemit"]
+
+
+def test_determinism(gmat):
+    dom = domains()["pore"]
+    P = M.MultiProblem(gmat, dom, 20000, 10**6)
+    a = P.solve(dt=0.5e-12, nsteps=300, precision=32, steps_per_launch=30, seed=9)
+    ea = P.stats["events"]
+    b = P.solve(dt=0.5e-12, nsteps=300, precision=32, steps_per_launch=30, seed=9)
+    assert P.stats["events"] == ea
+    assert field_err(a, b) < 1e-10

@@ -1,0 +1,217 @@
+"""CPU tests of the oracle: RNG known answers, samplers, material tables,
+Field::accumulate partition of unity, the bulk-conductivity known answer and
+the committed golden fixtures."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == \
+        [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_mt19937_known_answer():
+    # the C++ standard's check value for mt19937 (10000th output, seed 5489)
+    assert O.mt19937_nth(5489, 10000) == 4123659995
+
+
+def _grid_words(n):
+    return ((np.arange(n, dtype=np.float64) + 0.5) * (2**32 / n)).astype(np.uint64).astype(np.uint32)
+
+
+def test_draw_iso_moments():
+    xs = _grid_words(256)
+    v = np.array([O.draw_iso(int(a), int(b)) for a in xs for b in xs[::16]])
+    assert np.allclose(np.linalg.norm(v, axis=1), 1.0, atol=1e-14)
+    assert abs(v[:, 2].mean()) < 1e-3
+    assert abs((v[:, 2] ** 2).mean() - 1 / 3) < 2e-3
+
+
+def test_draw_aniso_moments():
+    xs = _grid_words(512)
+    v = np.array([O.draw_aniso(int(a), int(b), False) for a in xs for b in xs[::32]])
+    assert (v[:, 2] >= 0).all()
+    assert abs(v[:, 2].mean() - 2 / 3) < 2e-3  # cosine (Lambertian) law
+    vb = np.array([O.draw_aniso(int(a), int(b), True) for a in xs for b in xs[::32]])
+    assert abs(vb[:, 2].mean()) < 2e-3
+    assert abs(np.abs(vb[:, 2]).mean() - 2 / 3) < 2e-3
+
+
+@pytest.mark.parametrize("n", [(0, 0, 1), (1, 0, 0), (0, -1, 0), (0, 0, -1), (1, 2, -3)])
+def test_rotation_z_to_n(n):
+    n = np.array(n, dtype=float)
+    n /= np.linalg.norm(n)
+    R = O.rot_z_to(n)
+    assert np.allclose(R @ np.array([0, 0, 1.0]), n, atol=1e-15)
+    assert np.allclose(R @ R.T, np.eye(3), atol=1e-15)
+    assert abs(np.linalg.det(R) - 1) < 1e-14
+
+
+def test_material_matches_library(si_tables, omat):
+    import montecarlocpp_gb300 as M
+    m = M.Material(T=300.0, tables=si_tables)
+    s = omat.sums()
+    assert m.energySum() == pytest.approx(s["energySum"], rel=1e-13)
+    assert m.fluxSum() == pytest.approx(s["fluxSum"], rel=1e-13)
+    assert m.scatSum() == pytest.approx(s["scatSum"], rel=1e-13)
+    assert m.cond() == pytest.approx(s["cond"], rel=1e-13)
+    vel, tau = m.tables()
+    assert np.array_equal(vel, si_tables[0][:, 2::2])
+    assert np.isfinite(tau).all() and (tau > 0).all()
+
+
+def test_material_files_roundtrip(tmp_path, si_tables):
+    import montecarlocpp_gb300 as M
+    from montecarlocpp_gb300.materials import read_material_files
+    d, r = M.write_material_files(str(tmp_path))
+    disp, relax = read_material_files(d, r)
+    assert np.array_equal(disp, si_tables[0]) and np.array_equal(relax, si_tables[1])
+    a = M.Material(d, r, 300.0)
+    b = O.OMaterial(paths=(d, r), T=300.0)
+    assert a.cond() == pytest.approx(b.sums()["cond"], rel=1e-13)
+
+
+def test_inverse_cdf_draws(omat, si_tables):
+    # reimplementation of the two-level inverse-CDF search in numpy
+    disp, _ = si_tables
+    rng = np.random.default_rng(0)
+    # flux pdf rows from the oracle's own tables are not exported; check
+    # structural properties instead: zero-DOS branches are never drawn
+    dos = disp[:, 3::2]
+    for _ in range(2000):
+        x1, x2 = (int(v) for v in rng.integers(0, 2**32, 2))
+        w, p = omat.draw(1, x1, x2)
+        assert 0 <= w < disp.shape[0] and 0 <= p < 3
+        assert dos[w, p] > 0
+    # monotone in the first word
+    ws = [omat.draw(2, int(x), 0)[0] for x in np.linspace(0, 2**32 - 1, 200)]
+    assert all(a <= b for a, b in zip(ws, ws[1:]))
+
+
+def _random_segment(rng, dom, s):
+    p = dom.ppeds[s]
+    a = p.o + p.M @ rng.random(3)
+    b = p.o + p.M @ rng.random(3)
+    return a, b
+
+
+@pytest.mark.parametrize("dom_name", ["film", "pore", "cross", "bulk"])
+def test_accumulate_partition_of_unity(dom_name):
+    import montecarlocpp_gb300 as M
+    dom = {"film": M.FilmDomain.from_cli(1e-7, 1e-7, 37),
+           "pore": M.PoreCellDomain(5e-7, 2.5e-7, (3, 5, 4)),
+           "cross": M.CrossPlaneFilmDomain(1e-7, 1e-7, 20),
+           "bulk": M.BulkDomain((1e-7, 2e-7, 3e-7), (4, 5, 6), 1e-1)}[dom_name]
+    od = O.ODomain(dom)
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        s = int(rng.integers(len(dom.ppeds)))
+        a, b = _random_segment(rng, dom, s)
+        amount = rng.normal(size=4)
+        data = od.accumulate(s, a, b, amount, np.zeros((4, od.cols)))
+        assert np.allclose(data.sum(axis=1), amount, rtol=1e-11, atol=1e-14)
+
+
+def test_accumulate_1d_closed_form():
+    import montecarlocpp_gb300 as M
+    dom = M.CrossPlaneFilmDomain(10.0, 1.0, 10)
+    od = O.ODomain(dom)
+    data = od.accumulate(0, [0.5, 0.2, 0.2], [3.5, 0.7, 0.3], np.array([3.0]), np.zeros((1, 10)))
+    assert np.allclose(data[0], [0.5, 1, 1, 0.5, 0, 0, 0, 0, 0, 0])
+
+
+def test_bulk_conductivity_known_answer(omat):
+    """Bulk flux with the volumetric gradient source recovers
+    Material::cond() = sum tau v^2 C / 3 (montecarlo/material.cpp:233)."""
+    import montecarlocpp_gb300 as M
+    dom = M.BulkDomain.from_cli(1e-3, 1)
+    od = O.ODomain(dom)
+    ks = []
+    for seed in range(6):
+        out, st, _ = O.solve(omat, od, O.FLUX, nemit=60000, maxscat=1, maxloop=10**7, rng=O.RNG_PHILOX,
+                             seed=seed)
+        ks.append(out[0].mean() / 1e6)
+    ks = np.array(ks)
+    se = ks.std(ddof=1) / np.sqrt(len(ks))
+    cond = omat.sums()["cond"]
+    assert abs(ks.mean() - cond) < 4 * se + 0.01 * cond
+
+
+def test_emitter_rounding(omat):
+    """montecarlo/problem.cpp:329-337: n_i = max(1, round(w_i / W * nemit))."""
+    import montecarlocpp_gb300 as M
+    dom = M.PoreCellDomain(5e-7, 2.5e-7, (2, 3, 2))
+    od = O.ODomain(dom)
+    _, st, _ = O.solve(omat, od, O.TEMP, nemit=1000, maxscat=1, dt=1e-12, horizon=1e-12)
+    vols = np.array([np.prod(np.diag(p.M)) for p in dom.ppeds])
+    n = np.maximum(1, np.ceil(vols / vols.sum() * 1000 - 0.5)).astype(int)
+    assert st["nemit"] == n.sum()
+
+
+def test_film_builder_matches_reference_restatement(omat):
+    """The package's FilmDomain description equals the oracle's own
+    restatement of montecarlo/domain.cpp:188-199."""
+    import montecarlocpp_gb300 as M
+    a = O.ODomain(M.FilmDomain((1e-7, 5e-8, 1e-7), (0, 25, 0), 0.1))
+    b = O.ODomain.film(1e-7, 5e-8, 1e-7, 25, 0.1)
+    ra, sa, _ = O.solve(omat, a, O.MULTI, nemit=3000, maxscat=100, dt=1e-12, horizon=2e-10, seed=5)
+    rb, sb, _ = O.solve(omat, b, O.MULTI, nemit=3000, maxscat=100, dt=1e-12, horizon=2e-10, seed=5)
+    assert sa["events"] == sb["events"]
+    assert np.allclose(ra, rb, rtol=0, atol=1e-12 * np.abs(ra).max())
+    c = O.ODomain(M.BulkDomain.from_cli(1e-7, 5))
+    d = O.ODomain.bulk(1e-7, 5, 1e6 * 1e-7)
+    rc, _, _ = O.solve(omat, c, O.FLUX, nemit=2000, maxscat=10, seed=2)
+    rd, _, _ = O.solve(omat, d, O.FLUX, nemit=2000, maxscat=10, seed=2)
+    assert np.allclose(rc, rd, rtol=0, atol=1e-12 * np.abs(rc).max())
+
+
+def test_replay_reproduces_recorded_stream(omat):
+    """The reference scheme (per-thread mt19937, static chunks) recorded per
+    phonon and fed back as a replay stream gives the same trajectories."""
+    import montecarlocpp_gb300 as M
+    od = O.ODomain(M.FilmDomain.from_cli(1e-7, 1e-7, 20))
+    kw = dict(nemit=300, maxscat=10**6, dt=0.5e-12, horizon=0.5e-12 * 300)
+    a, sa, ea = O.solve(omat, od, O.MULTI, rng=O.RNG_MT, nchunk=4, seed=0, record_cap=4096, log_cap=256,
+                        log_phonons=300, **kw)
+    rep = O.record_to_replay(ea["record"])
+    b, sb, eb = O.solve(omat, od, O.MULTI, rng=O.RNG_REPLAY, replay=rep, log_cap=256, log_phonons=300, **kw)
+    assert sb["replay_exhausted"] == 0
+    assert sa["events"] == sb["events"]
+    assert np.array_equal(ea["log"][1], eb["log"][1])
+    assert np.allclose(a, b, rtol=0, atol=1e-12 * np.abs(a).max())
+
+
+def test_horizon_stops_everything(omat):
+    import montecarlocpp_gb300 as M
+    od = O.ODomain(M.FilmDomain.from_cli(1e-7, 1e-7, 10))
+    _, st, _ = O.solve(omat, od, O.TEMP, nemit=500, maxscat=10**6, dt=1e-12, horizon=50e-12)
+    assert st["horizon_stops"] == st["nemit"]
+    assert st["phonon_steps"] == 50 * st["nemit"]
+
+
+@pytest.mark.parametrize("name", ["oracle_film_multi", "oracle_cross_temp", "oracle_pore_multi"])
+def test_golden_fixtures(name, omat):
+    """Oracle outputs committed by tests/golden/make_golden.py; pins the
+    oracle across compilers and machines (x86 here, Arm on the GPU machine)."""
+    from tests.golden.make_golden import CASES, run_case
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        ref = json.load(f)
+    got = run_case(CASES[name], omat)
+    for k in ("nemit", "events", "scatters", "absorbed", "horizon_stops"):
+        assert got["stats"][k] == ref["stats"][k], k
+    a, b = np.array(got["field"]), np.array(ref["field"])
+    assert np.allclose(a, b, rtol=0, atol=1e-12 * np.abs(b).max())
+    assert got["log_counts"] == ref["log_counts"]
+    for ga, ra in zip(got["log"], ref["log"]):
+        assert np.allclose(np.array(ga), np.array(ra), rtol=1e-13, atol=1e-22)
