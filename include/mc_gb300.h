@@ -126,7 +126,14 @@ typedef struct {
     long log_cap;
     long log_phonons;
     void* stream;           /* cudaStream_t; NULL -> library stream        */
+    int schedule;           /* MC_SCHED_*: static one-phonon-per-thread
+                               passes with front/back compaction, or
+                               dynamic lane refill with in-place state     */
+    int compact_interval;   /* dynamic schedule: compact dead slots every
+                               this many launches (0: never)               */
 } mc_problem_desc;
+
+enum { MC_SCHED_AUTO = 0, MC_SCHED_STATIC = 1, MC_SCHED_DYNAMIC = 2 };
 
 typedef struct {
     long nemit;             /* phonons after rounding                      */

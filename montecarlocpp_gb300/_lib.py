@@ -36,7 +36,8 @@ class ProblemDesc(C.Structure):
                 ("block_size", C.c_int), ("grid_blocks", C.c_int), ("tally_mode", C.c_int),
                 ("replay_words", C.POINTER(C.c_uint32)), ("replay_offsets", C.POINTER(C.c_int64)),
                 ("log", C.POINTER(C.c_double)), ("log_counts", C.POINTER(C.c_int64)),
-                ("log_cap", C.c_long), ("log_phonons", C.c_long), ("stream", C.c_void_p)]
+                ("log_cap", C.c_long), ("log_phonons", C.c_long), ("stream", C.c_void_p),
+                ("schedule", C.c_int), ("compact_interval", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -38,14 +38,14 @@ def _time_config(prob, W, stream, nemit, nsteps, K, block, tally, precision=32, 
     return best
 
 
-def tune(prob, W, stream, Ks=(20, 50, 100, 200, 400, 1000), blocks=(128, 256), tallies=(0,),
+def tune(prob, W, stream, Ks=(50, 200, 1000, 4000), blocks=(128, 256), tallies=(0,),
          nemit=None, nsteps=None, precision=32, budget_s=60.0):
     """Return (best config dict, list of (config, rate))."""
     key = (type(prob.dom).__name__, tuple(sorted((k, str(v)) for k, v in W.items())), precision)
     if key in _cache:
         return _cache[key]
-    nemit = nemit or min(W["nemit"], 2_000_000)
-    nsteps = nsteps or min(W["nsteps"], 1000)
+    nemit = nemit or min(W["nemit"], 1_000_000)
+    nsteps = nsteps or W["nsteps"]
     results = []
     t0 = time.time()
     for K, b, t in itertools.product(Ks, blocks, tallies):

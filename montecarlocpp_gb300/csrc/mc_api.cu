@@ -355,8 +355,6 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             S.o[k] = p.o[k];
             if (p.div[k] < 0) neg = true;
             if (p.div[k] > 0) ++npos;
-            S.shape[k] = (int)std::max(p.div[k], 1L);
-            S.S[k] = S.shape[k];
             S.gradT[k] = p.gradT[k];
         }
         // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
@@ -364,6 +362,18 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         else if (npos == 0) S.accum = -1;
         else if (npos == 1) { int d = 0; for (int k = 1; k < 3; ++k) if (p.div[k] > p.div[d]) d = k; S.accum = d; }
         else S.accum = npos + 1;
+        // walk cells: the tally cells, refined to WALK_CELLS on axes without
+        // tally cells when the field is 0-D or 1-D
+        int tsh[3];
+        for (int k = 0; k < 3; ++k) {
+            tsh[k] = (int)std::max(p.div[k], 1L);
+            const bool virt = neg || (p.div[k] <= 0 && S.accum <= 2);
+            S.shape[k] = virt ? WALK_CELLS : tsh[k];
+            S.S[k] = S.shape[k];
+        }
+        S.tstride[0] = (!neg && p.div[0] > 0) ? 1 : 0;
+        S.tstride[1] = (!neg && p.div[1] > 0) ? tsh[0] : 0;
+        S.tstride[2] = (!neg && p.div[2] > 0) ? tsh[0] * tsh[1] : 0;
         M3 gr = rotZTo(unit(mk(p.gradT[0], p.gradT[1], p.gradT[2])));
         std::memcpy(S.grot, gr.m, sizeof(gr.m));
         double maxn = 0.;
@@ -378,7 +388,7 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             D->em.push_back(EmitterD{s, f});
             D->emWeight.push_back(F.area * std::fabs(F.T));  // montecarlo/boundary.cpp:413-416
         }
-        long sp = neg ? 0 : (long)S.shape[0] * S.shape[1] * S.shape[2];
+        long sp = neg ? 0 : (long)tsh[0] * tsh[1] * tsh[2];
         if (sp == 0) { S.colbeg = -1; D->colbeg.push_back(-1); continue; }
         S.colbeg = (int)cols;
         D->colbeg.push_back(cols);
@@ -422,6 +432,18 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
                 V3 b = mvec(Mi2, x0);
                 std::memcpy(G.A, A.m, sizeof(A.m));
                 for (int k = 0; k < 3; ++k) G.b[k] = T2.S[k] * b[k];
+                // tangential identity: same axis, A = I and no tangential
+                // shift (within rounding of the FP64 products)
+                const int ax = f % 3;
+                bool tang = (F.pairF % 3) == ax;
+                for (int i = 0; i < 3 && tang; ++i) {
+                    if (i == ax) continue;  // the normal coordinate is snapped
+                    for (int j = 0; j < 3; ++j)
+                        if (std::fabs(A.m[3 * i + j] - (i == j ? 1. : 0.)) > 1e-12) tang = false;
+                }
+                for (int k = 0; k < 3 && tang; ++k)
+                    if (k != ax && std::fabs(G.b[k]) > 1e-12 * T2.S[k]) tang = false;
+                G.tang = tang ? 1 : 0;
             }
         }
     }
@@ -433,7 +455,10 @@ template <typename R>
 void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
     std::memset(&b, 0, sizeof(b));
     for (int i = 0; i < 9; ++i) { b.Minv[i] = (R)a.Minv[i]; b.M[i] = (R)a.M[i]; b.grot[i] = (R)a.grot[i]; }
-    for (int i = 0; i < 3; ++i) { b.o[i] = (R)a.o[i]; b.S[i] = (R)a.S[i]; b.gradT[i] = (R)a.gradT[i]; b.shape[i] = a.shape[i]; }
+    for (int i = 0; i < 3; ++i) {
+        b.o[i] = (R)a.o[i]; b.S[i] = (R)a.S[i]; b.gradT[i] = (R)a.gradT[i];
+        b.shape[i] = a.shape[i]; b.tstride[i] = a.tstride[i];
+    }
     // escape tolerance: 100 ulp of the largest edge in the flight precision
     b.eps = (R)(f32 ? a.eps / DEPS * (double)std::numeric_limits<float>::epsilon() : a.eps);
     b.accum = a.accum;
@@ -441,7 +466,7 @@ void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
     for (int f = 0; f < 6; ++f) {
         const FaceD<double>& x = a.f[f];
         FaceD<R>& y = b.f[f];
-        y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident;
+        y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident; y.tang = x.tang;
         for (int i = 0; i < 3; ++i) { y.n[i] = (R)x.n[i]; y.b[i] = (R)x.b[i]; }
         for (int i = 0; i < 9; ++i) { y.rot[i] = (R)x.rot[i]; y.Rd[i] = (R)x.Rd[i]; y.A[i] = (R)x.A[i]; }
         y.T = (R)x.T;
@@ -457,6 +482,8 @@ struct mc_session_s {
     mc_problem_desc desc{};
     int prec = 32;
     bool replay = false, logging = false;
+    bool dyn = false;
+    int sinceCompact = 0;
     int tm = TM_SHARED;
     int block = 256, grid = 0;
     size_t smem = 0;
@@ -487,6 +514,7 @@ struct mc_session_s {
     double* log_d = nullptr;
     int* logcnt_d = nullptr;
     int parity = 0;               // which half holds the live phonons
+    double vmax = 0.;             // largest group velocity of the material
     Params<float> p32{};
     Params<double> p64{};
 };
@@ -504,6 +532,8 @@ int setupSession(mc_session_s* S) {
     char* base = (char*)S->tables;
     std::vector<R> vel(nt), vt(nt);
     for (size_t i = 0; i < nt; ++i) { vel[i] = (R)m.vel[i]; vt[i] = (R)(m.vel[i] * m.tau[i]); }
+    S->vmax = 0.;
+    for (size_t i = 0; i < nt; ++i) S->vmax = std::max(S->vmax, m.vel[i]);
     Params<R> P{};
     P.vel = (R*)base; base += sizeof(R) * nt;
     P.vt = (R*)base; base += sizeof(R) * nt;
@@ -562,8 +592,8 @@ int setupSession(mc_session_s* S) {
         h1[h] = (V4*)sb; sb += al(sizeof(V4) * n);
         h2[h] = (uint4*)sb; sb += al(sizeof(uint4) * n);
     }
-    // counters: C_NCOUNTERS + 2 live counts
-    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 2)));
+    // counters: C_NCOUNTERS + two (front, back) live-count pairs
+    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
     CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
     S->rows = S->desc.problem == MC_TEMP ? 1 : (S->desc.problem == MC_FLUX ? 3 : 4);
     CK(cudaMalloc(&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L)));
@@ -577,6 +607,7 @@ int setupSession(mc_session_s* S) {
     P.key0 = (uint32_t)S->desc.seed;
     P.key1 = (uint32_t)(S->desc.seed >> 32);
     P.counters = S->cnt_d;
+    P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;
     CK(cudaMalloc(&S->csum_d, sizeof(double) * 4));
@@ -612,7 +643,7 @@ int setupSession(mc_session_s* S) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    int occ = advanceOccupancy<R>(S->replay, S->logging, S->tm, S->block, S->smem);
+    int occ = advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
     // halves
@@ -640,7 +671,7 @@ int emitT(mc_session_s* S) {
     if (S->parity == 1) { a0 = P.P0out; a1 = P.P1out; a2 = P.P2out; }
     Params<R> E = P;
     E.P0out = a0; E.P1out = a1; E.P2out = a2;
-    CK(cudaMemsetAsync(S->cnt_d, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 2), S->stream));
+    CK(cudaMemsetAsync(S->cnt_d, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), S->stream));
     CK(cudaMemsetAsync(S->status_d, 0, sizeof(unsigned int), S->stream));
     CK(cudaMemsetAsync(S->csum_d, 0, sizeof(double) * 4, S->stream));
     CK(cudaMemsetAsync(S->tally_d, 0, sizeof(double) * (size_t)S->rows * std::max(S->dom->cols, 1L), S->stream));
@@ -649,14 +680,33 @@ int emitT(mc_session_s* S) {
         CK(cudaMemsetAsync(S->logcnt_d, 0, sizeof(int) * std::min<long long>(S->desc.log_phonons, S->nemit), S->stream));
         CK(cudaMemsetAsync(S->log_d, 0xFF, sizeof(double) * 12 * (size_t)std::min<long long>(S->desc.log_phonons, S->nemit) * S->desc.log_cap, S->stream));
     }
-    // live count of the emitted half
+    // live counts of the emitted half: all in front
     unsigned long long n = (unsigned long long)S->nemit;
-    CK(cudaMemcpyAsync(S->cnt_d + C_NCOUNTERS + S->parity, &n, sizeof(n), cudaMemcpyHostToDevice, S->stream));
+    CK(cudaMemcpyAsync(S->cnt_d + C_NCOUNTERS + 2 * S->parity, &n, sizeof(n), cudaMemcpyHostToDevice, S->stream));
     CK(launchEmit<R>(E, S->replay, S->stream));
     CK(cudaStreamSynchronize(S->stream));  // n lives on the host stack
     S->step = 0;
     S->launches = 1;
     return MC_OK;
+}
+
+// Fixed-point quantum of the per-block shared tally: a block's partial of
+// any cell is bounded by (phonons the block handles) x (largest amount one
+// phonon can add in a window: the window itself for time rows, vmax x
+// window for displacement rows); 2^-61 of that bound keeps every partial
+// and difference entry inside int64.
+template <typename R>
+void setQuanta(const mc_session_s* S, Params<R>& P) {
+    const int keff = (int)std::min<long>(S->desc.steps_per_launch, S->desc.nsteps - S->step);
+    const double window = (double)keff * S->desc.dt;
+    const double perBlock = std::ceil((double)S->nemit / ((double)S->grid * S->block)) * S->block;
+    for (int r = 0; r < 4; ++r) {
+        const bool timeRow = (S->desc.problem == MC_TEMP && r == 0) || (S->desc.problem == MC_MULTI && r == 0);
+        const double bound = perBlock * window * (timeRow ? 1.0 : S->vmax) * 1.0001;
+        const double q = std::ldexp(bound, -61);
+        P.tq[r] = q;
+        P.tqinv[r] = (R)(1.0 / q);
+    }
 }
 
 template <typename R>
@@ -668,14 +718,43 @@ int advanceT(mc_session_s* S, int nl, int* done) {
         if (S->parity == 1) {
             std::swap(P.P0in, P.P0out); std::swap(P.P1in, P.P1out); std::swap(P.P2in, P.P2out);
         }
-        P.nlive_in = S->cnt_d + C_NCOUNTERS + S->parity;
-        P.nlive_out = S->cnt_d + C_NCOUNTERS + (S->parity ^ 1);
         P.step0 = S->step;
-        CK(cudaMemsetAsync(P.nlive_out, 0, sizeof(unsigned long long), S->stream));
-        CK(launchAdvance<R>(P, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
-        S->parity ^= 1;
-        S->step += S->desc.steps_per_launch;
-        S->launches++;
+        setQuanta(S, P);
+        unsigned long long* cur = S->cnt_d + C_NCOUNTERS + 2 * S->parity;
+        unsigned long long* oth = S->cnt_d + C_NCOUNTERS + 2 * (S->parity ^ 1);
+        if (S->dyn) {
+            // in place: slots [0, cur[0]) of the current half, survivors
+            // counted in cur[1]
+            P.P0out = P.P0in; P.P1out = P.P1in; P.P2out = P.P2in;
+            P.live_in = cur;
+            P.live_out = cur + 1;
+            CK(cudaMemsetAsync(cur + 1, 0, sizeof(unsigned long long), S->stream));
+            CK(launchAdvance<R>(P, true, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+            S->launches++;
+            S->step += S->desc.steps_per_launch;
+            if (S->desc.compact_interval > 0 && ++S->sinceCompact >= S->desc.compact_interval &&
+                S->step < nsteps) {
+                Params<R> Q = P0;
+                if (S->parity == 1) {
+                    std::swap(Q.P0in, Q.P0out); std::swap(Q.P1in, Q.P1out); std::swap(Q.P2in, Q.P2out);
+                }
+                Q.live_in = cur;
+                Q.live_out = oth;
+                CK(cudaMemsetAsync(oth, 0, 2 * sizeof(unsigned long long), S->stream));
+                CK(launchCompact<R>(Q, S->grid, S->stream));
+                S->launches++;
+                S->parity ^= 1;
+                S->sinceCompact = 0;
+            }
+        } else {
+            P.live_in = cur;
+            P.live_out = oth;
+            CK(cudaMemsetAsync(oth, 0, 2 * sizeof(unsigned long long), S->stream));
+            CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+            S->parity ^= 1;
+            S->step += S->desc.steps_per_launch;
+            S->launches++;
+        }
     }
     if (done) *done = S->step >= nsteps ? 1 : 0;
     return MC_OK;
@@ -685,7 +764,7 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
     CK(cudaStreamSynchronize(S->stream));
     const mc_domain_s& D = *S->dom;
     const mc_material_s& m = *S->mat;
-    std::vector<unsigned long long> c(C_NCOUNTERS + 2);
+    std::vector<unsigned long long> c(C_NCOUNTERS + 4);
     unsigned int status = 0;
     CK(cudaMemcpy(c.data(), S->cnt_d, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&status, S->status_d, sizeof(status), cudaMemcpyDeviceToHost));
@@ -818,6 +897,8 @@ int mc_session_create(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, 
     S->prec = p->precision;
     S->replay = p->replay_words != nullptr;
     S->logging = p->log != nullptr;
+    if (p->schedule < MC_SCHED_AUTO || p->schedule > MC_SCHED_DYNAMIC) { delete S; return fail(MC_ERR_ARG, "invalid schedule"); }
+    S->dyn = p->schedule == MC_SCHED_DYNAMIC || (p->schedule == MC_SCHED_AUTO && p->steps_per_launch > 1);
     S->maxloop = p->maxloop != 0 ? p->maxloop : 100 * p->maxscat;
     if (p->stream) S->stream = (cudaStream_t)p->stream;
     else {

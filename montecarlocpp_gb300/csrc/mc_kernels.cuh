@@ -69,8 +69,17 @@ struct Params {
     // state (ping-pong halves chosen by the host)
     typename Vec4<R>::T* P0in; typename Vec4<R>::T* P1in; uint4* P2in;
     typename Vec4<R>::T* P0out; typename Vec4<R>::T* P1out; uint4* P2out;
-    const unsigned long long* nlive_in;
-    unsigned long long* nlive_out;
+    // live phonons: the input holds [0, live_in[0]) and
+    // [cap - live_in[1], cap); survivors whose next event falls inside the
+    // next window are written from the front of the output, the others
+    // from the back, so that warps see phonons of one kind
+    const unsigned long long* live_in;
+    unsigned long long* live_out;
+    unsigned long long cap;
+    // fixed-point quantum of the per-block shared tally and of the
+    // per-thread checksums, per row
+    R tqinv[4];
+    double tq[4];
     unsigned long long* counters;
     unsigned int* status;
     double* tally;  // rows x cols, column-major
@@ -151,13 +160,17 @@ template <> struct Rng<true> {
 };
 
 // Uniform conversions. FP64 follows boost's uniform_01 / uniform_real on a
-// 32-bit engine exactly (u = x / 2^32); FP32 keeps the top 24 bits.
+// 32-bit engine exactly (u = x / 2^32); FP32 rounds the exact value once
+// (u01 keeps the top 24 bits so that it stays below 1).
 template <typename R> __device__ __forceinline__ R u01(uint32_t x);
 template <> __device__ __forceinline__ double u01<double>(uint32_t x) { return (double)x * 0x1p-32; }
 template <> __device__ __forceinline__ float u01<float>(uint32_t x) { return (float)(x >> 8) * 0x1p-24f; }
 template <typename R> __device__ __forceinline__ R uone(uint32_t x);
 template <> __device__ __forceinline__ double uone<double>(uint32_t x) { return (double)x * 0x1p-32 * 2.0 + (-1.0); }
-template <> __device__ __forceinline__ float uone<float>(uint32_t x) { return (float)(x >> 8) * 0x1p-23f - 1.0f; }
+template <> __device__ __forceinline__ float uone<float>(uint32_t x) {
+    // 2u - 1 = (2x - 2^32) / 2^32, rounded once
+    return __ll2float_rn(2LL * (long long)x - 0x100000000LL) * 0x1p-32f;
+}
 // -log(1 - u) with 1 - u formed exactly as (2^32 - x) / 2^32
 __device__ __forceinline__ double neglog1m(uint32_t x, double) {
     return -log((double)(0x100000000ull - (unsigned long long)x) * 0x1p-32);
@@ -302,24 +315,26 @@ struct Smem {
     R* vel;
     R* vt;
     unsigned long long* wthr;
-    unsigned long long* pthr;
-    double* tal;   // rows x cols (row-major in shared: r * cols + c)
-    double* dif;   // rows x (cols + 1) difference array
+    long long* tal;   // rows x cols fixed-point partial field (r * cols + c)
+    long long* dif;   // rows x (cols + 1) difference array, fixed point
 };
 
-// Shared layout sizes (bytes); tables first, tally last.
+// Shared layout sizes (bytes): velocity and vel*tau tables, the scatter
+// bin thresholds, then the block's tally.
 template <typename R>
 __host__ __device__ inline size_t smemTableBytes(int nw, int np) {
     size_t b = 2 * sizeof(R) * (size_t)nw * np;
     b = (b + 15) & ~(size_t)15;
-    b += sizeof(unsigned long long) * (size_t)nw * (np + 1);
+    b += sizeof(unsigned long long) * (size_t)nw;
     return (b + 15) & ~(size_t)15;
 }
 __host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
-    return sizeof(double) * (size_t)rows * (2 * (size_t)cols + 1);
+    return sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1);
 }
 
-// Tally modes
+// Tally modes: per-block shared histogram (64-bit fixed point, exact and
+// order-independent adds) flushed with FP64 atomics, or FP64 atomics
+// straight to the global field (fields too large for shared memory).
 enum { TM_SHARED = 0, TM_GLOBAL = 1 };
 
 // Hard cap on events one thread processes in one launch (a guard: a
@@ -338,6 +353,20 @@ struct Phn {
     uint32_t nscat, nloop, id;
 };
 
+// Round a float to the nearest int64 with integer instructions only (the
+// float -> int64 conversion runs on GB300's narrow FP64 pipe). |v| < 2^61.
+__device__ __forceinline__ long long toFixed(float v) {
+    const uint32_t b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xFFu) - 150;  // v = m * 2^e
+    const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+    long long r;
+    if (e >= 0) r = m << e;
+    else if (e > -25) r = (m + (1LL << (-e - 1))) >> (-e);
+    else r = 0;
+    return (b >> 31) ? -r : r;
+}
+__device__ __forceinline__ long long toFixed(double v) { return __double2ll_rn(v); }
+
 template <typename R, int TM>
 struct Tally {
     const Params<R>* P;
@@ -346,116 +375,152 @@ struct Tally {
     // amount per metre of flight, rows entries: Temp sign/v; Flux sign*d
     R rho[4];
 
-    __device__ __forceinline__ void addCell(int col, R t) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            if (r < rows) {
-                if (TM == TM_SHARED) atomicAdd(&sm->tal[r * P->cols + col], (double)(rho[r] * t));
-                else atomicAdd(&P->tally[(size_t)col * rows + r], (double)(rho[r] * t));
-            }
-        }
+    // fixed-point amount of row r for path length t
+    __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * P->tqinv[r])); }
+    __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&sm->tal[r * P->cols + col]), (unsigned long long)v);
     }
-    // interior cells [c0, c1) of a 1-D walk each get path length t
-    __device__ __forceinline__ void addRange(int c0, int c1, int stride, R t) {
-        if (c0 >= c1) return;
-        if (TM == TM_SHARED && stride == 1) {
+    __device__ __forceinline__ void atomRange(int r, int c0, int c1, long long v) const {
+        unsigned long long* d = reinterpret_cast<unsigned long long*>(sm->dif + r * (P->cols + 1));
+        atomicAdd(d + c0, (unsigned long long)v);
+        atomicAdd(d + c1, (unsigned long long)(-v));
+    }
+    __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                if (r < rows) {
-                    double v = (double)(rho[r] * t);
-                    atomicAdd(&sm->dif[r * (P->cols + 1) + c0], v);
-                    atomicAdd(&sm->dif[r * (P->cols + 1) + c1], -v);
-                }
-            }
-        } else {
-            for (int c = c0; c < c1; ++c) addCell(c * stride, t);
-        }
+        for (int r = 0; r < 4; ++r)
+            if (r < rows) atomicAdd(&P->tally[(size_t)col * rows + r], (double)(rho[r] * t));
     }
 };
 
+// Reduced velocity a = S (M^-1 d) and its reciprocal.
 template <typename R>
-__device__ __forceinline__ void reducedVel(const SdomD<R>& S, const R d[3], R a[3]) {
+__device__ __forceinline__ void reducedVel(const SdomD<R>& S, const R d[3], R a[3], R ia[3]) {
     R m[3];
     rotate(S.Minv, d, m);
-    a[0] = S.S[0] * m[0]; a[1] = S.S[1] * m[1]; a[2] = S.S[2] * m[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = S.S[k] * m[k];
+        ia[k] = R(1) / a[k];
+    }
 }
 
 template <typename R>
 __device__ __forceinline__ R clamp01(R x) { return fmin(fmax(x, R(0)), R(1)); }
 
+// Move along axis k by du cells (no tally): displacement relative to the
+// current cell, then re-split into cell index and offset.
+template <typename R>
+__device__ __forceinline__ void moveAxis(Phn<R>& ph, const SdomD<R>& S, int k, R du) {
+    const int sh = (int)floor(du);
+    const int i = min(max(ph.idx[k] + sh, 0), S.shape[k] - 1);
+    ph.off[k] = clamp01(du - (R)(i - ph.idx[k]));
+    ph.idx[k] = i;
+}
+
 // 1-D flight along axis K (the only axis with cells): closed form of
 // montecarlo/field.cpp:187-223 -- partial first and last cells, full
-// interior cells through the difference array.
+// interior cells through the difference array. In the shared layout the
+// flight's whole fixed-point amount V is computed once and the last cell
+// takes the integer remainder, so the cells add up to V exactly.
 template <typename R, int TM, int K>
-__device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], R s, Tally<R, TM>& T) {
+__device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
+                                      Tally<R, TM>& T, long long csum[4]) {
     const int cb = S.colbeg;
     const int b = ph.idx[K];
     const int n = S.shape[K];
-    const R u = (R)b + ph.off[K] + s * a[K];
-    int e = (int)floor(u);
+    // displacement in cell units relative to the current cell
+    const R du = ph.off[K] + s * a[K];
+    int e = b + (int)floor(du);
     e = min(max(e, 0), n - 1);
-    const int stride = (K == 0) ? 1 : (K == 1 ? S.shape[0] : S.shape[0] * S.shape[1]);
-    if (e == b) {
-        T.addCell(cb + b * stride, s);
-    } else {
-        const R inva = R(1) / fabs(a[K]);
-        const int lo = min(b, e), hi = max(b, e);
-        const R tfirst = (e > b ? (R(1) - ph.off[K]) : ph.off[K]) * inva;
-        const R tlast = s - tfirst - (R)(hi - lo - 1) * inva;
-        T.addCell(cb + b * stride, tfirst);
-        T.addCell(cb + e * stride, fmax(tlast, R(0)));
-        if (stride == 1) T.addRange(cb + lo + 1, cb + hi, 1, inva);
-        else for (int c = lo + 1; c < hi; ++c) T.addCell(cb + c * stride, inva);
+    const int stride = S.tstride[K];
+    const R inva = fabs(ia[K]);
+    const int lo = min(b, e), hi = max(b, e);
+    const R tfirst = (e > b ? (R(1) - ph.off[K]) : ph.off[K]) * inva;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        if (r >= T.rows) break;
+        const long long V = T.fixedOf(r, s);
+        csum[r] += V;
+        if (TM == TM_SHARED) {
+            if (e == b) {
+                T.atomShared(r, cb + b * stride, V);
+            } else {
+                const long long F = T.fixedOf(r, tfirst);
+                const long long I = T.fixedOf(r, inva);
+                T.atomShared(r, cb + b * stride, F);
+                T.atomShared(r, cb + e * stride, V - F - (long long)(hi - lo - 1) * I);
+                if (stride == 1) { if (hi - lo > 1) T.atomRange(r, cb + lo + 1, cb + hi, I); }
+                else for (int c = lo + 1; c < hi; ++c) T.atomShared(r, cb + c * stride, I);
+            }
+        }
+    }
+    if (TM == TM_GLOBAL) {
+        if (e == b) {
+            T.addGlobal(cb + b * stride, s);
+        } else {
+            const R tlast = s - tfirst - (R)(hi - lo - 1) * inva;
+            T.addGlobal(cb + b * stride, tfirst);
+            T.addGlobal(cb + e * stride, fmax(tlast, R(0)));
+            for (int c = lo + 1; c < hi; ++c) T.addGlobal(cb + c * stride, inva);
+        }
     }
     ph.idx[K] = e;
-    ph.off[K] = clamp01(u - (R)e);
+    ph.off[K] = clamp01(du - (R)(e - b));
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-        if (j != K) ph.off[j] = clamp01(ph.off[j] + s * a[j]);
+        if (j != K) moveAxis(ph, S, j, ph.off[j] + s * a[j]);
 }
 
 // Flight of path length s from the current cell, tallied cell by cell
-// (Field::accumulate, montecarlo/field.cpp:160-288, as a cell walk).
+// (Field::accumulate, montecarlo/field.cpp:160-288, as a cell walk); adds
+// the flight's fixed-point amount to the thread's checksums.
 template <typename R, int TM>
-__device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], R s, Tally<R, TM>& T) {
+__device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
+                                   Tally<R, TM>& T, long long csum[4]) {
     const int acc = S.accum;
     const int cb = S.colbeg;
-    if (acc < -1) {
-        // no tally: move only
+    if (acc < 0) {
+        // a single field column (or none): move only
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            R u = (R)ph.idx[k] + ph.off[k] + s * a[k];
-            int i = (int)floor(u);
-            i = min(max(i, 0), S.shape[k] - 1);
-            ph.idx[k] = i;
-            ph.off[k] = clamp01(u - (R)i);
+        for (int r = 0; r < 4; ++r) {
+            if (r >= T.rows) break;
+            const long long V = T.fixedOf(r, s);
+            csum[r] += V;
+            if (acc == -1 && TM == TM_SHARED) T.atomShared(r, cb, V);
         }
-        return;
-    }
-    if (acc == -1) {
-        T.addCell(cb, s);
+        if (acc == -1 && TM == TM_GLOBAL) T.addGlobal(cb, s);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) ph.off[k] = clamp01(ph.off[k] + s * a[k]);
+        for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
         return;
     }
-    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, s, T); return; }
-    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, s, T); return; }
-    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, s, T); return; }
+    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, ia, s, T, csum); return; }
+    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, ia, s, T, csum); return; }
+    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, ia, s, T, csum); return; }
     // 2-D / 3-D: walk the cells (Amanatides-Woo)
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        if (r < T.rows) csum[r] += T.fixedOf(r, s);
     R rem = s;
-    const int s0 = S.shape[0], s01 = S.shape[0] * S.shape[1];
+    const int s0 = S.tstride[1], s01 = S.tstride[2];
     for (int guard = 0; guard < 3 * MAX_SHAPE + 4; ++guard) {
         R tmin = rem;
         int ax = -1;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             R t = tmin;
-            if (a[k] > R(0) && ph.idx[k] < S.shape[k] - 1) t = (R(1) - ph.off[k]) / a[k];
-            else if (a[k] < R(0) && ph.idx[k] > 0) t = ph.off[k] / (-a[k]);
+            if (a[k] > R(0) && ph.idx[k] < S.shape[k] - 1) t = (R(1) - ph.off[k]) * ia[k];
+            else if (a[k] < R(0) && ph.idx[k] > 0) t = -ph.off[k] * ia[k];
             if (t < tmin) { tmin = t; ax = k; }
         }
         tmin = fmax(tmin, R(0));
-        T.addCell(cb + ph.idx[0] + ph.idx[1] * s0 + ph.idx[2] * s01, tmin);
+        const int col = cb + ph.idx[0] * S.tstride[0] + ph.idx[1] * s0 + ph.idx[2] * s01;
+        if (TM == TM_SHARED) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < T.rows) T.atomShared(r, col, T.fixedOf(r, tmin));
+        } else {
+            T.addGlobal(col, tmin);
+        }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             ph.off[k] = clamp01(ph.off[k] + tmin * a[k]);
@@ -479,9 +544,8 @@ __device__ __forceinline__ void physPos(const SdomD<R>& S, const Phn<R>& ph, dou
 }
 
 template <typename R>
-__device__ __forceinline__ void logEvent(const Params<R>& P, const Phn<R>& ph, const SdomD<R>& Sb,
-                                         int sBefore, int face, int sAfter, double xEnd[3], double time,
-                                         int cellEnd) {
+__device__ __forceinline__ void logEvent(const Params<R>& P, const Phn<R>& ph, int sBefore, int face,
+                                         int sAfter, double xEnd[3], double time, int cellEnd) {
     if (P.log == nullptr || (long long)ph.id >= P.logn) return;
     long long i = ph.nloop;
     if (i >= P.logcap) return;
@@ -492,9 +556,19 @@ __device__ __forceinline__ void logEvent(const Params<R>& P, const Phn<R>& ph, c
     atomicMax(&P.logcount[ph.id], (int)(i + 1));
 }
 
+// drawScatNext (montecarlo/material.cpp:287-296): d = v tau (-log(1 - u)),
+// redrawn while below the smallest normal number.
+template <typename R, typename G>
+__device__ __forceinline__ R drawScatNext(G& g, R vt) {
+    R dist = R(0);
+    for (int guard = 0; guard < 64 && dist < Lim<R>::tiny(); ++guard) dist = vt * neglog1m(g.next(), R(0));
+    return dist;
+}
+
 // -------------------------------------------------------------- emission
 // FieldProblem::solve emission part (montecarlo/problem.cpp:386-399) and
-// Emitter::emit (montecarlo/boundary.cpp:378-385).
+// Emitter::emit (montecarlo/boundary.cpp:378-385). Writes phonon n to slot n
+// of the front half-range.
 template <typename R, bool REPLAY>
 __global__ void __launch_bounds__(256) k_emit(Params<R> P) {
     long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -549,6 +623,7 @@ __global__ void __launch_bounds__(256) k_emit(Params<R> P) {
         ph.neg = !(((dir[0] * S.gradT[0] + dir[1] * S.gradT[1]) + dir[2] * S.gradT[2]) < R(0));
     }
     normalize(dir);
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
         int i = (int)floor(u[k]);
         i = min(max(i, 0), S.shape[k] - 1);
@@ -556,11 +631,7 @@ __global__ void __launch_bounds__(256) k_emit(Params<R> P) {
         ph.off[k] = u[k] - (R)i;
         ph.d[k] = dir[k];
     }
-    // drawScatNext (montecarlo/material.cpp:287-296)
-    R vt = P.vt[ph.w * P.np + ph.p];
-    R dist = R(0);
-    for (int guard = 0; guard < 64 && dist < Lim<R>::tiny(); ++guard) dist = vt * neglog1m(g.next(), R(0));
-    ph.scatNext = dist;
+    ph.scatNext = drawScatNext<R>(g, P.vt[ph.w * P.np + ph.p]);
     if (REPLAY) {
         g.save();
         if (g.exhausted()) atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED);
@@ -574,269 +645,288 @@ __global__ void __launch_bounds__(256) k_emit(Params<R> P) {
 }
 
 // ----------------------------------------------------------------- advance
-template <typename R, bool REPLAY, bool LOG, int TM>
-__global__ void __launch_bounds__(256) k_advance(Params<R> P) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    Smem<R> sm;
-    {
-        size_t nt = (size_t)P.nw * P.np;
-        sm.vel = reinterpret_cast<R*>(smraw);
-        sm.vt = sm.vel + nt;
-        size_t off = (2 * sizeof(R) * nt + 15) & ~(size_t)15;
-        sm.wthr = reinterpret_cast<unsigned long long*>(smraw + off);
-        sm.pthr = sm.wthr + P.nw;
-        size_t tb = smemTableBytes<R>(P.nw, P.np);
-        sm.tal = reinterpret_cast<double*>(smraw + tb);
-        sm.dif = sm.tal + (size_t)P.rows * P.cols;
-        for (size_t i = threadIdx.x; i < nt; i += blockDim.x) {
-            sm.vel[i] = P.vel[i];
-            sm.vt[i] = P.vt[i];
-            sm.pthr[i] = P.pthr[i];
-        }
-        for (int i = threadIdx.x; i < P.nw; i += blockDim.x) sm.wthr[i] = P.wthr[i];
-        if (TM == TM_SHARED) {
-            size_t nz = (size_t)P.rows * (2 * P.cols + 1);
-            for (size_t i = threadIdx.x; i < nz; i += blockDim.x) sm.tal[i] = 0.0;
-        }
+// Per-launch constants of the advance kernels.
+template <typename R>
+struct Window {
+    int keff;        // dt-steps in this launch
+    R len;           // keff * dt
+    R invdt;
+    bool last;       // the horizon ends with this launch
+    R next;          // length of the following window (0 if none)
+    __device__ __forceinline__ void init(const Params<R>& P) {
+        keff = min(P.ksteps, P.nsteps - P.step0);
+        len = (R)keff * P.dt;
+        invdt = R(1) / P.dt;
+        last = (P.step0 + keff >= P.nsteps);
+        next = (R)min(P.ksteps, max(P.nsteps - P.step0 - keff, 0)) * P.dt;
     }
-    __syncthreads();
+};
 
-    const unsigned long long n = *P.nlive_in;
-    const int keff = min(P.ksteps, P.nsteps - P.step0);
-    const R window = (R)keff * P.dt;
-    const R invdt = R(1) / P.dt;
-    const bool last = (P.step0 + keff >= P.nsteps);
-    double csum[4] = {0.0, 0.0, 0.0, 0.0};
-    unsigned long long cSteps = 0, cEvents = 0, cScat = 0, cEsc = 0, cHor = 0, cMaxs = 0, cMaxl = 0,
-                       cAbs = 0, cBad = 0;
-    const int lane = threadIdx.x & 31;
+// Per-thread counters, reduced once per launch.
+struct Counts {
+    uint32_t steps = 0, events = 0, scat = 0, esc = 0, hor = 0, maxs = 0, maxl = 0, abs = 0, bad = 0;
+};
 
-    Tally<R, TM> T;
-    T.P = &P;
-    T.sm = &sm;
-    T.rows = P.rows;
+// Dead marker in the prop word of a slot written back in place.
+constexpr uint32_t PROP_DEAD = 1u << 25;
 
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n;
-         base += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long i = base + threadIdx.x;
-        bool alive = false;
-        Phn<R> ph;
-        typename Vec4<R>::T A0, A1;
-        uint4 A2;
-        if (i < n) {
-            ld4(P.P0in + i, A0);
-            ld4(P.P1in + i, A1);
-            A2 = __ldcs(P.P2in + i);
-            unpackCell(A2.x, ph.s, ph.idx);
-            ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
-            ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
-            ph.id = realToId<R>(A1.w);
-            ph.w = (int)(A2.y & 0xFFFFu);
-            ph.p = (int)((A2.y >> 16) & 0xFFu);
-            ph.neg = (A2.y >> 24) & 1u;
-            ph.nscat = A2.z;
-            ph.nloop = A2.w;
-            alive = true;
+// One phonon in flight: its state and the launch-local quantities derived
+// from it. iterate() runs one loop iteration of montecarlo/problem.cpp:401-435
+// (flight to the next event or to the end of the window, its tally, the
+// event); finish() closes the phonon's window.
+template <typename R, bool REPLAY, bool LOG, int TM>
+struct Walker {
+    Phn<R> ph;
+    const SdomD<R>* S;
+    R a[3], ia[3];
+    R v, iv, sg;
+    R budget;
+    R tnext;       // time to the next event after the window end
+    int nev;
+    int stop;      // 0 alive, else the counter of the stop reason
+    Rng<REPLAY> g;
 
-            Rng<REPLAY> g;
-            g.init(P.key0, P.key1, ph.id, &P);
-            R budget = window;
-            const SdomD<R>* S = &P.sd[ph.s];
-            R a[3];
-            reducedVel(*S, ph.d, a);
-            R v = sm.vel[ph.w * P.np + ph.p];
-            R sg = ph.neg ? R(-1) : R(1);
-            int stopReason = 0;  // 0 alive, else counter id
-            int nev = 0;
-            T.rho[1] = T.rho[2] = T.rho[3] = R(0);
-            for (;;) {
-                // Subdomain::advect: nearest approaching face vs free path
-                R sev = ph.scatNext;
-                int face = -1;
+    __device__ __forceinline__ void load(const Params<R>& P, const Smem<R>& sm, const Window<R>& W,
+                                         const typename Vec4<R>::T& A0, const typename Vec4<R>::T& A1,
+                                         const uint4& A2) {
+        unpackCell(A2.x, ph.s, ph.idx);
+        ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
+        ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
+        ph.id = realToId<R>(A1.w);
+        ph.w = (int)(A2.y & 0xFFFFu);
+        ph.p = (int)((A2.y >> 16) & 0xFFu);
+        ph.neg = (A2.y >> 24) & 1u;
+        ph.nscat = A2.z;
+        ph.nloop = A2.w;
+        g.init(P.key0, P.key1, ph.id, &P);
+        budget = W.len;
+        S = &P.sd[ph.s];
+        reducedVel(*S, ph.d, a, ia);
+        v = sm.vel[ph.w * P.np + ph.p];
+        iv = R(1) / v;
+        sg = ph.neg ? R(-1) : R(1);
+        stop = 0;
+        nev = 0;
+        tnext = R(0);
+    }
+
+    __device__ __forceinline__ void pack(typename Vec4<R>::T& A0, typename Vec4<R>::T& A1, uint4& A2) const {
+        A0.x = ph.off[0]; A0.y = ph.off[1]; A0.z = ph.off[2]; A0.w = ph.scatNext;
+        A1.x = ph.d[0]; A1.y = ph.d[1]; A1.z = ph.d[2]; A1.w = idToReal<R>(ph.id);
+        A2.x = packCell(ph.s, ph.idx);
+        A2.y = packProp(ph.w, ph.p, ph.neg);
+        A2.z = ph.nscat;
+        A2.w = ph.nloop;
+    }
+
+    // returns true when the phonon's window is over (alive or stopped)
+    __device__ __forceinline__ bool iterate(const Params<R>& P, const Smem<R>& sm, const Window<R>& W,
+                                            Tally<R, TM>& T, Counts& C, long long csum[4]) {
+        // Subdomain::advect (montecarlo/subdomain.cpp:161-192): the
+        // approaching face of each axis, in the reference's face order
+        // (lower faces 0..2, then upper faces 3..5), against the free path;
+        // strict < keeps the first of equals
+        R sev = ph.scatNext;
+        int face = -1;
 #pragma unroll
-                for (int f = 0; f < 6; ++f) {
-                    const int k = f % 3;
-                    R dist;
-                    bool app;
-                    if (f < 3) { app = a[k] < R(0); dist = (-(R)ph.idx[k] - ph.off[k]) / a[k]; }
-                    else { app = a[k] > R(0); dist = (((R)(S->shape[k] - ph.idx[k])) - ph.off[k]) / a[k]; }
-                    if (app && dist < sev) { sev = dist; face = f; }
-                }
-                const R tev = sev / v;
-                const bool event = tev <= budget;
-                const R s = event ? sev : budget * v;
-                // tally amounts per metre (montecarlo/problem.cpp:473-544)
-                if (P.problem == P_TEMP) { T.rho[0] = sg / v; }
-                else if (P.problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; }
-                else { T.rho[0] = sg / v; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
-                const int sBefore = ph.s;
-                int cellEnd = 0;
+        for (int k = 0; k < 3; ++k) {
+            const R dist = (-(R)ph.idx[k] - ph.off[k]) * ia[k];
+            if (a[k] < R(0) && dist < sev) { sev = dist; face = k; }
+        }
 #pragma unroll
-                for (int r = 0; r < 4; ++r) csum[r] += (double)(T.rho[r] * s);
-                fly<R, TM>(ph, *S, a, s, T);
-                if (LOG) cellEnd = ph.idx[0] + ph.idx[1] * S->shape[0] + ph.idx[2] * S->shape[0] * S->shape[1];
-                ph.scatNext -= s;
-                if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
-                if (!event) {
-                    budget = R(0);
-                    if (!(ph.scatNext == ph.scatNext)) stopReason = C_BAD;
-                    break;
-                }
-                budget -= tev;
-                if (sev < -S->eps) {
-                    stopReason = C_ESCAPES;
-                    if (LOG) {
-                        double x[3]; physPos(*S, ph, x);
-                        logEvent(P, ph, *S, sBefore, -3, sBefore, x,
-                                 (double)P.step0 * (double)P.dt + (double)(window - budget), cellEnd);
-                    }
-                    break;
-                }
-                double xe[3];
-                if (LOG) physPos(*S, ph, xe);
-                g.setEvent(ph.nloop + 1);
-                bool dirChanged = false;
-                if (face >= 0) {
-                    const FaceD<R>& F = S->f[face];
-                    // the flight ends on the face: snap that coordinate
+        for (int k = 0; k < 3; ++k) {
+            const R dist = (((R)(S->shape[k] - ph.idx[k])) - ph.off[k]) * ia[k];
+            if (a[k] > R(0) && dist < sev) { sev = dist; face = k + 3; }
+        }
+        const R tev = sev * iv;
+        const bool event = tev <= budget;
+        const R s = event ? sev : budget * v;
+        // tally amounts per metre (montecarlo/problem.cpp:473-544)
+        if (P.problem == P_TEMP) { T.rho[0] = sg * iv; }
+        else if (P.problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; }
+        else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
+        const int sBefore = ph.s;
+        int cellEnd = 0;
+        fly<R, TM>(ph, *S, a, ia, s, T, csum);
+        if (LOG) cellEnd = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
+        ph.scatNext -= s;
+        if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
+        if (!event) {
+            tnext = (sev - s) * iv;
+            budget = R(0);
+            if (!(ph.scatNext == ph.scatNext)) stop = C_BAD;
+            return true;
+        }
+        budget -= tev;
+        if (sev < -S->eps) {
+            stop = C_ESCAPES;
+            if (LOG) {
+                double x[3]; physPos(*S, ph, x);
+                logEvent(P, ph, sBefore, -3, sBefore, x, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
+                         cellEnd);
+            }
+            return true;
+        }
+        double xe[3];
+        if (LOG) physPos(*S, ph, xe);
+        g.setEvent(ph.nloop + 1);
+        if (face >= 0) {
+            const FaceD<R>& F = S->f[face];
+            // the flight ends on the face: snap that coordinate
 #pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        if (face == k) { ph.idx[k] = 0; ph.off[k] = R(0); }
-                        if (face == k + 3) { ph.idx[k] = S->shape[k] - 1; ph.off[k] = R(1); }
-                    }
-                    switch (F.kind) {
-                    case F_SPEC: {  // montecarlo/boundary.cpp:283-287
-                        R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
-                        for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F.n[j];
-                        normalize(ph.d);
-                        dirChanged = true;
-                        break;
-                    }
-                    case F_DIFF: {  // montecarlo/boundary.cpp:308-312
-                        R vv[3];
-                        drawAniso<R>(g, false, vv);
-                        rotate(F.rot, vv, ph.d);
-                        normalize(ph.d);
-                        ph.nscat++;
-                        dirChanged = true;
-                        break;
-                    }
-                    case F_ISOT:  // montecarlo/boundary.cpp:455-460
-                        stopReason = C_ABSORBED;
-                        break;
-                    case F_PERI:   // montecarlo/boundary.cpp:516-522
-                    case F_INTER: {  // montecarlo/boundary.cpp:349-359 (single pair)
-                        if (F.to < 0) { stopReason = C_ESCAPES; break; }
-                        R u[3], u2[3];
-                        for (int j = 0; j < 3; ++j) u[j] = (R)ph.idx[j] + ph.off[j];
-                        rotate(F.A, u, u2);
-                        for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
-                        ph.s = F.to;
-                        S = &P.sd[ph.s];
+            for (int k = 0; k < 3; ++k) {
+                if (face == k) { ph.idx[k] = 0; ph.off[k] = R(0); }
+                if (face == k + 3) { ph.idx[k] = S->shape[k] - 1; ph.off[k] = R(1); }
+            }
+            switch (F.kind) {
+            case F_SPEC: {  // montecarlo/boundary.cpp:283-287
+                R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
+                for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F.n[j];
+                normalize(ph.d);
+                break;
+            }
+            case F_DIFF: {  // montecarlo/boundary.cpp:308-312
+                R vv[3];
+                drawAniso<R>(g, false, vv);
+                rotate(F.rot, vv, ph.d);
+                normalize(ph.d);
+                ph.nscat++;
+                break;
+            }
+            case F_ISOT:  // montecarlo/boundary.cpp:455-460
+                stop = C_ABSORBED;
+                break;
+            case F_PERI:     // montecarlo/boundary.cpp:516-522
+            case F_INTER: {  // montecarlo/boundary.cpp:349-359 (single pair)
+                if (F.to < 0) { stop = C_ESCAPES; break; }
+                if (F.tang) {
+                    // same axis, tangential cells unchanged: keep the split
+                    // coordinates, move onto the paired face
+                    ph.s = F.to;
+                    S = &P.sd[ph.s];
 #pragma unroll
-                        for (int j = 0; j < 3; ++j) {
-                            if (F.toface == j) u2[j] = R(0);
-                            if (F.toface == j + 3) u2[j] = S->S[j];
-                        }
-#pragma unroll
-                        for (int j = 0; j < 3; ++j) {
-                            int ii = (int)floor(u2[j]);
-                            ii = min(max(ii, 0), S->shape[j] - 1);
-                            ph.idx[j] = ii;
-                            ph.off[j] = fmin(fmax(u2[j] - (R)ii, R(0)), R(1));
-                        }
-                        if (F.kind == F_PERI && !F.ident) {
-                            R dd[3] = {ph.d[0], ph.d[1], ph.d[2]};
-                            rotate(F.Rd, dd, ph.d);
-                            normalize(ph.d);
-                        }
-                        dirChanged = true;
-                        break;
-                    }
+                    for (int j = 0; j < 3; ++j) {
+                        if (F.toface == j) { ph.idx[j] = 0; ph.off[j] = R(0); }
+                        if (F.toface == j + 3) { ph.idx[j] = S->shape[j] - 1; ph.off[j] = R(1); }
                     }
                 } else {
-                    // Material::scatter (montecarlo/material.cpp:298-303)
-                    uint32_t x1 = g.next(), x2 = g.next();
-                    ph.w = searchThr(sm.wthr, P.nw, x1);
-                    ph.p = searchBranch(sm.pthr + ph.w * P.np, P.np, x2);
-                    drawIso<R>(g, ph.d);
-                    normalize(ph.d);
-                    ph.nscat++;
-                    R vt = sm.vt[ph.w * P.np + ph.p];
-                    R dist = R(0);
-                    for (int guard = 0; guard < 64 && dist < Lim<R>::tiny(); ++guard)
-                        dist = vt * neglog1m(g.next(), R(0));
-                    ph.scatNext = dist;
-                    v = sm.vel[ph.w * P.np + ph.p];
-                    dirChanged = true;
-                    ++cScat;
-                }
-                ++cEvents;
-                if (LOG) {
-                    logEvent(P, ph, P.sd[sBefore], sBefore, face, ph.s, xe,
-                             (double)P.step0 * (double)P.dt + (double)(window - budget), cellEnd);
-                }
-                ph.nloop++;
-                if (REPLAY && g.exhausted()) { stopReason = C_REPLAY_EXHAUSTED; break; }
-                if (stopReason) break;
-                if ((long long)ph.nscat >= P.maxscat) { stopReason = C_MAXSCAT; break; }
-                if ((long long)ph.nloop >= P.maxloop) { stopReason = C_MAXLOOP; break; }
-                if (++nev >= MAX_EVENTS_PER_LAUNCH) { stopReason = C_BAD; break; }
-                if (dirChanged) reducedVel(*S, ph.d, a);
-            }
-            if (REPLAY) g.save();
-            // phonon-steps processed in this window
-            if (stopReason == 0) {
-                cSteps += keff;
-                if (last) {
-                    stopReason = C_HORIZON;
-                    if (LOG) {
-                        double x[3]; physPos(*S, ph, x);
-                        int ce = ph.idx[0] + ph.idx[1] * S->shape[0] + ph.idx[2] * S->shape[0] * S->shape[1];
-                        logEvent(P, ph, *S, ph.s, -2, ph.s, x, (double)P.nsteps * (double)P.dt, ce);
+                    R u[3], u2[3];
+                    for (int j = 0; j < 3; ++j) u[j] = (R)ph.idx[j] + ph.off[j];
+                    rotate(F.A, u, u2);
+                    for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
+                    ph.s = F.to;
+                    S = &P.sd[ph.s];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        if (F.toface == j) u2[j] = R(0);
+                        if (F.toface == j + 3) u2[j] = S->S[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        int ii = (int)floor(u2[j]);
+                        ii = min(max(ii, 0), S->shape[j] - 1);
+                        ph.idx[j] = ii;
+                        ph.off[j] = clamp01(u2[j] - (R)ii);
                     }
                 }
-            } else {
-                R el = window - budget;
-                long long st = (long long)ceil(el * invdt);
-                st = st < 1 ? 1 : (st > keff ? keff : st);
-                cSteps += st;
+                if (F.kind == F_PERI && !F.ident) {
+                    R dd[3] = {ph.d[0], ph.d[1], ph.d[2]};
+                    rotate(F.Rd, dd, ph.d);
+                    normalize(ph.d);
+                }
+                break;
             }
-            switch (stopReason) {
-            case 0: break;
-            case C_ESCAPES: ++cEsc; break;
-            case C_HORIZON: ++cHor; break;
-            case C_MAXSCAT: ++cMaxs; break;
-            case C_MAXLOOP: ++cMaxl; break;
-            case C_ABSORBED: ++cAbs; break;
-            case C_REPLAY_EXHAUSTED: atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED); break;
-            default: ++cBad; atomicOr(P.status, (unsigned)S_NONFINITE); break;
             }
-            alive = (stopReason == 0);
-            if (alive) {
-                A0.x = ph.off[0]; A0.y = ph.off[1]; A0.z = ph.off[2]; A0.w = ph.scatNext;
-                A1.x = ph.d[0]; A1.y = ph.d[1]; A1.z = ph.d[2];
-                A2.x = packCell(ph.s, ph.idx);
-                A2.y = packProp(ph.w, ph.p, ph.neg);
-                A2.z = ph.nscat;
-                A2.w = ph.nloop;
-            }
+        } else {
+            // Material::scatter (montecarlo/material.cpp:298-303)
+            uint32_t x1 = g.next(), x2 = g.next();
+            ph.w = searchThr(sm.wthr, P.nw, x1);
+            ph.p = searchBranch(P.pthr + ph.w * P.np, P.np, x2);
+            drawIso<R>(g, ph.d);
+            normalize(ph.d);
+            ph.nscat++;
+            ph.scatNext = drawScatNext<R>(g, sm.vt[ph.w * P.np + ph.p]);
+            v = sm.vel[ph.w * P.np + ph.p];
+            iv = R(1) / v;
+            ++C.scat;
         }
-        // fused compaction: one atomic per warp
-        const unsigned mask = __ballot_sync(0xFFFFFFFFu, alive);
-        unsigned long long wbase = 0;
-        if (lane == 0 && mask) wbase = atomicAdd(P.nlive_out, (unsigned long long)__popc(mask));
-        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-        if (alive) {
-            const unsigned long long o = wbase + __popc(mask & ((1u << lane) - 1u));
-            st4(P.P0out + o, A0);
-            st4(P.P1out + o, A1);
-            __stcs(P.P2out + o, A2);
-        }
+        ++C.events;
+        if (LOG) logEvent(P, ph, sBefore, face, ph.s, xe, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
+                          cellEnd);
+        ph.nloop++;
+        if (REPLAY && g.exhausted()) { stop = C_REPLAY_EXHAUSTED; return true; }
+        if (stop) return true;
+        if ((long long)ph.nscat >= P.maxscat) { stop = C_MAXSCAT; return true; }
+        if ((long long)ph.nloop >= P.maxloop) { stop = C_MAXLOOP; return true; }
+        if (++nev >= MAX_EVENTS_PER_LAUNCH) { stop = C_BAD; return true; }
+        reducedVel(*S, ph.d, a, ia);
+        return false;
     }
 
-    // counters: warp reduce, one atomic per warp
-    unsigned long long cs[9] = {cSteps, cEvents, cScat, cEsc, cHor, cMaxs, cMaxl, cAbs, cBad};
+    // the phonon's window is over: count its steps and its stop reason;
+    // returns true if it stays alive
+    __device__ __forceinline__ bool finish(const Params<R>& P, const Window<R>& W, Counts& C) {
+        if (REPLAY) g.save();
+        if (stop == 0) {
+            C.steps += W.keff;
+            if (W.last) {
+                stop = C_HORIZON;
+                if (LOG) {
+                    double x[3]; physPos(*S, ph, x);
+                    int ce = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
+                    logEvent(P, ph, ph.s, -2, ph.s, x, (double)P.nsteps * (double)P.dt, ce);
+                }
+            }
+        } else {
+            R el = W.len - budget;
+            int st = (int)ceil(el * W.invdt);
+            st = st < 1 ? 1 : (st > W.keff ? W.keff : st);
+            C.steps += st;
+        }
+        switch (stop) {
+        case 0: break;
+        case C_ESCAPES: ++C.esc; break;
+        case C_HORIZON: ++C.hor; break;
+        case C_MAXSCAT: ++C.maxs; break;
+        case C_MAXLOOP: ++C.maxl; break;
+        case C_ABSORBED: ++C.abs; break;
+        case C_REPLAY_EXHAUSTED: atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED); break;
+        default: ++C.bad; atomicOr(P.status, (unsigned)S_NONFINITE); break;
+        }
+        return stop == 0;
+    }
+};
+
+// Stage the material tables (and zero the block's tally) in shared memory.
+template <typename R, int TM>
+__device__ __forceinline__ void stageTables(const Params<R>& P, Smem<R>& sm, unsigned char* smraw) {
+    const int nt = P.nw * P.np;
+    sm.vel = reinterpret_cast<R*>(smraw);
+    sm.vt = sm.vel + nt;
+    size_t off = (2 * sizeof(R) * (size_t)nt + 15) & ~(size_t)15;
+    sm.wthr = reinterpret_cast<unsigned long long*>(smraw + off);
+    const size_t tb = smemTableBytes<R>(P.nw, P.np);
+    sm.tal = reinterpret_cast<long long*>(smraw + tb);
+    sm.dif = sm.tal + (size_t)P.rows * P.cols;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        sm.vel[i] = P.vel[i];
+        sm.vt[i] = P.vt[i];
+    }
+    for (int i = threadIdx.x; i < P.nw; i += blockDim.x) sm.wthr[i] = P.wthr[i];
+    if (TM == TM_SHARED) {
+        const int nz = P.rows * (2 * P.cols + 1);
+        for (int i = threadIdx.x; i < nz; i += blockDim.x) sm.tal[i] = 0;
+    }
+}
+
+// Reduce the counters and checksums (one atomic per warp), then turn the
+// block's difference array into cell values and flush the fixed-point field
+// as FP64 atomics.
+template <typename R, int TM>
+__device__ __forceinline__ void closeBlock(const Params<R>& P, const Smem<R>& sm, const Counts& C,
+                                           const long long csum[4]) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t cs[9] = {C.steps, C.events, C.scat, C.esc, C.hor, C.maxs, C.maxl, C.abs, C.bad};
     const int ids[9] = {C_PHONON_STEPS, C_EVENTS, C_SCATTERS, C_ESCAPES, C_HORIZON, C_MAXSCAT,
                         C_MAXLOOP, C_ABSORBED, C_BAD};
 #pragma unroll
@@ -845,26 +935,23 @@ __global__ void __launch_bounds__(256) k_advance(Params<R> P) {
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
         if (lane == 0 && x) atomicAdd(&P.counters[ids[q]], x);
     }
-
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        double x = csum[r];
+        long long x = csum[r];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && r < P.rows && x != 0.0) atomicAdd(&P.csum[r], x);
+        if (lane == 0 && r < P.rows && x != 0) atomicAdd(&P.csum[r], (double)x * P.tq[r]);
     }
-
     if (TM == TM_SHARED) {
         __syncthreads();
-        // difference array -> cell values (one warp per row), then flush
         const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
         for (int r = warp; r < P.rows; r += nwarps) {
-            double carry = 0.0;
-            double* dr = sm.dif + r * (P.cols + 1);
+            long long carry = 0;
+            const long long* dr = sm.dif + r * (P.cols + 1);
             for (int c0 = 0; c0 < P.cols; c0 += 32) {
-                int c = c0 + lane;
-                double x = c < P.cols ? dr[c] : 0.0;
+                const int c = c0 + lane;
+                long long x = c < P.cols ? dr[c] : 0;
                 for (int o = 1; o < 32; o <<= 1) {
-                    double y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
                     if (lane >= o) x += y;
                 }
                 x += carry;
@@ -875,11 +962,190 @@ __global__ void __launch_bounds__(256) k_advance(Params<R> P) {
         __syncthreads();
         const int tot = P.rows * P.cols;
         for (int q = threadIdx.x; q < tot; q += blockDim.x) {
-            double x = sm.tal[q];
-            if (x != 0.0) {
+            const long long x = sm.tal[q];
+            if (x != 0) {
                 const int r = q / P.cols, c = q - r * P.cols;
-                atomicAdd(&P.tally[(size_t)c * P.rows + r], x);
+                atomicAdd(&P.tally[(size_t)c * P.rows + r], (double)x * P.tq[r]);
             }
+        }
+    }
+}
+
+// Static kernel: one phonon per thread per pass of a grid-stride loop;
+// survivors are compacted to the two ends of the other half of the
+// ping-pong state (front: next event inside the next window).
+template <typename R, bool REPLAY, bool LOG, int TM>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_advance(Params<R> P) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    Smem<R> sm;
+    stageTables<R, TM>(P, sm, smraw);
+    __syncthreads();
+
+    const unsigned long long nf = P.live_in[0], nb = P.live_in[1];
+    const unsigned long long n = nf + nb;
+    Window<R> W;
+    W.init(P);
+    long long csum[4] = {0, 0, 0, 0};
+    Counts C;
+    const int lane = threadIdx.x & 31;
+    Tally<R, TM> T;
+    T.P = &P;
+    T.sm = &sm;
+    T.rows = P.rows;
+    T.rho[1] = T.rho[2] = T.rho[3] = R(0);
+
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long i = base + threadIdx.x;
+        bool alive = false, soon = false;
+        typename Vec4<R>::T A0, A1;
+        uint4 A2;
+        if (i < n) {
+            const unsigned long long slot = i < nf ? i : P.cap - nb + (i - nf);
+            ld4(P.P0in + slot, A0);
+            ld4(P.P1in + slot, A1);
+            A2 = __ldcs(P.P2in + slot);
+            Walker<R, REPLAY, LOG, TM> wk;
+            wk.load(P, sm, W, A0, A1, A2);
+            while (!wk.iterate(P, sm, W, T, C, csum)) {}
+            alive = wk.finish(P, W, C);
+            soon = wk.tnext < W.next;
+            if (alive) wk.pack(A0, A1, A2);
+        }
+        // fused compaction into two ends: one atomic per warp and end
+        const unsigned mf = __ballot_sync(0xFFFFFFFFu, alive && soon);
+        const unsigned mb = __ballot_sync(0xFFFFFFFFu, alive && !soon);
+        unsigned long long bf = 0, bb = 0;
+        if (lane == 0) {
+            if (mf) bf = atomicAdd(&P.live_out[0], (unsigned long long)__popc(mf));
+            if (mb) bb = atomicAdd(&P.live_out[1], (unsigned long long)__popc(mb));
+        }
+        bf = __shfl_sync(0xFFFFFFFFu, bf, 0);
+        bb = __shfl_sync(0xFFFFFFFFu, bb, 0);
+        if (alive) {
+            const unsigned lt = (1u << lane) - 1u;
+            const unsigned long long o = soon ? bf + __popc(mf & lt) : P.cap - 1 - (bb + __popc(mb & lt));
+            st4(P.P0out + o, A0);
+            st4(P.P1out + o, A1);
+            __stcs(P.P2out + o, A2);
+        }
+    }
+    closeBlock<R, TM>(P, sm, C, csum);
+}
+
+// Dynamic kernel: block b owns input slots [b C, (b + 1) C); each warp keeps
+// its lanes busy by refilling finished lanes from the block's queue whenever
+// at least REFILL of them are idle, so a long phonon no longer holds up its
+// warp. Survivors are written back in place; dead slots get PROP_DEAD and are
+// skipped until the host compacts. Input == output state half.
+constexpr int REFILL = 8;
+
+template <typename R, bool REPLAY, bool LOG, int TM>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_advance_dyn(Params<R> P) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ unsigned long long qnext;
+    Smem<R> sm;
+    stageTables<R, TM>(P, sm, smraw);
+    const unsigned long long n = P.live_in[0];  // slots [0, n)
+    const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
+    const unsigned long long qend = min(qbeg + chunk, n);
+    if (threadIdx.x == 0) qnext = qbeg;
+    __syncthreads();
+
+    Window<R> W;
+    W.init(P);
+    long long csum[4] = {0, 0, 0, 0};
+    Counts C;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    Tally<R, TM> T;
+    T.P = &P;
+    T.sm = &sm;
+    T.rows = P.rows;
+    T.rho[1] = T.rho[2] = T.rho[3] = R(0);
+
+    Walker<R, REPLAY, LOG, TM> wk;
+    bool have = false;
+    unsigned long long slot = 0;
+    bool drained = false;
+    uint32_t alive = 0;
+    for (int guard = 0; guard < (1 << 30); ++guard) {
+        const unsigned idle = __ballot_sync(0xFFFFFFFFu, !have);
+        if (!drained && (idle == 0xFFFFFFFFu || __popc(idle) >= REFILL)) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&qnext, (unsigned long long)__popc(idle));
+            b = __shfl_sync(0xFFFFFFFFu, b, 0);
+            if (b + __popc(idle) >= qend) drained = true;
+            if (!have) {
+                const unsigned long long my = b + __popc(idle & lt);
+                if (my < qend) {
+                    typename Vec4<R>::T A0, A1;
+                    uint4 A2 = __ldcs(P.P2in + my);
+                    if (!(A2.y & PROP_DEAD)) {
+                        ld4(P.P0in + my, A0);
+                        ld4(P.P1in + my, A1);
+                        wk.load(P, sm, W, A0, A1, A2);
+                        have = true;
+                        slot = my;
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, have) == 0) {
+            if (drained) break;
+            continue;
+        }
+        if (have && wk.iterate(P, sm, W, T, C, csum)) {
+            typename Vec4<R>::T A0, A1;
+            uint4 A2;
+            if (wk.finish(P, W, C)) {
+                wk.pack(A0, A1, A2);
+                st4(P.P0out + slot, A0);
+                st4(P.P1out + slot, A1);
+                __stcs(P.P2out + slot, A2);
+                ++alive;
+            } else if (!W.last) {
+                // no later launch reads the slots after the horizon
+                A2.x = 0u; A2.y = PROP_DEAD; A2.z = 0u; A2.w = 0u;
+                __stcs(P.P2out + slot, A2);
+            }
+            have = false;
+        }
+    }
+    // survivors: the host compacts when many slots are dead
+    {
+        unsigned long long x = alive;
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if (lane == 0 && x) atomicAdd(&P.live_out[0], x);
+    }
+    closeBlock<R, TM>(P, sm, C, csum);
+}
+
+// Stream compaction of the live slots of a dynamic-kernel state into the
+// other half (order of arrival per warp).
+template <typename R>
+__global__ void __launch_bounds__(256) k_compact(Params<R> P) {
+    const unsigned long long n = P.live_in[0];
+    const int lane = threadIdx.x & 31;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long i = base + threadIdx.x;
+        uint4 A2 = make_uint4(0, PROP_DEAD, 0, 0);
+        if (i < n) A2 = __ldcs(P.P2in + i);
+        const bool live = !(A2.y & PROP_DEAD);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, live);
+        unsigned long long b = 0;
+        if (lane == 0 && m) b = atomicAdd(&P.live_out[0], (unsigned long long)__popc(m));
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (live) {
+            const unsigned long long o = b + __popc(m & ((1u << lane) - 1u));
+            typename Vec4<R>::T A0, A1;
+            ld4(P.P0in + i, A0);
+            ld4(P.P1in + i, A1);
+            st4(P.P0out + o, A0);
+            st4(P.P1out + o, A1);
+            __stcs(P.P2out + o, A2);
         }
     }
 }

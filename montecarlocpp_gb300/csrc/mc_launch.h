@@ -11,14 +11,17 @@ namespace mcg {
 template <typename R>
 cudaError_t launchEmit(const Params<R>& p, bool replay, cudaStream_t s);
 
-// tm: TM_SHARED or TM_GLOBAL
+// tm: TM_SHARED or TM_GLOBAL; dyn: the dynamic-refill kernel
 template <typename R>
-cudaError_t launchAdvance(const Params<R>& p, bool replay, bool log, int tm, int grid, int block,
+cudaError_t launchAdvance(const Params<R>& p, bool dyn, bool replay, bool log, int tm, int grid, int block,
                           size_t smem, cudaStream_t s);
+
+template <typename R>
+cudaError_t launchCompact(const Params<R>& p, int grid, cudaStream_t s);
 
 // Maximum resident blocks per SM of the advance kernel for this
 // configuration (0 if it cannot launch).
 template <typename R>
-int advanceOccupancy(bool replay, bool log, int tm, int block, size_t smem);
+int advanceOccupancy(bool dyn, bool replay, bool log, int tm, int block, size_t smem);
 
 }  // namespace mcg

@@ -5,20 +5,26 @@
 
 namespace mcg {
 
-template <typename R, bool REPLAY, bool LOG, int TM>
-static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t smem, cudaStream_t s) {
-    auto fn = k_advance<R, REPLAY, LOG, TM>;
+template <typename K>
+static cudaError_t prepare(K fn, size_t smem) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
+static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t smem, cudaStream_t s) {
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
+    cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
     fn<<<grid, block, smem, s>>>(p);
     return cudaGetLastError();
 }
 
-template <typename R, bool REPLAY, bool LOG, int TM>
+template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
 static int occOne(int block, size_t smem) {
-    auto fn = k_advance<R, REPLAY, LOG, TM>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 0;
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
+    if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess) return 0;
     return nb;
@@ -35,32 +41,46 @@ cudaError_t launchEmit<MC_REAL>(const Params<MC_REAL>& p, bool replay, cudaStrea
 }
 
 template <>
-cudaError_t launchAdvance<MC_REAL>(const Params<MC_REAL>& p, bool replay, bool log, int tm, int grid,
+cudaError_t launchCompact<MC_REAL>(const Params<MC_REAL>& p, int grid, cudaStream_t s) {
+    k_compact<MC_REAL><<<grid, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+#define MC_DISPATCH(F, ...)                                                                 \
+    if (dyn) {                                                                             \
+        if (tm == TM_SHARED) {                                                             \
+            if (replay) return log ? F<MC_REAL, true, true, true, TM_SHARED>(__VA_ARGS__)   \
+                                   : F<MC_REAL, true, true, false, TM_SHARED>(__VA_ARGS__); \
+            return log ? F<MC_REAL, true, false, true, TM_SHARED>(__VA_ARGS__)              \
+                       : F<MC_REAL, true, false, false, TM_SHARED>(__VA_ARGS__);            \
+        }                                                                                  \
+        if (replay) return log ? F<MC_REAL, true, true, true, TM_GLOBAL>(__VA_ARGS__)       \
+                               : F<MC_REAL, true, true, false, TM_GLOBAL>(__VA_ARGS__);     \
+        return log ? F<MC_REAL, true, false, true, TM_GLOBAL>(__VA_ARGS__)                  \
+                   : F<MC_REAL, true, false, false, TM_GLOBAL>(__VA_ARGS__);                \
+    }                                                                                      \
+    if (tm == TM_SHARED) {                                                                 \
+        if (replay) return log ? F<MC_REAL, false, true, true, TM_SHARED>(__VA_ARGS__)      \
+                               : F<MC_REAL, false, true, false, TM_SHARED>(__VA_ARGS__);    \
+        return log ? F<MC_REAL, false, false, true, TM_SHARED>(__VA_ARGS__)                 \
+                   : F<MC_REAL, false, false, false, TM_SHARED>(__VA_ARGS__);               \
+    }                                                                                      \
+    if (replay) return log ? F<MC_REAL, false, true, true, TM_GLOBAL>(__VA_ARGS__)          \
+                           : F<MC_REAL, false, true, false, TM_GLOBAL>(__VA_ARGS__);        \
+    return log ? F<MC_REAL, false, false, true, TM_GLOBAL>(__VA_ARGS__)                     \
+               : F<MC_REAL, false, false, false, TM_GLOBAL>(__VA_ARGS__);
+
+template <>
+cudaError_t launchAdvance<MC_REAL>(const Params<MC_REAL>& p, bool dyn, bool replay, bool log, int tm, int grid,
                                    int block, size_t smem, cudaStream_t s) {
-    if (tm == TM_SHARED) {
-        if (replay) return log ? advanceOne<MC_REAL, true, true, TM_SHARED>(p, grid, block, smem, s)
-                               : advanceOne<MC_REAL, true, false, TM_SHARED>(p, grid, block, smem, s);
-        return log ? advanceOne<MC_REAL, false, true, TM_SHARED>(p, grid, block, smem, s)
-                   : advanceOne<MC_REAL, false, false, TM_SHARED>(p, grid, block, smem, s);
-    }
-    if (replay) return log ? advanceOne<MC_REAL, true, true, TM_GLOBAL>(p, grid, block, smem, s)
-                           : advanceOne<MC_REAL, true, false, TM_GLOBAL>(p, grid, block, smem, s);
-    return log ? advanceOne<MC_REAL, false, true, TM_GLOBAL>(p, grid, block, smem, s)
-               : advanceOne<MC_REAL, false, false, TM_GLOBAL>(p, grid, block, smem, s);
+    MC_DISPATCH(advanceOne, p, grid, block, smem, s)
 }
 
 template <>
-int advanceOccupancy<MC_REAL>(bool replay, bool log, int tm, int block, size_t smem) {
-    if (tm == TM_SHARED) {
-        if (replay) return log ? occOne<MC_REAL, true, true, TM_SHARED>(block, smem)
-                               : occOne<MC_REAL, true, false, TM_SHARED>(block, smem);
-        return log ? occOne<MC_REAL, false, true, TM_SHARED>(block, smem)
-                   : occOne<MC_REAL, false, false, TM_SHARED>(block, smem);
-    }
-    if (replay) return log ? occOne<MC_REAL, true, true, TM_GLOBAL>(block, smem)
-                           : occOne<MC_REAL, true, false, TM_GLOBAL>(block, smem);
-    return log ? occOne<MC_REAL, false, true, TM_GLOBAL>(block, smem)
-               : occOne<MC_REAL, false, false, TM_GLOBAL>(block, smem);
+int advanceOccupancy<MC_REAL>(bool dyn, bool replay, bool log, int tm, int block, size_t smem) {
+    MC_DISPATCH(occOne, block, smem)
 }
+
+#undef MC_DISPATCH
 
 }  // namespace mcg

@@ -45,6 +45,8 @@ struct FaceD {
     int to;       // destination subdomain (Peri / Inter), else -1
     int toface;   // face of `to` the phonon arrives on
     int ident;    // 1 if the Peri rotation is the identity
+    int tang;     // 1 if the map keeps the tangential cell coordinates
+    int pad;
     R n[3];       // inward unit normal (Spec reflection)
     R rot[9];     // rotation z-hat -> n, row-major (Diff, Isot emission)
     R Rd[9];      // Peri direction rotation, row-major
@@ -62,10 +64,12 @@ struct SdomD {
     R gradT[3];   // volumetric gradient (EmitSubdomain)
     R grot[9];    // rotation z-hat -> gradT-hat
     R eps;        // escape tolerance in path length
-    int shape[3];
-    int accum;    // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
-    int colbeg;   // first field column, -1 if the subdomain has none
-    int pad[3];
+    int shape[3];    // walk cells per axis: max(div, 1), or WALK_CELLS on an
+                     // axis without tally cells (finer FP32 offsets)
+    int tstride[3];  // field column stride of each axis, 0 if the axis has
+                     // no tally cells
+    int accum;       // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
+    int colbeg;      // first field column, -1 if the subdomain has none
     FaceD<R> f[6];
 };
 
@@ -79,6 +83,10 @@ struct EmitterD {
 constexpr int CELL_BITS = 9;
 constexpr int MAX_SHAPE = 1 << CELL_BITS;
 constexpr int MAX_SDOM = 32;
+// Walk cells on an axis that carries no tally cells (div = 0) of a
+// subdomain with a 0-D or 1-D field: positions are stored as cell index +
+// offset, so this sets the FP32 resolution along that axis.
+constexpr int WALK_CELLS = 256;
 
 // Bytes moved per phonon per launch by the FP32 kernel's state (read once,
 // written once): three 16-byte words.

@@ -153,7 +153,8 @@ class FieldProblem:
         return {TEMP: 1, FLUX: 3, MULTI: 4}[self.kind]
 
     def desc(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
-             grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0, stream=None):
+             grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0, stream=None,
+             schedule=0, compact_interval=0):
         d = _lib.ProblemDesc()
         d.problem, d.nemit, d.maxscat, d.maxloop = self.kind, self.nemit_requested, self.maxscat, self.maxloop
         d.dt, d.nsteps, d.precision, d.seed = float(dt), int(nsteps), int(precision), int(seed)
@@ -177,17 +178,20 @@ class FieldProblem:
             d.log_cap, d.log_phonons = int(log_cap), int(log_phonons)
             log = (log, counts)
         d.stream = stream
+        d.schedule, d.compact_interval = int(schedule), int(compact_interval)
         return d, keep, log
 
     def solve(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
-              grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0):
+              grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0, schedule=0,
+              compact_interval=0):
         """Run every phonon on the GPU; returns the rows x cols field
         (power * postProc(tally) / cellVol, montecarlo/problem.cpp:439-444).
         With log_cap, ``self.log`` holds (records, counts)."""
         d, keep, log = self.desc(dt=dt, nsteps=nsteps, seed=seed, precision=precision,
                                  steps_per_launch=steps_per_launch, block_size=block_size,
                                  grid_blocks=grid_blocks, tally_mode=tally_mode, replay=replay,
-                                 log_cap=log_cap, log_phonons=log_phonons)
+                                 log_cap=log_cap, log_phonons=log_phonons, schedule=schedule,
+                                 compact_interval=compact_interval)
         out = np.zeros(self.rows() * self.handle.cols)
         st = _lib.Stats()
         _lib.check(_lib.lib().mc_solve(self.mat.h, self.handle.h, C.byref(d), _dp(out), C.byref(st)))
