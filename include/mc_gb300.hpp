@@ -1,0 +1,197 @@
+// mc_gb300.hpp -- C++ host mirror of montecarlocpp's Material / Domain /
+// Problem API over the C ABI of mc_gb300.h (header only).
+//
+// Names, constructor arguments and meanings follow the reference:
+//   Material(disp, relax, T)                  montecarlo/material.h:51-67
+//   FilmDomain(dim, div, dT), BulkDomain(...)  montecarlo/domain.h:93-137
+//   TempProblem / FluxProblem / MultiProblem
+//       (mat, dom, nemit, maxscat, maxloop)   montecarlo/problem.h:157-203
+// FieldProblem::solve() returns the rows x cols field in the column-major
+// layout of Eigen::ArrayXXd (montecarlo/problem.cpp:370-445); errors that the
+// reference turns into BOOST_ASSERT_MSG aborts are thrown as mcgb::Error.
+#ifndef MC_GB300_HPP
+#define MC_GB300_HPP
+
+#include <array>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mc_gb300.h"
+
+namespace mcgb {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc) {
+    if (rc != MC_OK) throw Error(rc, mc_last_error());
+}
+
+class Material {
+public:
+    Material(const std::string& disp, const std::string& relax, double T) : T_(T) {
+        mc_material_h h = nullptr;
+        check(mc_material_load(disp.c_str(), relax.c_str(), T, &h));
+        h_.reset(h, mc_material_destroy);
+        check(mc_material_sums(h_.get(), sums_.data()));
+    }
+    Material(const std::vector<double>& disp, long nw, long np, const std::vector<double>& relax, double T) : T_(T) {
+        mc_material_h h = nullptr;
+        check(mc_material_create(disp.data(), nw, np, relax.data(), T, &h));
+        h_.reset(h, mc_material_destroy);
+        check(mc_material_sums(h_.get(), sums_.data()));
+    }
+    double temp() const { return T_; }
+    double cond() const { return sums_[3]; }
+    double energySum() const { return sums_[0]; }
+    double fluxSum() const { return sums_[1]; }
+    double scatSum() const { return sums_[2]; }
+    mc_material_h handle() const { return h_.get(); }
+
+private:
+    double T_;
+    std::array<double, 4> sums_{};
+    std::shared_ptr<mc_material_s> h_;
+};
+
+// A domain: Parallelepiped subdomains plus makePair calls.
+class Domain {
+public:
+    virtual ~Domain() = default;
+    long cols() const { return mc_domain_cols(handle()); }
+    std::vector<double> cellVolumes() const {
+        std::vector<double> v((size_t)cols());
+        check(mc_domain_cell_volumes(handle(), v.data()));
+        return v;
+    }
+    mc_domain_h handle() const {
+        if (!h_) {
+            mc_domain_h h = nullptr;
+            check(mc_domain_create(ppeds_.data(), (int)ppeds_.size(), pairs_.empty() ? nullptr : pairs_.data(),
+                                   (int)pairs_.size(), &h));
+            h_.reset(h, mc_domain_destroy);
+        }
+        return h_.get();
+    }
+
+protected:
+    static mc_pped_desc box(const double o[3], const double dim[3], const long div[3], const double gradT[3],
+                            const int kind[6], const double T[6]) {
+        mc_pped_desc p;
+        std::memset(&p, 0, sizeof(p));
+        for (int i = 0; i < 3; ++i) {
+            p.o[i] = o[i];
+            p.M[4 * i] = dim[i];
+            p.div[i] = div[i];
+            p.gradT[i] = gradT[i];
+        }
+        for (int i = 0; i < 6; ++i) { p.kind[i] = kind[i]; p.T[i] = T[i]; }
+        return p;
+    }
+    static mc_pair_desc peri(int s1, int f1, int s2, int f2, const double t[3]) {
+        mc_pair_desc q;
+        std::memset(&q, 0, sizeof(q));
+        q.kind = MC_PERI; q.sdom1 = s1; q.face1 = f1; q.sdom2 = s2; q.face2 = f2;
+        for (int i = 0; i < 3; ++i) q.transl[i] = t[i];
+        q.rot[0] = q.rot[4] = q.rot[8] = 1.;
+        return q;
+    }
+    std::vector<mc_pped_desc> ppeds_;
+    std::vector<mc_pair_desc> pairs_;
+    mutable std::shared_ptr<mc_domain_s> h_;
+};
+
+// FilmDomain: PeriP along x, Diff along y, Spec along z
+// (montecarlo/domain.cpp:188-199).
+class FilmDomain : public Domain {
+public:
+    FilmDomain(const double dim[3], const long div[3], double dT) {
+        const double o[3] = {0, 0, 0}, g[3] = {-dT / dim[0], 0, 0}, T[6] = {0, 0, 0, 0, 0, 0};
+        const int k[6] = {MC_PERI, MC_DIFF, MC_SPEC, MC_PERI, MC_DIFF, MC_SPEC};
+        ppeds_.push_back(box(o, dim, div, g, k, T));
+        const double t[3] = {dim[0], 0, 0};
+        pairs_.push_back(peri(0, 0, 0, 3, t));
+    }
+};
+
+// BulkDomain: PeriP along x, Spec along y and z (montecarlo/domain.cpp:137-148).
+class BulkDomain : public Domain {
+public:
+    BulkDomain(const double dim[3], const long div[3], double dT) {
+        const double o[3] = {0, 0, 0}, g[3] = {-dT / dim[0], 0, 0}, T[6] = {0, 0, 0, 0, 0, 0};
+        const int k[6] = {MC_PERI, MC_SPEC, MC_SPEC, MC_PERI, MC_SPEC, MC_SPEC};
+        ppeds_.push_back(box(o, dim, div, g, k, T));
+        const double t[3] = {dim[0], 0, 0};
+        pairs_.push_back(peri(0, 0, 0, 3, t));
+    }
+};
+
+// Options of the GPU run loop that the reference does not have: the time
+// horizon (nsteps x dt), the flight precision, the Philox key and the
+// launch shape.
+struct RunOptions {
+    double dt = 0.5e-12;
+    long nsteps = 4000;
+    int precision = 32;
+    uint64_t seed = 0;
+    int stepsPerLaunch = 0;  // 0: the whole horizon in one launch
+};
+
+class FieldProblem {
+public:
+    FieldProblem(const Material& mat, const Domain& dom, long nemit, long maxscat, long maxloop, int kind)
+        : mat_(mat), dom_(dom), nemit_(nemit), maxscat_(maxscat), maxloop_(maxloop), kind_(kind) {
+        if (nemit <= 0 || maxscat <= 0 || maxloop < 0) throw Error(MC_ERR_ARG, "Invalid problem arguments");
+    }
+    virtual ~FieldProblem() = default;
+    long rows() const { return kind_ == MC_TEMP ? 1 : (kind_ == MC_FLUX ? 3 : 4); }
+
+    // all phonons on the GPU; column-major rows x cols
+    std::vector<double> solve(const RunOptions& o = RunOptions(), mc_stats* stats = nullptr) const {
+        mc_problem_desc d;
+        std::memset(&d, 0, sizeof(d));
+        d.problem = kind_;
+        d.nemit = nemit_;
+        d.maxscat = maxscat_;
+        d.maxloop = maxloop_;
+        d.dt = o.dt;
+        d.nsteps = o.nsteps;
+        d.precision = o.precision;
+        d.seed = o.seed;
+        d.steps_per_launch = o.stepsPerLaunch > 0 ? o.stepsPerLaunch : (int)o.nsteps;
+        d.tally_mode = MC_TALLY_AUTO;
+        std::vector<double> out((size_t)(rows() * dom_.cols()));
+        mc_stats st;
+        check(mc_solve(mat_.handle(), dom_.handle(), &d, out.data(), &st));
+        if (stats) *stats = st;
+        return out;
+    }
+
+private:
+    const Material& mat_;
+    const Domain& dom_;
+    long nemit_, maxscat_, maxloop_;
+    int kind_;
+};
+
+struct TempProblem : FieldProblem {
+    TempProblem(const Material& m, const Domain& d, long nemit, long maxscat, long maxloop = 0)
+        : FieldProblem(m, d, nemit, maxscat, maxloop, MC_TEMP) {}
+};
+struct FluxProblem : FieldProblem {
+    FluxProblem(const Material& m, const Domain& d, long nemit, long maxscat, long maxloop = 0)
+        : FieldProblem(m, d, nemit, maxscat, maxloop, MC_FLUX) {}
+};
+struct MultiProblem : FieldProblem {
+    MultiProblem(const Material& m, const Domain& d, long nemit, long maxscat, long maxloop = 0)
+        : FieldProblem(m, d, nemit, maxscat, maxloop, MC_MULTI) {}
+};
+
+}  // namespace mcgb
+
+#endif  // MC_GB300_HPP

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmc_gb300.so")
+MAIN = os.path.join(OUT, "mc_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr"]
@@ -36,11 +37,13 @@ def nvcc() -> str:
 
 def _sources():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
-        os.path.join(HERE, "..", "include", "mc_gb300.h")]
+        os.path.join(HERE, "..", "include", "mc_gb300.h"), os.path.join(HERE, "..", "include", "mc_gb300.hpp")]
 
 
 def up_to_date() -> bool:
     if not os.path.exists(LIB):
+        return False
+    if not os.path.exists(MAIN):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(s) <= t for s in _sources() if os.path.exists(s))
@@ -55,7 +58,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
     def one(item):
         src, extra = item
         obj = os.path.join(OUT, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *COMMON, *extra, *os.environ.get("MC_NVCC_FLAGS", "").split(), "-c",
+               os.path.join(CSRC, src), "-o", obj]
         if ptxas_v:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -73,6 +77,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # C++ driver over the C++ mirror of the reference API
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", os.path.join(CSRC, "mc_main.cpp"), "-I", os.path.join(HERE, "..", "include"),
+           "-L", OUT, "-lmc_gb300", "-Wl,-rpath,$ORIGIN", "-o", MAIN]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"mc_main build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -527,7 +527,7 @@ int setupSession(mc_session_s* S) {
     const mc_domain_s& D = *S->dom;
     const size_t nt = (size_t)m.nw * m.np;
     // tables
-    size_t tb = 2 * sizeof(R) * nt + sizeof(unsigned long long) * (2 * m.nw + 2 * nt) + 64;
+    size_t tb = 2 * sizeof(R) * nt + sizeof(unsigned long long) * (2 * m.nw + 2 * nt) + 2 * GUIDE + 128;
     CK(cudaMalloc(&S->tables, tb));
     char* base = (char*)S->tables;
     std::vector<R> vel(nt), vt(nt);
@@ -542,12 +542,24 @@ int setupSession(mc_session_s* S) {
     P.pthr = (unsigned long long*)base; base += 8 * nt;
     P.fwthr = (unsigned long long*)base; base += 8 * m.nw;
     P.fpthr = (unsigned long long*)base; base += 8 * nt;
+    P.wguide = (const uint16_t*)base; base += 2 * GUIDE;
     CK(cudaMemcpy((void*)P.vel, vel.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.vt, vt.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.wthr, m.swthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.pthr, m.spthr.data(), 8 * nt, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.fwthr, m.fwthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.fpthr, m.fpthr.data(), 8 * nt, cudaMemcpyHostToDevice));
+    {
+        // guide table: first bin whose threshold exceeds k * 2^32 / GUIDE
+        std::vector<uint16_t> g(GUIDE);
+        for (int k = 0; k < GUIDE; ++k) {
+            const unsigned long long x = (unsigned long long)k << (32 - GUIDE_BITS);
+            long i = 0;
+            while (i < m.nw - 1 && x >= m.swthr[i]) ++i;
+            g[k] = (uint16_t)i;
+        }
+        CK(cudaMemcpy((void*)P.wguide, g.data(), 2 * GUIDE, cudaMemcpyHostToDevice));
+    }
     // domain
     std::vector<SdomD<R>> sd(D.sd.size());
     for (size_t i = 0; i < sd.size(); ++i) castSdom(D.sd[i], sd[i], sizeof(R) == 4);
@@ -636,7 +648,12 @@ int setupSession(mc_session_s* S) {
     const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
     S->tm = S->desc.tally_mode;
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
-    S->smem = smemTableBytes<R>((int)m.nw, (int)m.np) + (S->tm == TM_SHARED ? tallyB : 0);
+    {
+        const int nsdShared = sizeof(SdomD<R>) * D.sd.size() <= SD_SHARED_MAX ? (int)D.sd.size() : 0;
+        SmemLayout L;
+        L.init<R>((int)m.nw, (int)m.np, nsdShared, S->rows, (int)D.cols, S->tm == TM_SHARED);
+        S->smem = L.total;
+    }
     if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
     S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
     if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");

@@ -57,6 +57,7 @@ struct Params {
     const R* vel;   // nw x np
     const R* vt;    // vel * tau, nw x np
     const unsigned long long* wthr;   // scatter bin thresholds, nw
+    const uint16_t* wguide;           // scatter bin guide table, GUIDE entries
     const unsigned long long* pthr;   // scatter branch thresholds, nw x np
     const unsigned long long* fwthr;  // flux (emission) bin thresholds
     const unsigned long long* fpthr;
@@ -264,6 +265,16 @@ __device__ __forceinline__ int searchThr(const unsigned long long* thr, int n, u
     }
     return lo < n ? lo : n - 1;
 }
+// Guide-table search (Chen and Asau's indexed search): guide[k] is the
+// answer for x = k * 2^32 / GUIDE, a lower bound for every x in slot k, so a
+// short upward scan finishes the search.
+constexpr int GUIDE_BITS = 10;
+constexpr int GUIDE = 1 << GUIDE_BITS;
+__device__ __forceinline__ int searchGuided(const unsigned long long* thr, const uint16_t* guide, int n, uint32_t x) {
+    int i = guide[x >> (32 - GUIDE_BITS)];
+    while (i < n - 1 && (unsigned long long)x >= thr[i]) ++i;
+    return i;
+}
 __device__ __forceinline__ int searchBranch(const unsigned long long* thr, int np, uint32_t x) {
     for (int j = 0; j < np - 1; ++j)
         if ((unsigned long long)x < thr[j]) return j;
@@ -315,19 +326,33 @@ struct Smem {
     R* vel;
     R* vt;
     unsigned long long* wthr;
-    long long* tal;   // rows x cols fixed-point partial field (r * cols + c)
-    long long* dif;   // rows x (cols + 1) difference array, fixed point
+    uint16_t* wguide;
+    const SdomD<R>* sd;  // subdomains (shared when they fit, else global)
+    long long* tal;      // rows x cols fixed-point partial field (r * cols + c)
+    long long* dif;      // rows x (cols + 1) difference array, fixed point
 };
 
-// Shared layout sizes (bytes): velocity and vel*tau tables, the scatter
-// bin thresholds, then the block's tally.
-template <typename R>
-__host__ __device__ inline size_t smemTableBytes(int nw, int np) {
-    size_t b = 2 * sizeof(R) * (size_t)nw * np;
-    b = (b + 15) & ~(size_t)15;
-    b += sizeof(unsigned long long) * (size_t)nw;
-    return (b + 15) & ~(size_t)15;
-}
+// Shared layout: vel and vel*tau tables, the scatter bin thresholds and
+// guide table, the subdomains (when staged), then the block's tally.
+struct SmemLayout {
+    size_t vel, vt, wthr, guide, sd, tal, total;
+    template <typename R>
+    __host__ __device__ void init(int nw, int np, int nsdShared, int rows, int cols, bool sharedTally) {
+        auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+        const size_t nt = (size_t)nw * np;
+        vel = 0;
+        vt = vel + sizeof(R) * nt;
+        wthr = al(vt + sizeof(R) * nt);
+        guide = al(wthr + sizeof(unsigned long long) * (size_t)nw);
+        sd = al(guide + sizeof(uint16_t) * GUIDE);
+        tal = al(sd + sizeof(SdomD<R>) * (size_t)nsdShared);
+        total = tal + (sharedTally ? sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1) : 0);
+    }
+};
+
+// Subdomain images staged in shared memory up to this many bytes.
+constexpr size_t SD_SHARED_MAX = 32 * 1024;
+
 __host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
     return sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1);
 }
@@ -340,6 +365,12 @@ enum { TM_SHARED = 0, TM_GLOBAL = 1 };
 // Hard cap on events one thread processes in one launch (a guard: a
 // phonon that reaches it is killed and flagged non-finite).
 constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
+
+// Resident blocks of 256 threads per SM the FP32 advance kernels are
+// compiled for (register budget 65536 / (256 x this)).
+#ifndef MC_MIN_BLOCKS_F32
+#define MC_MIN_BLOCKS_F32 4
+#endif
 
 template <typename R>
 struct Phn {
@@ -367,6 +398,18 @@ __device__ __forceinline__ long long toFixed(float v) {
 }
 __device__ __forceinline__ long long toFixed(double v) { return __double2ll_rn(v); }
 
+// float -> double by moving the bits (the conversion instruction runs on
+// GB300's narrow FP64 pipe); zero and subnormal inputs give zero.
+__device__ __forceinline__ double toDouble(float v) {
+    const uint32_t b = __float_as_uint(v);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if (e == 0u) return 0.0;
+    const uint32_t m = b & 0x7FFFFFu;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
+}
+__device__ __forceinline__ double toDouble(double v) { return v; }
+
 template <typename R, int TM>
 struct Tally {
     const Params<R>* P;
@@ -388,7 +431,7 @@ struct Tally {
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < rows) atomicAdd(&P->tally[(size_t)col * rows + r], (double)(rho[r] * t));
+            if (r < rows) atomicAdd(&P->tally[(size_t)col * rows + r], toDouble(rho[r] * t));
     }
 };
 
@@ -700,7 +743,7 @@ struct Walker {
         ph.nloop = A2.w;
         g.init(P.key0, P.key1, ph.id, &P);
         budget = W.len;
-        S = &P.sd[ph.s];
+        S = &sm.sd[ph.s];
         reducedVel(*S, ph.d, a, ia);
         v = sm.vel[ph.w * P.np + ph.p];
         iv = R(1) / v;
@@ -803,7 +846,7 @@ struct Walker {
                     // same axis, tangential cells unchanged: keep the split
                     // coordinates, move onto the paired face
                     ph.s = F.to;
-                    S = &P.sd[ph.s];
+                    S = &sm.sd[ph.s];
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         if (F.toface == j) { ph.idx[j] = 0; ph.off[j] = R(0); }
@@ -815,7 +858,7 @@ struct Walker {
                     rotate(F.A, u, u2);
                     for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
                     ph.s = F.to;
-                    S = &P.sd[ph.s];
+                    S = &sm.sd[ph.s];
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         if (F.toface == j) u2[j] = R(0);
@@ -840,7 +883,7 @@ struct Walker {
         } else {
             // Material::scatter (montecarlo/material.cpp:298-303)
             uint32_t x1 = g.next(), x2 = g.next();
-            ph.w = searchThr(sm.wthr, P.nw, x1);
+            ph.w = searchGuided(sm.wthr, sm.wguide, P.nw, x1);
             ph.p = searchBranch(P.pthr + ph.w * P.np, P.np, x2);
             drawIso<R>(g, ph.d);
             normalize(ph.d);
@@ -897,22 +940,35 @@ struct Walker {
     }
 };
 
-// Stage the material tables (and zero the block's tally) in shared memory.
+// Stage the material tables, the subdomains and (zeroed) the block's tally
+// in shared memory.
 template <typename R, int TM>
 __device__ __forceinline__ void stageTables(const Params<R>& P, Smem<R>& sm, unsigned char* smraw) {
     const int nt = P.nw * P.np;
-    sm.vel = reinterpret_cast<R*>(smraw);
-    sm.vt = sm.vel + nt;
-    size_t off = (2 * sizeof(R) * (size_t)nt + 15) & ~(size_t)15;
-    sm.wthr = reinterpret_cast<unsigned long long*>(smraw + off);
-    const size_t tb = smemTableBytes<R>(P.nw, P.np);
-    sm.tal = reinterpret_cast<long long*>(smraw + tb);
+    const int nsdShared = (size_t)P.nsd * sizeof(SdomD<R>) <= SD_SHARED_MAX ? P.nsd : 0;
+    SmemLayout L;
+    L.init<R>(P.nw, P.np, nsdShared, P.rows, P.cols, TM == TM_SHARED);
+    sm.vel = reinterpret_cast<R*>(smraw + L.vel);
+    sm.vt = reinterpret_cast<R*>(smraw + L.vt);
+    sm.wthr = reinterpret_cast<unsigned long long*>(smraw + L.wthr);
+    sm.wguide = reinterpret_cast<uint16_t*>(smraw + L.guide);
+    sm.tal = reinterpret_cast<long long*>(smraw + L.tal);
     sm.dif = sm.tal + (size_t)P.rows * P.cols;
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         sm.vel[i] = P.vel[i];
         sm.vt[i] = P.vt[i];
     }
     for (int i = threadIdx.x; i < P.nw; i += blockDim.x) sm.wthr[i] = P.wthr[i];
+    for (int i = threadIdx.x; i < GUIDE; i += blockDim.x) sm.wguide[i] = P.wguide[i];
+    if (nsdShared) {
+        const int nw4 = (int)(sizeof(SdomD<R>) * nsdShared / 4);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smraw + L.sd);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(P.sd);
+        for (int i = threadIdx.x; i < nw4; i += blockDim.x) dst[i] = src[i];
+        sm.sd = reinterpret_cast<const SdomD<R>*>(smraw + L.sd);
+    } else {
+        sm.sd = P.sd;
+    }
     if (TM == TM_SHARED) {
         const int nz = P.rows * (2 * P.cols + 1);
         for (int i = threadIdx.x; i < nz; i += blockDim.x) sm.tal[i] = 0;
@@ -975,7 +1031,7 @@ __device__ __forceinline__ void closeBlock(const Params<R>& P, const Smem<R>& sm
 // survivors are compacted to the two ends of the other half of the
 // ping-pong state (front: next event inside the next window).
 template <typename R, bool REPLAY, bool LOG, int TM>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_advance(Params<R> P) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance(Params<R> P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     Smem<R> sm;
     stageTables<R, TM>(P, sm, smraw);
@@ -1041,7 +1097,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_advance(Params<
 constexpr int REFILL = 8;
 
 template <typename R, bool REPLAY, bool LOG, int TM>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_advance_dyn(Params<R> P) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ unsigned long long qnext;
     Smem<R> sm;

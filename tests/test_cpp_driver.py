@@ -1,0 +1,56 @@
+"""The C++ driver (reference CLI grammar, C++ mirror of the reference API
+over the C ABI): builds, fails loudly without a device, and on a GPU gives
+the same field as the Python binding for the same seed."""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import montecarlocpp_gb300 as M
+from montecarlocpp_gb300 import build as B
+
+
+def _run(tmp_path, *extra):
+    M.write_material_files(str(tmp_path))
+    B.build()
+    cmd = [B.MAIN, str(tmp_path), "silicon", "300", "film", "1e-7", "1e-7", "10", "multi", "500", "1000000", "0",
+           "1", "5e-13", "100", "64", "3", *extra]
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a CUDA device is present")
+def test_driver_fails_loudly_without_device(tmp_path):
+    r = _run(tmp_path)
+    assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+def test_driver_rejects_bad_arguments(tmp_path):
+    M.write_material_files(str(tmp_path))
+    B.build()
+    r = subprocess.run([B.MAIN, str(tmp_path), "silicon", "300", "hex", "1", "2"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Invalid domain" in r.stderr
+    r = subprocess.run([B.MAIN, "/nonexistent/dir", "silicon", "300"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Invalid directory" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_matches_python_binding(tmp_path, gmat):
+    r = _run(tmp_path)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip() and not ln.startswith("Solution")]
+    field = np.array([[float(x) for x in ln.split()] for ln in lines])
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 10)
+    P = M.MultiProblem(gmat, dom, 500, 1000000)
+    ref = P.solve(dt=5e-13, nsteps=100, precision=64, seed=3)
+    assert field.shape == ref.shape
+    assert np.allclose(field, ref, rtol=1e-8, atol=1e-8 * np.abs(ref).max())
