@@ -172,6 +172,41 @@ int mc_session_result(mc_session_h s, double* out, mc_stats* st);
 size_t mc_session_state_bytes(mc_session_h s);
 void mc_session_destroy(mc_session_h s);
 
+/* ------------------------------------------------------------ batches */
+/* Many solves -- each its own Material, Domain and problem, with uneven
+ * phonon counts -- run to one time horizon in ONE persistent kernel launch
+ * per window: each lane takes a phonon of any instance and works against
+ * that instance's tables, geometry and field. With use_graph the launch
+ * sequence is captured into a CUDA graph on the first run and replayed. */
+typedef struct mc_batch_s* mc_batch_h;
+
+typedef struct {
+    double dt;              /* shared time step, s                         */
+    long nsteps;            /* shared horizon = nsteps * dt                */
+    int precision;          /* 32 or 64                                    */
+    int steps_per_launch;   /* 0: the whole horizon in one launch          */
+    int block_size;         /* 0 -> 256                                    */
+    int grid_blocks;        /* 0 -> resident blocks x SMs                  */
+    int use_graph;          /* capture and replay the launch sequence      */
+    void* stream;           /* cudaStream_t; NULL -> library stream        */
+} mc_batch_desc;
+
+/* n instances; from probs[i] the batch uses problem, nemit, maxscat,
+ * maxloop and seed (the time and launch fields come from bd). */
+int mc_batch_create(int n, const mc_material_h* mats, const mc_domain_h* doms, const mc_problem_desc* probs,
+                    const mc_batch_desc* bd, mc_batch_h* out);
+/* Emission, every window and the field finish of all instances;
+ * asynchronous on the batch stream. */
+int mc_batch_run(mc_batch_h b);
+/* Synchronise; instance i's field (rows x cols, column-major, as mc_solve)
+ * and its stats (nemit, power, rows, cols, checksum; counters are
+ * batch-wide). out may be NULL. */
+int mc_batch_result(mc_batch_h b, int i, double* out, mc_stats* st);
+/* Batch-wide counters of the last run (synchronises). */
+int mc_batch_stats(mc_batch_h b, mc_stats* st);
+size_t mc_batch_state_bytes(mc_batch_h b);
+void mc_batch_destroy(mc_batch_h b);
+
 #ifdef __cplusplus
 }
 #endif

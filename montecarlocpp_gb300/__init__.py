@@ -6,6 +6,7 @@ ABI in include/mc_gb300.h). This package mirrors the reference's host API
 (Material, *Domain, Temp/Flux/MultiProblem) over that ABI.
 """
 
+from .batch import Batch
 from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PERI, RIG, SPEC, TOP, BulkDomain,
                       CrossPlaneFilmDomain, Domain, FilmDomain, Pair, Parallelepiped, PoreCellDomain)
 from .materials import SiliconModel, silicon_tables, write_material_files
@@ -17,5 +18,5 @@ __all__ = [
     "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "Pair",
     "Parallelepiped", "SiliconModel", "silicon_tables", "write_material_files", "Material",
     "TempProblem", "FluxProblem", "MultiProblem", "Session", "TEMP", "FLUX", "MULTI",
-    "kappa_from_flux",
+    "kappa_from_flux", "Batch",
 ]

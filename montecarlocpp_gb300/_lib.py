@@ -54,6 +54,12 @@ class Stats(C.Structure):
         return d
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [("dt", C.c_double), ("nsteps", C.c_long), ("precision", C.c_int),
+                ("steps_per_launch", C.c_int), ("block_size", C.c_int), ("grid_blocks", C.c_int),
+                ("use_graph", C.c_int), ("stream", C.c_void_p)]
+
+
 # every symbol declared in include/mc_gb300.h
 SYMBOLS = [
     "mc_last_error", "mc_version",
@@ -63,6 +69,8 @@ SYMBOLS = [
     "mc_solve",
     "mc_session_create", "mc_session_emit", "mc_session_advance", "mc_session_result",
     "mc_session_state_bytes", "mc_session_destroy",
+    "mc_batch_create", "mc_batch_run", "mc_batch_result", "mc_batch_stats", "mc_batch_state_bytes",
+    "mc_batch_destroy",
 ]
 
 _lib = None
@@ -106,6 +114,14 @@ def lib(build_if_missing: bool = True):
     L.mc_session_state_bytes.restype = C.c_size_t
     L.mc_session_state_bytes.argtypes = [C.c_void_p]
     L.mc_session_destroy.argtypes = [C.c_void_p]
+    L.mc_batch_create.argtypes = [C.c_int, P(C.c_void_p), P(C.c_void_p), P(ProblemDesc), P(BatchDesc),
+                                  P(C.c_void_p)]
+    L.mc_batch_run.argtypes = [C.c_void_p]
+    L.mc_batch_result.argtypes = [C.c_void_p, C.c_int, P(C.c_double), P(Stats)]
+    L.mc_batch_stats.argtypes = [C.c_void_p, P(Stats)]
+    L.mc_batch_state_bytes.restype = C.c_size_t
+    L.mc_batch_state_bytes.argtypes = [C.c_void_p]
+    L.mc_batch_destroy.argtypes = [C.c_void_p]
     _lib = L
     return L
 

@@ -521,20 +521,18 @@ struct mc_session_s {
 
 namespace {
 
+// Material tables in the flight precision, thresholds, guide table: one
+// device allocation; fills the table pointers of P.
 template <typename R>
-int setupSession(mc_session_s* S) {
-    const mc_material_s& m = *S->mat;
-    const mc_domain_s& D = *S->dom;
+int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vmax) {
     const size_t nt = (size_t)m.nw * m.np;
-    // tables
     size_t tb = 2 * sizeof(R) * nt + sizeof(unsigned long long) * (2 * m.nw + 2 * nt) + 2 * GUIDE + 128;
-    CK(cudaMalloc(&S->tables, tb));
-    char* base = (char*)S->tables;
+    CK(cudaMalloc(buf, tb));
+    char* base = (char*)*buf;
     std::vector<R> vel(nt), vt(nt);
     for (size_t i = 0; i < nt; ++i) { vel[i] = (R)m.vel[i]; vt[i] = (R)(m.vel[i] * m.tau[i]); }
-    S->vmax = 0.;
-    for (size_t i = 0; i < nt; ++i) S->vmax = std::max(S->vmax, m.vel[i]);
-    Params<R> P{};
+    vmax = 0.;
+    for (size_t i = 0; i < nt; ++i) vmax = std::max(vmax, m.vel[i]);
     P.vel = (R*)base; base += sizeof(R) * nt;
     P.vt = (R*)base; base += sizeof(R) * nt;
     base = (char*)(((uintptr_t)base + 15) & ~(uintptr_t)15);
@@ -560,14 +558,22 @@ int setupSession(mc_session_s* S) {
         }
         CK(cudaMemcpy((void*)P.wguide, g.data(), 2 * GUIDE, cudaMemcpyHostToDevice));
     }
-    // domain
+    P.nw = (int)m.nw;
+    P.np = (int)m.np;
+    return MC_OK;
+}
+
+// Subdomain images, emitters and the phonon allocation of a requested
+// count (montecarlo/problem.cpp:315-342); fills P.sd / em / emitCdf.
+template <typename R>
+int uploadDomain(const mc_domain_s& D, double fluxSum, long nemitReq, void** sd_d, EmitterD** em_d,
+                 long long** cdf_d, Params<R>& P, long& nemit, double& power) {
     std::vector<SdomD<R>> sd(D.sd.size());
     for (size_t i = 0; i < sd.size(); ++i) castSdom(D.sd[i], sd[i], sizeof(R) == 4);
-    CK(cudaMalloc(&S->dom_d, sizeof(SdomD<R>) * sd.size()));
-    CK(cudaMemcpy(S->dom_d, sd.data(), sizeof(SdomD<R>) * sd.size(), cudaMemcpyHostToDevice));
-    P.sd = (const SdomD<R>*)S->dom_d;
+    CK(cudaMalloc(sd_d, sizeof(SdomD<R>) * sd.size()));
+    CK(cudaMemcpy(*sd_d, sd.data(), sizeof(SdomD<R>) * sd.size(), cudaMemcpyHostToDevice));
+    P.sd = (const SdomD<R>*)*sd_d;
     P.nsd = (int)sd.size();
-    // emitters: rounded phonon counts (montecarlo/problem.cpp:319-341)
     const long ne = (long)D.em.size();
     if (ne == 0) return fail(MC_ERR_ARG, "No phonons to emit");
     double wsum = 0.;
@@ -576,20 +582,33 @@ int setupSession(mc_session_s* S) {
     long long tot = 0;
     for (long i = 0; i < ne; ++i) {
         double frac = D.emWeight[i] / wsum;
-        double rounded = std::ceil(frac * S->desc.nemit - 0.5);
+        double rounded = std::ceil(frac * nemitReq - 0.5);
         tot += std::max(1LL, (long long)rounded);
         cdf[i] = tot;
     }
-    S->nemit = (long)tot;
-    S->power = wsum / (double)tot * m.fluxSum / 4.;
+    nemit = (long)tot;
+    power = wsum / (double)tot * fluxSum / 4.;
     for (long i = 0; i < ne; ++i)
         if (!(D.emWeight[i] > 0.)) return fail(MC_ERR_ARG, "No phonons to emit");
-    CK(cudaMalloc(&S->em_d, sizeof(EmitterD) * ne));
-    CK(cudaMemcpy(S->em_d, D.em.data(), sizeof(EmitterD) * ne, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&S->cdf_d, sizeof(long long) * ne));
-    CK(cudaMemcpy(S->cdf_d, cdf.data(), sizeof(long long) * ne, cudaMemcpyHostToDevice));
-    P.em = S->em_d; P.emitCdf = S->cdf_d; P.nem = (int)ne;
-    P.nw = (int)m.nw; P.np = (int)m.np;
+    CK(cudaMalloc(em_d, sizeof(EmitterD) * ne));
+    CK(cudaMemcpy(*em_d, D.em.data(), sizeof(EmitterD) * ne, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(cdf_d, sizeof(long long) * ne));
+    CK(cudaMemcpy(*cdf_d, cdf.data(), sizeof(long long) * ne, cudaMemcpyHostToDevice));
+    P.em = *em_d;
+    P.emitCdf = *cdf_d;
+    P.nem = (int)ne;
+    return MC_OK;
+}
+
+template <typename R>
+int setupSession(mc_session_s* S) {
+    const mc_material_s& m = *S->mat;
+    const mc_domain_s& D = *S->dom;
+    Params<R> P{};
+    int rc = uploadMaterial<R>(m, &S->tables, P, S->vmax);
+    if (rc) return rc;
+    rc = uploadDomain<R>(D, m.fluxSum, S->desc.nemit, &S->dom_d, &S->em_d, &S->cdf_d, P, S->nemit, S->power);
+    if (rc) return rc;
     // state: two halves of (P0, P1, P2)
     const size_t n = (size_t)S->nemit;
     using V4 = typename Vec4<R>::T;
@@ -843,6 +862,225 @@ void freeSession(mc_session_s* S) {
 
 }  // namespace
 
+// ================================================================ batches
+struct mc_batch_s {
+    int n = 0;
+    int prec = 32;
+    mc_batch_desc bd{};
+    std::vector<mc_material_h> mats;
+    std::vector<mc_domain_h> doms;
+    std::vector<mc_problem_desc> probs;
+    // per instance
+    std::vector<void*> tables, sd;
+    std::vector<EmitterD*> em;
+    std::vector<long long*> cdf;
+    std::vector<long> nemit;
+    std::vector<double> power;
+    std::vector<int> rows, cols;
+    std::vector<size_t> fieldOff;   // offset of the instance's field block in `fields`
+    // device
+    double* fields = nullptr;       // per instance: rows x cols, rows x (cols+1) difference, 4 checksums
+    size_t fieldDoubles = 0;
+    void* insts = nullptr;
+    long long* islot = nullptr;
+    void* state = nullptr;
+    size_t stateBytes = 0;
+    unsigned long long* cnt = nullptr;
+    unsigned int* status = nullptr;
+    long long cap = 0;
+    int block = 256, grid = 0;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+    Params<float> p32{};
+    Params<double> p64{};
+};
+
+namespace {
+
+void freeBatch(mc_batch_s* B) {
+    if (!B) return;
+    for (void* p : B->tables) if (p) cudaFree(p);
+    for (void* p : B->sd) if (p) cudaFree(p);
+    for (auto* p : B->em) if (p) cudaFree(p);
+    for (auto* p : B->cdf) if (p) cudaFree(p);
+    void* ps[] = {B->fields, B->insts, B->islot, B->state, B->cnt, B->status};
+    for (void* p : ps) if (p) cudaFree(p);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->ownStream && B->stream) cudaStreamDestroy(B->stream);
+    delete B;
+}
+
+template <typename R>
+Params<R>& batchParams(mc_batch_s* B);
+template <> Params<float>& batchParams<float>(mc_batch_s* B) { return B->p32; }
+template <> Params<double>& batchParams<double>(mc_batch_s* B) { return B->p64; }
+
+template <typename R>
+int setupBatch(mc_batch_s* B) {
+    const int n = B->n;
+    B->tables.assign(n, nullptr); B->sd.assign(n, nullptr); B->em.assign(n, nullptr); B->cdf.assign(n, nullptr);
+    B->nemit.assign(n, 0); B->power.assign(n, 0.); B->rows.assign(n, 1); B->cols.assign(n, 0);
+    B->fieldOff.assign(n, 0);
+    std::vector<InstD<R>> inst(n);
+    std::vector<long long> islot(n + 1, 0);
+    const int K = B->bd.steps_per_launch > 0 ? B->bd.steps_per_launch : (int)B->bd.nsteps;
+    const double window = (double)std::min<long>(K, B->bd.nsteps) * B->bd.dt;
+    // fields: one allocation
+    size_t off = 0;
+    for (int i = 0; i < n; ++i) {
+        const mc_problem_desc& p = B->probs[i];
+        B->rows[i] = p.problem == MC_TEMP ? 1 : (p.problem == MC_FLUX ? 3 : 4);
+        B->cols[i] = (int)B->doms[i]->cols;
+        B->fieldOff[i] = off;
+        off += (size_t)B->rows[i] * B->cols[i] + (size_t)B->rows[i] * (B->cols[i] + 1) + 4;
+    }
+    B->fieldDoubles = off;
+    CK(cudaMalloc(&B->fields, sizeof(double) * std::max<size_t>(off, 1)));
+    for (int i = 0; i < n; ++i) {
+        const mc_material_s& m = *B->mats[i];
+        const mc_domain_s& D = *B->doms[i];
+        const mc_problem_desc& pd = B->probs[i];
+        Params<R> P{};
+        double vmax = 0.;
+        int rc = uploadMaterial<R>(m, &B->tables[i], P, vmax);
+        if (rc) return rc;
+        rc = uploadDomain<R>(D, m.fluxSum, pd.nemit, &B->sd[i], &B->em[i], &B->cdf[i], P, B->nemit[i], B->power[i]);
+        if (rc) return rc;
+        islot[i + 1] = islot[i] + B->nemit[i];
+        InstD<R>& I = inst[i];
+        std::memset(&I, 0, sizeof(I));
+        I.vel = P.vel; I.vt = P.vt; I.wthr = P.wthr; I.wguide = P.wguide; I.pthr = P.pthr;
+        I.fwthr = P.fwthr; I.fpthr = P.fpthr;
+        I.sd = P.sd; I.em = P.em; I.emitCdf = P.emitCdf;
+        I.nw = P.nw; I.np = P.np; I.nem = P.nem; I.nsd = P.nsd;
+        I.problem = pd.problem; I.rows = B->rows[i]; I.cols = B->cols[i]; I.inst = i;
+        I.maxscat = pd.maxscat;
+        I.maxloop = pd.maxloop != 0 ? pd.maxloop : 100 * pd.maxscat;
+        I.slot0 = islot[i]; I.nemit = B->nemit[i];
+        I.key0 = (uint32_t)pd.seed; I.key1 = (uint32_t)(pd.seed >> 32);
+        double* f = B->fields + B->fieldOff[i];
+        I.tally = f;
+        bool oneD = false;
+        for (const auto& sd : D.sd) oneD = oneD || (sd.accum >= 0 && sd.accum <= 2);
+        I.gdif = oneD ? f + (size_t)I.rows * I.cols : nullptr;
+        I.csum = f + (size_t)I.rows * I.cols + (size_t)I.rows * (I.cols + 1);
+        for (int r = 0; r < 4; ++r) {
+            const bool timeRow = (pd.problem == MC_TEMP || pd.problem == MC_MULTI) && r == 0;
+            const double q = std::ldexp(window * (timeRow ? 1.0 : vmax) * 1.0001, -61);
+            I.tq[r] = q;
+            I.tqinv[r] = (R)(1.0 / q);
+        }
+        if (pd.maxscat <= 0 || pd.maxloop < 0 || pd.nemit <= 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
+        if (pd.problem < MC_TEMP || pd.problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+    }
+    B->cap = islot[n];
+    CK(cudaMalloc(&B->insts, sizeof(InstD<R>) * n));
+    CK(cudaMemcpy(B->insts, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&B->islot, sizeof(long long) * (n + 1)));
+    CK(cudaMemcpy(B->islot, islot.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice));
+    // state: one half, updated in place
+    using V4 = typename Vec4<R>::T;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t cap = (size_t)B->cap;
+    B->stateBytes = (2 * sizeof(V4) + sizeof(uint4)) * cap;
+    CK(cudaMalloc(&B->state, 2 * al(sizeof(V4) * cap) + al(sizeof(uint4) * cap)));
+    char* sb = (char*)B->state;
+    Params<R>& P = batchParams<R>(B);
+    P = Params<R>{};
+    P.P0in = P.P0out = (V4*)sb; sb += al(sizeof(V4) * cap);
+    P.P1in = P.P1out = (V4*)sb; sb += al(sizeof(V4) * cap);
+    P.P2in = P.P2out = (uint4*)sb;
+    CK(cudaMalloc(&B->cnt, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
+    CK(cudaMalloc(&B->status, sizeof(unsigned int)));
+    P.counters = B->cnt;
+    P.status = B->status;
+    P.live_in = B->cnt + C_NCOUNTERS;
+    P.live_out = B->cnt + C_NCOUNTERS + 1;
+    P.cap = (unsigned long long)cap;
+    P.dt = (R)B->bd.dt;
+    P.nsteps = (int)B->bd.nsteps;
+    P.ksteps = K;
+    P.insts = (const InstD<R>*)B->insts;
+    P.islot = B->islot;
+    P.ninst = n;
+    if (batchSmemBytes<R>(n) > 200 * 1024) return fail(MC_ERR_UNSUPPORTED, "too many instances in one batch");
+    B->block = B->bd.block_size > 0 ? B->bd.block_size : 256;
+    if (B->block % 32 || B->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int occ = advanceBatchOccupancy<R>(n, B->block);
+    if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
+    B->grid = B->bd.grid_blocks > 0 ? B->bd.grid_blocks : occ * nsm;
+    return MC_OK;
+}
+
+// The launch sequence of one batched run (captured into a graph or issued
+// directly).
+template <typename R>
+int enqueueBatch(mc_batch_s* B) {
+    Params<R> P = batchParams<R>(B);
+    CK(cudaMemsetAsync(B->fields, 0, sizeof(double) * B->fieldDoubles, B->stream));
+    CK(cudaMemsetAsync(B->cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), B->stream));
+    CK(cudaMemsetAsync(B->status, 0, sizeof(unsigned int), B->stream));
+    CK(launchEmitBatch<R>(P, B->stream));
+    int launches = 1;
+    for (int step = 0; step < (int)B->bd.nsteps; step += P.ksteps) {
+        P.step0 = step;
+        CK(cudaMemsetAsync(B->cnt + C_NCOUNTERS + 1, 0, sizeof(unsigned long long), B->stream));
+        CK(launchAdvanceBatch<R>(P, B->grid, B->block, B->stream));
+        ++launches;
+    }
+    CK(launchDifPrefix<R>(P, B->stream));
+    B->launches = launches + 1;
+    return MC_OK;
+}
+
+template <typename R>
+int runBatch(mc_batch_s* B) {
+    if (!B->bd.use_graph) return enqueueBatch<R>(B);
+    if (!B->exec) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueueBatch<R>(B);
+        cudaError_t e = cudaStreamEndCapture(B->stream, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return cudaFail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&B->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cudaFail(e, "cudaGraphInstantiate");
+    }
+    CK(cudaGraphLaunch(B->exec, B->stream));
+    return MC_OK;
+}
+
+int batchCounters(mc_batch_s* B, mc_stats* st) {
+    CK(cudaStreamSynchronize(B->stream));
+    std::vector<unsigned long long> c(C_NCOUNTERS + 4);
+    unsigned int status = 0;
+    CK(cudaMemcpy(c.data(), B->cnt, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&status, B->status, sizeof(status), cudaMemcpyDeviceToHost));
+    std::memset(st, 0, sizeof(*st));
+    st->nemit = (long)B->cap;
+    st->phonon_steps = (double)c[C_PHONON_STEPS];
+    st->events = (long)c[C_EVENTS];
+    st->scatters = (long)c[C_SCATTERS];
+    st->escapes = (long)c[C_ESCAPES];
+    st->horizon_stops = (long)c[C_HORIZON];
+    st->maxscat_stops = (long)c[C_MAXSCAT];
+    st->maxloop_stops = (long)c[C_MAXLOOP];
+    st->absorbed = (long)c[C_ABSORBED];
+    st->nonfinite = (long)c[C_BAD];
+    st->status = status;
+    st->launches = B->launches;
+    if (status & S_NONFINITE) return fail(MC_ERR_NONFINITE, "non-finite phonon state");
+    return MC_OK;
+}
+
+}  // namespace
+
 // ================================================================== C ABI
 extern "C" {
 
@@ -974,4 +1212,79 @@ int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* o
     return rc;
 }
 
+
+int mc_batch_create(int n, const mc_material_h* mats, const mc_domain_h* doms, const mc_problem_desc* probs,
+                    const mc_batch_desc* bd, mc_batch_h* out) {
+    if (n <= 0 || !mats || !doms || !probs || !bd || !out) return fail(MC_ERR_ARG, "invalid batch arguments");
+    for (int i = 0; i < n; ++i)
+        if (!mats[i] || !doms[i]) return fail(MC_ERR_ARG, "null material or domain in batch");
+    if (!(bd->dt > 0.) || bd->nsteps <= 0 || bd->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
+    if (bd->precision != 32 && bd->precision != 64) return fail(MC_ERR_ARG, "precision must be 32 or 64");
+    if (bd->steps_per_launch < 0) return fail(MC_ERR_ARG, "steps_per_launch must be >= 0");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    mc_batch_s* B = new mc_batch_s;
+    B->n = n;
+    B->prec = bd->precision;
+    B->bd = *bd;
+    B->mats.assign(mats, mats + n);
+    B->doms.assign(doms, doms + n);
+    B->probs.assign(probs, probs + n);
+    if (bd->stream) B->stream = (cudaStream_t)bd->stream;
+    else {
+        cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete B; return cudaFail(e, "cudaStreamCreate"); }
+        B->ownStream = true;
+    }
+    rc = B->prec == 32 ? setupBatch<float>(B) : setupBatch<double>(B);
+    if (rc) { std::string msg = g_err; freeBatch(B); g_err = msg; return rc; }
+    *out = B;
+    return MC_OK;
+}
+
+int mc_batch_run(mc_batch_h b) {
+    if (!b) return fail(MC_ERR_ARG, "null batch");
+    return b->prec == 32 ? runBatch<float>(b) : runBatch<double>(b);
+}
+
+int mc_batch_result(mc_batch_h b, int i, double* out, mc_stats* st) {
+    if (!b || i < 0 || i >= b->n) return fail(MC_ERR_ARG, "invalid batch instance");
+    CK(cudaStreamSynchronize(b->stream));
+    const int rows = b->rows[i], cols = b->cols[i];
+    std::vector<double> f((size_t)rows * cols + (size_t)rows * (cols + 1) + 4);
+    CK(cudaMemcpy(f.data(), b->fields + b->fieldOff[i], sizeof(double) * f.size(), cudaMemcpyDeviceToHost));
+    const mc_material_s& m = *b->mats[i];
+    const mc_domain_s& D = *b->doms[i];
+    const int problem = b->probs[i].problem;
+    if (out) {
+        for (int c = 0; c < cols; ++c)
+            for (int r = 0; r < rows; ++r) {
+                double v = f[(size_t)c * rows + r];
+                if (problem == MC_TEMP || (problem == MC_MULTI && r == 0)) v = v / m.energySum;
+                out[(size_t)c * rows + r] = b->power[i] * (v / D.cellVol[c]);
+            }
+    }
+    if (st) {
+        int rc = batchCounters(b, st);
+        st->nemit = b->nemit[i];
+        st->power = b->power[i];
+        st->rows = rows;
+        st->cols = cols;
+        const double* cs = f.data() + (size_t)rows * cols + (size_t)rows * (cols + 1);
+        for (int r = 0; r < 4; ++r) st->checksum[r] = cs[r];
+        return rc;
+    }
+    return MC_OK;
+}
+
+int mc_batch_stats(mc_batch_h b, mc_stats* st) {
+    if (!b || !st) return fail(MC_ERR_ARG, "null argument");
+    return batchCounters(b, st);
+}
+
+size_t mc_batch_state_bytes(mc_batch_h b) { return b ? b->stateBytes : 0; }
+
+void mc_batch_destroy(mc_batch_h b) { freeBatch(b); }
+
 }  // extern "C"
+

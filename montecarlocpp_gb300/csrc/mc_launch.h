@@ -19,6 +19,16 @@ cudaError_t launchAdvance(const Params<R>& p, bool dyn, bool replay, bool log, i
 template <typename R>
 cudaError_t launchCompact(const Params<R>& p, int grid, cudaStream_t s);
 
+// batched launches (all instances in one kernel)
+template <typename R>
+cudaError_t launchEmitBatch(const Params<R>& p, cudaStream_t s);
+template <typename R>
+cudaError_t launchAdvanceBatch(const Params<R>& p, int grid, int block, cudaStream_t s);
+template <typename R>
+cudaError_t launchDifPrefix(const Params<R>& p, cudaStream_t s);
+template <typename R>
+int advanceBatchOccupancy(int ninst, int block);
+
 // Maximum resident blocks per SM of the advance kernel for this
 // configuration (0 if it cannot launch).
 template <typename R>

@@ -46,6 +46,39 @@ cudaError_t launchCompact<MC_REAL>(const Params<MC_REAL>& p, int grid, cudaStrea
     return cudaGetLastError();
 }
 
+template <>
+cudaError_t launchEmitBatch<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
+    if (p.cap == 0) return cudaSuccess;
+    const long long grid = ((long long)p.cap + 255) / 256;
+    k_emit_batch<MC_REAL><<<(unsigned)grid, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int grid, int block, cudaStream_t s) {
+    const size_t smem = batchSmemBytes<MC_REAL>(p.ninst);
+    cudaError_t e = prepare(k_advance_batch<MC_REAL>, smem);
+    if (e != cudaSuccess) return e;
+    k_advance_batch<MC_REAL><<<grid, block, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launchDifPrefix<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
+    k_difprefix<MC_REAL><<<dim3((unsigned)p.ninst, 4), 32, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <>
+int advanceBatchOccupancy<MC_REAL>(int ninst, int block) {
+    const size_t smem = batchSmemBytes<MC_REAL>(ninst);
+    if (prepare(k_advance_batch<MC_REAL>, smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_advance_batch<MC_REAL>, block, smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
 #define MC_DISPATCH(F, ...)                                                                 \
     if (dyn) {                                                                             \
         if (tm == TM_SHARED) {                                                             \

@@ -1,0 +1,645 @@
+// mc_walker.cuh -- the phonon event loop shared by the single-instance and
+// batched kernels: shared-memory layout, field tallies, the cell walk of a
+// flight, emission, and Walker (one phonon in flight).
+#pragma once
+
+#include "mc_device.cuh"
+
+namespace mcg {
+
+// ---------------------------------------------------------------- tables
+// Shared layout of a single-instance launch: vel and vel*tau tables, the
+// scatter bin thresholds and guide table, the subdomains (when staged), the
+// instance descriptor, then the block's tally.
+struct SmemLayout {
+    size_t vel = 0, vt = 0, wthr = 0, guide = 0, sd = 0, inst = 0, tal = 0, total = 0;
+    template <typename R>
+    __host__ __device__ void init(int nw, int np, int nsdShared, int rows, int cols, bool sharedTally) {
+        auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+        const size_t nt = (size_t)nw * np;
+        vel = 0;
+        vt = vel + sizeof(R) * nt;
+        wthr = al(vt + sizeof(R) * nt);
+        guide = al(wthr + sizeof(unsigned long long) * (size_t)nw);
+        sd = al(guide + sizeof(uint16_t) * GUIDE);
+        inst = al(sd + sizeof(SdomD<R>) * (size_t)nsdShared);
+        tal = al(inst + sizeof(InstD<R>));
+        total = tal + (sharedTally ? sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1) : 0);
+    }
+};
+
+// Subdomain images staged in shared memory up to this many bytes.
+constexpr size_t SD_SHARED_MAX = 32 * 1024;
+
+__host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
+    return sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1);
+}
+
+// Tally modes: per-block shared histogram (64-bit fixed point, exact and
+// order-independent adds) flushed with FP64 atomics, or FP64 atomics
+// straight to the global field (fields too large for shared memory, and
+// batched launches).
+enum { TM_SHARED = 0, TM_GLOBAL = 1 };
+
+// Hard cap on events one thread processes in one launch (a guard: a
+// phonon that reaches it is killed and flagged non-finite).
+constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
+
+// Resident blocks of 256 threads per SM the FP32 advance kernels are
+// compiled for (register budget 65536 / (256 x this)).
+#ifndef MC_MIN_BLOCKS_F32
+#define MC_MIN_BLOCKS_F32 4
+#endif
+
+template <typename R>
+struct Phn {
+    int s;          // subdomain
+    int idx[3];     // cell
+    R off[3];       // offset inside the cell, in [0, 1]
+    R d[3];         // direction (unit, physical)
+    R scatNext;
+    int w, p;
+    bool neg;       // sign -1
+    uint32_t nscat, nloop, id;
+};
+
+// Round a float to the nearest int64 with integer instructions only (the
+// float -> int64 conversion runs on GB300's narrow FP64 pipe). |v| < 2^61.
+__device__ __forceinline__ long long toFixed(float v) {
+    const uint32_t b = __float_as_uint(v);
+    const int e = (int)((b >> 23) & 0xFFu) - 150;  // v = m * 2^e
+    const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
+    long long r;
+    if (e >= 0) r = m << e;
+    else if (e > -25) r = (m + (1LL << (-e - 1))) >> (-e);
+    else r = 0;
+    return (b >> 31) ? -r : r;
+}
+__device__ __forceinline__ long long toFixed(double v) { return __double2ll_rn(v); }
+
+// float -> double by moving the bits (the conversion instruction runs on
+// GB300's narrow FP64 pipe); zero and subnormal inputs give zero.
+__device__ __forceinline__ double toDouble(float v) {
+    const uint32_t b = __float_as_uint(v);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if (e == 0u) return 0.0;
+    const uint32_t m = b & 0x7FFFFFu;
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
+}
+__device__ __forceinline__ double toDouble(double v) { return v; }
+
+// Field accumulation for one flight of one instance.
+template <typename R, int TM>
+struct Tally {
+    const InstD<R>* I;
+    // amount per metre of flight, rows entries: Temp sign/v; Flux sign*d
+    R rho[4];
+
+    __device__ __forceinline__ int rows() const { return I->rows; }
+    // fixed-point amount of row r for path length t
+    __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * I->tqinv[r])); }
+    __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&I->tal[r * I->cols + col]), (unsigned long long)v);
+    }
+    __device__ __forceinline__ void atomRange(int r, int c0, int c1, long long v) const {
+        unsigned long long* d = reinterpret_cast<unsigned long long*>(I->dif + r * (I->cols + 1));
+        atomicAdd(d + c0, (unsigned long long)v);
+        atomicAdd(d + c1, (unsigned long long)(-v));
+    }
+    __device__ __forceinline__ void addGlobal(int col, R t) const {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (r < I->rows) atomicAdd(&I->tally[(size_t)col * I->rows + r], toDouble(rho[r] * t));
+    }
+    // interior cells [c0, c1) of a 1-D walk (stride 1) each with path t
+    __device__ __forceinline__ void addGlobalRange(int c0, int c1, R t) const {
+        if (I->gdif) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                if (r < I->rows) {
+                    const double v = toDouble(rho[r] * t);
+                    atomicAdd(&I->gdif[(size_t)r * (I->cols + 1) + c0], v);
+                    atomicAdd(&I->gdif[(size_t)r * (I->cols + 1) + c1], -v);
+                }
+            }
+        } else {
+            for (int c = c0; c < c1; ++c) addGlobal(c, t);
+        }
+    }
+};
+
+// Reduced velocity a = S (M^-1 d) and its reciprocal.
+template <typename R>
+__device__ __forceinline__ void reducedVel(const SdomD<R>& S, const R d[3], R a[3], R ia[3]) {
+    R m[3];
+    rotate(S.Minv, d, m);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = S.S[k] * m[k];
+        ia[k] = R(1) / a[k];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ R clamp01(R x) { return fmin(fmax(x, R(0)), R(1)); }
+
+// Move along axis k by du cells (no tally): displacement relative to the
+// current cell, then re-split into cell index and offset.
+template <typename R>
+__device__ __forceinline__ void moveAxis(Phn<R>& ph, const SdomD<R>& S, int k, R du) {
+    const int sh = (int)floor(du);
+    const int i = min(max(ph.idx[k] + sh, 0), S.shape[k] - 1);
+    ph.off[k] = clamp01(du - (R)(i - ph.idx[k]));
+    ph.idx[k] = i;
+}
+
+// 1-D flight along axis K (the only axis with cells): closed form of
+// montecarlo/field.cpp:187-223 -- partial first and last cells, full
+// interior cells through the difference array. In the shared layout the
+// flight's whole fixed-point amount V is computed once and the last cell
+// takes the integer remainder, so the cells add up to V exactly.
+template <typename R, int TM, int K>
+__device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
+                                      Tally<R, TM>& T, long long csum[4]) {
+    const int cb = S.colbeg;
+    const int b = ph.idx[K];
+    const int n = S.shape[K];
+    // displacement in cell units relative to the current cell
+    const R du = ph.off[K] + s * a[K];
+    int e = b + (int)floor(du);
+    e = min(max(e, 0), n - 1);
+    const int stride = S.tstride[K];
+    const R inva = fabs(ia[K]);
+    const int lo = min(b, e), hi = max(b, e);
+    const R tfirst = (e > b ? (R(1) - ph.off[K]) : ph.off[K]) * inva;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        if (r >= T.rows()) break;
+        const long long V = T.fixedOf(r, s);
+        csum[r] += V;
+        if (TM == TM_SHARED) {
+            if (e == b) {
+                T.atomShared(r, cb + b * stride, V);
+            } else {
+                const long long F = T.fixedOf(r, tfirst);
+                const long long I = T.fixedOf(r, inva);
+                T.atomShared(r, cb + b * stride, F);
+                T.atomShared(r, cb + e * stride, V - F - (long long)(hi - lo - 1) * I);
+                if (stride == 1) { if (hi - lo > 1) T.atomRange(r, cb + lo + 1, cb + hi, I); }
+                else for (int c = lo + 1; c < hi; ++c) T.atomShared(r, cb + c * stride, I);
+            }
+        }
+    }
+    if (TM == TM_GLOBAL) {
+        if (e == b) {
+            T.addGlobal(cb + b * stride, s);
+        } else {
+            const R tlast = s - tfirst - (R)(hi - lo - 1) * inva;
+            T.addGlobal(cb + b * stride, tfirst);
+            T.addGlobal(cb + e * stride, fmax(tlast, R(0)));
+            if (stride == 1) { if (hi - lo > 1) T.addGlobalRange(cb + lo + 1, cb + hi, inva); }
+            else for (int c = lo + 1; c < hi; ++c) T.addGlobal(cb + c * stride, inva);
+        }
+    }
+    ph.idx[K] = e;
+    ph.off[K] = clamp01(du - (R)(e - b));
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        if (j != K) moveAxis(ph, S, j, ph.off[j] + s * a[j]);
+}
+
+// Flight of path length s from the current cell, tallied cell by cell
+// (Field::accumulate, montecarlo/field.cpp:160-288, as a cell walk); adds
+// the flight's fixed-point amount to the checksums.
+template <typename R, int TM>
+__device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
+                                   Tally<R, TM>& T, long long csum[4]) {
+    const int acc = S.accum;
+    const int cb = S.colbeg;
+    if (acc < 0) {
+        // a single field column (or none): move only
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (r >= T.rows()) break;
+            const long long V = T.fixedOf(r, s);
+            csum[r] += V;
+            if (acc == -1 && TM == TM_SHARED) T.atomShared(r, cb, V);
+        }
+        if (acc == -1 && TM == TM_GLOBAL) T.addGlobal(cb, s);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
+        return;
+    }
+    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, ia, s, T, csum); return; }
+    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, ia, s, T, csum); return; }
+    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, ia, s, T, csum); return; }
+    // 2-D / 3-D: walk the cells (Amanatides-Woo)
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        if (r < T.rows()) csum[r] += T.fixedOf(r, s);
+    R rem = s;
+    const int s0 = S.tstride[1], s01 = S.tstride[2];
+    for (int guard = 0; guard < 3 * MAX_SHAPE + 4; ++guard) {
+        R tmin = rem;
+        int ax = -1;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            R t = tmin;
+            if (a[k] > R(0) && ph.idx[k] < S.shape[k] - 1) t = (R(1) - ph.off[k]) * ia[k];
+            else if (a[k] < R(0) && ph.idx[k] > 0) t = -ph.off[k] * ia[k];
+            if (t < tmin) { tmin = t; ax = k; }
+        }
+        tmin = fmax(tmin, R(0));
+        const int col = cb + ph.idx[0] * S.tstride[0] + ph.idx[1] * s0 + ph.idx[2] * s01;
+        if (TM == TM_SHARED) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (r < T.rows()) T.atomShared(r, col, T.fixedOf(r, tmin));
+        } else {
+            T.addGlobal(col, tmin);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            ph.off[k] = clamp01(ph.off[k] + tmin * a[k]);
+            if (k == ax) {
+                if (a[k] > R(0)) { ph.idx[k] += 1; ph.off[k] = R(0); }
+                else { ph.idx[k] -= 1; ph.off[k] = R(1); }
+            }
+        }
+        rem -= tmin;
+        if (ax < 0) break;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void physPos(const SdomD<R>& S, const Phn<R>& ph, double x[3]) {
+    double u[3];
+    for (int k = 0; k < 3; ++k) u[k] = ((double)ph.idx[k] + (double)ph.off[k]) / (double)S.S[k];
+    for (int r = 0; r < 3; ++r)
+        x[r] = (double)S.o[r] + (((double)S.M[3 * r] * u[0] + (double)S.M[3 * r + 1] * u[1]) +
+                                 (double)S.M[3 * r + 2] * u[2]);
+}
+
+template <typename R>
+__device__ __forceinline__ void logEvent(const Params<R>& P, const Phn<R>& ph, int sBefore, int face,
+                                         int sAfter, double xEnd[3], double time, int cellEnd) {
+    if (P.log == nullptr || (long long)ph.id >= P.logn) return;
+    long long i = ph.nloop;
+    if (i >= P.logcap) return;
+    double* r = P.log + ((long long)ph.id * P.logcap + i) * 12;
+    r[0] = (double)ph.nloop; r[1] = sBefore; r[2] = face; r[3] = sAfter; r[4] = cellEnd;
+    r[5] = xEnd[0]; r[6] = xEnd[1]; r[7] = xEnd[2]; r[8] = time; r[9] = (double)ph.nscat;
+    r[10] = ph.w; r[11] = ph.p;
+    atomicMax(&P.logcount[ph.id], (int)(i + 1));
+}
+
+// drawScatNext (montecarlo/material.cpp:287-296): d = v tau (-log(1 - u)),
+// redrawn while below the smallest normal number.
+template <typename R, typename G>
+__device__ __forceinline__ R drawScatNext(G& g, R vt) {
+    R dist = R(0);
+    for (int guard = 0; guard < 64 && dist < Lim<R>::tiny(); ++guard) dist = vt * neglog1m(g.next(), R(0));
+    return dist;
+}
+
+// FieldProblem::solve emission part (montecarlo/problem.cpp:386-399) and
+// Emitter::emit (montecarlo/boundary.cpp:378-385) for phonon `n` of
+// instance I (event 0 of its random stream).
+template <typename R, typename G>
+__device__ __forceinline__ void emitOne(const InstD<R>& I, long long n, G& g, Phn<R>& ph) {
+    // emitter = upper_bound(emitCdf, n)
+    int lo = 0, hi = I.nem;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (I.emitCdf[mid] <= n) lo = mid + 1; else hi = mid;
+    }
+    const EmitterD E = I.em[lo];
+    const SdomD<R>& S = I.sd[E.sdom];
+    g.setEvent(0);
+    ph.s = E.sdom;
+    ph.id = (uint32_t)n;
+    ph.nscat = 0; ph.nloop = 0;
+    {   // drawFluxProp (montecarlo/material.cpp:277-280)
+        uint32_t x1 = g.next(), x2 = g.next();
+        ph.w = searchThr(I.fwthr, I.nw, x1);
+        ph.p = searchBranch(I.fpthr + (size_t)ph.w * I.np, I.np, x2);
+    }
+    R u[3];
+    R dir[3];
+    if (E.face >= 0) {
+        // EmitBoundary: position on the face (montecarlo/boundary.cpp:147-152,
+        // 418-421), cosine direction about the inward normal (423-426)
+        const FaceD<R>& F = S.f[E.face];
+        R r1 = u01<R>(g.next()), r2 = u01<R>(g.next());
+        // (i, j) shape axes of each face (montecarlo/subdomain.h:149-154)
+        switch (E.face) {
+        case 0: u[0] = R(0); u[1] = r1 * S.S[1]; u[2] = r2 * S.S[2]; break;
+        case 1: u[1] = R(0); u[2] = r1 * S.S[2]; u[0] = r2 * S.S[0]; break;
+        case 2: u[2] = R(0); u[0] = r1 * S.S[0]; u[1] = r2 * S.S[1]; break;
+        case 3: u[0] = S.S[0]; u[2] = r1 * S.S[2]; u[1] = r2 * S.S[1]; break;
+        case 4: u[1] = S.S[1]; u[0] = r1 * S.S[0]; u[2] = r2 * S.S[2]; break;
+        default: u[2] = S.S[2]; u[1] = r1 * S.S[1]; u[0] = r2 * S.S[0]; break;
+        }
+        R v[3];
+        drawAniso<R>(g, false, v);
+        rotate(F.rot, v, dir);
+        ph.neg = !(F.T >= R(0));
+    } else {
+        // EmitSubdomain (montecarlo/subdomain.cpp:250-263,275-281)
+        R c0 = u01<R>(g.next()), c1 = u01<R>(g.next()), c2 = u01<R>(g.next());
+        u[0] = c0 * S.S[0]; u[1] = c1 * S.S[1]; u[2] = c2 * S.S[2];
+        R v[3];
+        drawAniso<R>(g, true, v);
+        rotate(S.grot, v, dir);
+        ph.neg = !(((dir[0] * S.gradT[0] + dir[1] * S.gradT[1]) + dir[2] * S.gradT[2]) < R(0));
+    }
+    normalize(dir);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int i = (int)floor(u[k]);
+        i = min(max(i, 0), S.shape[k] - 1);
+        ph.idx[k] = i;
+        ph.off[k] = u[k] - (R)i;
+        ph.d[k] = dir[k];
+    }
+    ph.scatNext = drawScatNext<R>(g, I.vt[ph.w * I.np + ph.p]);
+}
+
+template <typename R>
+__device__ __forceinline__ void packPhonon(const Phn<R>& ph, typename Vec4<R>::T& A0, typename Vec4<R>::T& A1,
+                                           uint4& A2) {
+    A0.x = ph.off[0]; A0.y = ph.off[1]; A0.z = ph.off[2]; A0.w = ph.scatNext;
+    A1.x = ph.d[0]; A1.y = ph.d[1]; A1.z = ph.d[2]; A1.w = idToReal<R>(ph.id);
+    A2.x = packCell(ph.s, ph.idx);
+    A2.y = packProp(ph.w, ph.p, ph.neg);
+    A2.z = ph.nscat;
+    A2.w = ph.nloop;
+}
+
+// ----------------------------------------------------------------- advance
+// Per-launch constants of the advance kernels.
+template <typename R>
+struct Window {
+    int keff;        // dt-steps in this launch
+    R len;           // keff * dt
+    R invdt;
+    bool last;       // the horizon ends with this launch
+    R next;          // length of the following window (0 if none)
+    __device__ __forceinline__ void init(const Params<R>& P) {
+        keff = min(P.ksteps, P.nsteps - P.step0);
+        len = (R)keff * P.dt;
+        invdt = R(1) / P.dt;
+        last = (P.step0 + keff >= P.nsteps);
+        next = (R)min(P.ksteps, max(P.nsteps - P.step0 - keff, 0)) * P.dt;
+    }
+};
+
+// Per-thread counters, reduced once per launch.
+struct Counts {
+    uint32_t steps = 0, events = 0, scat = 0, esc = 0, hor = 0, maxs = 0, maxl = 0, abs = 0, bad = 0;
+};
+
+// Dead marker in the prop word of a slot written back in place.
+constexpr uint32_t PROP_DEAD = 1u << 25;
+
+// One phonon in flight: its state and the launch-local quantities derived
+// from it. iterate() runs one loop iteration of montecarlo/problem.cpp:401-435
+// (flight to the next event or to the end of the window, its tally, the
+// event); finish() closes the phonon's window.
+template <typename R, bool REPLAY, bool LOG, int TM>
+struct Walker {
+    Phn<R> ph;
+    const InstD<R>* I;
+    const SdomD<R>* S;
+    R a[3], ia[3];
+    R v, iv, sg;
+    R budget;
+    R tnext;       // time to the next event after the window end
+    int nev;
+    int stop;      // 0 alive, else the counter of the stop reason
+    Rng<REPLAY> g;
+
+    __device__ __forceinline__ void load(const Params<R>& P, const InstD<R>* inst, const Window<R>& W,
+                                         const typename Vec4<R>::T& A0, const typename Vec4<R>::T& A1,
+                                         const uint4& A2) {
+        I = inst;
+        unpackCell(A2.x, ph.s, ph.idx);
+        ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
+        ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
+        ph.id = realToId<R>(A1.w);
+        ph.w = (int)(A2.y & 0xFFFFu);
+        ph.p = (int)((A2.y >> 16) & 0xFFu);
+        ph.neg = (A2.y >> 24) & 1u;
+        ph.nscat = A2.z;
+        ph.nloop = A2.w;
+        g.init(I->key0, I->key1, ph.id, &P);
+        budget = W.len;
+        S = &I->sd[ph.s];
+        reducedVel(*S, ph.d, a, ia);
+        v = I->vel[ph.w * I->np + ph.p];
+        iv = R(1) / v;
+        sg = ph.neg ? R(-1) : R(1);
+        stop = 0;
+        nev = 0;
+        tnext = R(0);
+    }
+
+    __device__ __forceinline__ void pack(typename Vec4<R>::T& A0, typename Vec4<R>::T& A1, uint4& A2) const {
+        packPhonon(ph, A0, A1, A2);
+    }
+
+    // returns true when the phonon's window is over (alive or stopped)
+    __device__ __forceinline__ bool iterate(const Params<R>& P, const Window<R>& W, Counts& C, long long csum[4]) {
+        // Subdomain::advect (montecarlo/subdomain.cpp:161-192): the
+        // approaching face of each axis, in the reference's face order
+        // (lower faces 0..2, then upper faces 3..5), against the free path;
+        // strict < keeps the first of equals
+        R sev = ph.scatNext;
+        int face = -1;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const R dist = (-(R)ph.idx[k] - ph.off[k]) * ia[k];
+            if (a[k] < R(0) && dist < sev) { sev = dist; face = k; }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const R dist = (((R)(S->shape[k] - ph.idx[k])) - ph.off[k]) * ia[k];
+            if (a[k] > R(0) && dist < sev) { sev = dist; face = k + 3; }
+        }
+        const R tev = sev * iv;
+        const bool event = tev <= budget;
+        const R s = event ? sev : budget * v;
+        // tally amounts per metre (montecarlo/problem.cpp:473-544)
+        Tally<R, TM> T;
+        T.I = I;
+        if (I->problem == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
+        else if (I->problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
+        else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
+        const int sBefore = ph.s;
+        int cellEnd = 0;
+        fly<R, TM>(ph, *S, a, ia, s, T, csum);
+        if (LOG) cellEnd = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
+        ph.scatNext -= s;
+        if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
+        if (!event) {
+            tnext = (sev - s) * iv;
+            budget = R(0);
+            if (!(ph.scatNext == ph.scatNext)) stop = C_BAD;
+            return true;
+        }
+        budget -= tev;
+        if (sev < -S->eps) {
+            stop = C_ESCAPES;
+            if (LOG) {
+                double x[3]; physPos(*S, ph, x);
+                logEvent(P, ph, sBefore, -3, sBefore, x, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
+                         cellEnd);
+            }
+            return true;
+        }
+        double xe[3];
+        if (LOG) physPos(*S, ph, xe);
+        g.setEvent(ph.nloop + 1);
+        if (face >= 0) {
+            const FaceD<R>& F = S->f[face];
+            // the flight ends on the face: snap that coordinate
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (face == k) { ph.idx[k] = 0; ph.off[k] = R(0); }
+                if (face == k + 3) { ph.idx[k] = S->shape[k] - 1; ph.off[k] = R(1); }
+            }
+            switch (F.kind) {
+            case F_SPEC: {  // montecarlo/boundary.cpp:283-287
+                R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
+                for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F.n[j];
+                normalize(ph.d);
+                break;
+            }
+            case F_DIFF: {  // montecarlo/boundary.cpp:308-312
+                R vv[3];
+                drawAniso<R>(g, false, vv);
+                rotate(F.rot, vv, ph.d);
+                normalize(ph.d);
+                ph.nscat++;
+                break;
+            }
+            case F_ISOT:  // montecarlo/boundary.cpp:455-460
+                stop = C_ABSORBED;
+                break;
+            case F_PERI:     // montecarlo/boundary.cpp:516-522
+            case F_INTER: {  // montecarlo/boundary.cpp:349-359 (single pair)
+                if (F.to < 0) { stop = C_ESCAPES; break; }
+                if (F.tang) {
+                    // same axis, tangential cells unchanged: keep the split
+                    // coordinates, move onto the paired face
+                    ph.s = F.to;
+                    S = &I->sd[ph.s];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        if (F.toface == j) { ph.idx[j] = 0; ph.off[j] = R(0); }
+                        if (F.toface == j + 3) { ph.idx[j] = S->shape[j] - 1; ph.off[j] = R(1); }
+                    }
+                } else {
+                    R u[3], u2[3];
+                    for (int j = 0; j < 3; ++j) u[j] = (R)ph.idx[j] + ph.off[j];
+                    rotate(F.A, u, u2);
+                    for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
+                    ph.s = F.to;
+                    S = &I->sd[ph.s];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        if (F.toface == j) u2[j] = R(0);
+                        if (F.toface == j + 3) u2[j] = S->S[j];
+                    }
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        int ii = (int)floor(u2[j]);
+                        ii = min(max(ii, 0), S->shape[j] - 1);
+                        ph.idx[j] = ii;
+                        ph.off[j] = clamp01(u2[j] - (R)ii);
+                    }
+                }
+                if (F.kind == F_PERI && !F.ident) {
+                    R dd[3] = {ph.d[0], ph.d[1], ph.d[2]};
+                    rotate(F.Rd, dd, ph.d);
+                    normalize(ph.d);
+                }
+                break;
+            }
+            }
+        } else {
+            // Material::scatter (montecarlo/material.cpp:298-303)
+            uint32_t x1 = g.next(), x2 = g.next();
+            ph.w = searchGuided(I->wthr, I->wguide, I->nw, x1);
+            ph.p = searchBranch(I->pthr + ph.w * I->np, I->np, x2);
+            drawIso<R>(g, ph.d);
+            normalize(ph.d);
+            ph.nscat++;
+            ph.scatNext = drawScatNext<R>(g, I->vt[ph.w * I->np + ph.p]);
+            v = I->vel[ph.w * I->np + ph.p];
+            iv = R(1) / v;
+            ++C.scat;
+        }
+        ++C.events;
+        if (LOG) logEvent(P, ph, sBefore, face, ph.s, xe, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
+                          cellEnd);
+        ph.nloop++;
+        if (REPLAY && g.exhausted()) { stop = C_REPLAY_EXHAUSTED; return true; }
+        if (stop) return true;
+        if ((long long)ph.nscat >= I->maxscat) { stop = C_MAXSCAT; return true; }
+        if ((long long)ph.nloop >= I->maxloop) { stop = C_MAXLOOP; return true; }
+        if (++nev >= MAX_EVENTS_PER_LAUNCH) { stop = C_BAD; return true; }
+        reducedVel(*S, ph.d, a, ia);
+        return false;
+    }
+
+    // the phonon's window is over: count its steps and its stop reason;
+    // returns true if it stays alive
+    __device__ __forceinline__ bool finish(const Params<R>& P, const Window<R>& W, Counts& C) {
+        if (REPLAY) g.save();
+        if (stop == 0) {
+            C.steps += W.keff;
+            if (W.last) {
+                stop = C_HORIZON;
+                if (LOG) {
+                    double x[3]; physPos(*S, ph, x);
+                    int ce = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
+                    logEvent(P, ph, ph.s, -2, ph.s, x, (double)P.nsteps * (double)P.dt, ce);
+                }
+            }
+        } else {
+            R el = W.len - budget;
+            int st = (int)ceil(el * W.invdt);
+            st = st < 1 ? 1 : (st > W.keff ? W.keff : st);
+            C.steps += st;
+        }
+        switch (stop) {
+        case 0: break;
+        case C_ESCAPES: ++C.esc; break;
+        case C_HORIZON: ++C.hor; break;
+        case C_MAXSCAT: ++C.maxs; break;
+        case C_MAXLOOP: ++C.maxl; break;
+        case C_ABSORBED: ++C.abs; break;
+        case C_REPLAY_EXHAUSTED: atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED); break;
+        default: ++C.bad; atomicOr(P.status, (unsigned)S_NONFINITE); break;
+        }
+        return stop == 0;
+    }
+};
+
+// Reduce the counters (one atomic per warp).
+__device__ __forceinline__ void flushCounts(unsigned long long* counters, const Counts& C) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t cs[9] = {C.steps, C.events, C.scat, C.esc, C.hor, C.maxs, C.maxl, C.abs, C.bad};
+    const int ids[9] = {C_PHONON_STEPS, C_EVENTS, C_SCATTERS, C_ESCAPES, C_HORIZON, C_MAXSCAT,
+                        C_MAXLOOP, C_ABSORBED, C_BAD};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        unsigned long long x = cs[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if (lane == 0 && x) atomicAdd(&counters[ids[q]], x);
+    }
+}
+
+}  // namespace mcg

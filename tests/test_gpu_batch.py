@@ -1,0 +1,71 @@
+"""Batched solves (one persistent kernel over many instances) against the
+same problems solved one at a time through the C ABI."""
+
+import numpy as np
+import pytest
+
+import montecarlocpp_gb300 as M
+
+pytestmark = pytest.mark.gpu
+
+
+def field_err(a, b):
+    scale = np.abs(a).max(axis=1, keepdims=True)
+    scale[scale == 0] = 1
+    return float((np.abs(a - b) / scale).max())
+
+
+def instances():
+    mats = {T: M.Material.silicon(T) for T in (150.0, 300.0, 380.0)}
+    return [
+        M.MultiProblem(mats[150.0], M.FilmDomain.from_cli(1e-7, 5e-8, 40), 3000, 10**6),
+        M.MultiProblem(mats[300.0], M.FilmDomain.from_cli(1e-7, 2e-7, 100), 7000, 10**6),
+        M.TempProblem(mats[380.0], M.CrossPlaneFilmDomain(1e-7, 1e-7, 20), 2000, 10**6),
+        M.MultiProblem(mats[300.0], M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4)), 1500, 10**6),
+        M.FluxProblem(mats[150.0], M.BulkDomain.from_cli(1e-6, 10), 500, 1000),
+    ]
+
+
+@pytest.mark.parametrize("K", [0, 40])
+def test_batch_equals_single_fp64(K):
+    probs = instances()
+    seeds = [11, 12, 13, 14, 15]
+    dt, nsteps = 0.5e-12, 400
+    B = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=64, steps_per_launch=K, use_graph=False)
+    B.run()
+    total_events = 0
+    for i, (p, s) in enumerate(zip(probs, seeds)):
+        got, st = B.result(i)
+        ref = p.solve(dt=dt, nsteps=nsteps, precision=64, seed=s, steps_per_launch=K or nsteps)
+        assert st["nemit"] == p.stats["nemit"]
+        assert field_err(ref, got) < 1e-9, i
+        assert np.allclose(st["checksum"], p.stats["checksum"], rtol=1e-9, atol=0)
+        total_events += p.stats["events"]
+    assert B.stats()["events"] == total_events
+
+
+def test_batch_graph_replay_fp32():
+    probs = instances()
+    dt, nsteps = 0.5e-12, 300
+    B = M.Batch(probs, dt=dt, nsteps=nsteps, precision=32, use_graph=True)
+    B.run()
+    first = [B.result(i)[0] for i in range(len(probs))]
+    e1 = B.stats()["events"]
+    B.run()
+    assert B.stats()["events"] == e1
+    for i, p in enumerate(probs):
+        again = B.result(i)[0]
+        assert field_err(first[i], again) < 1e-12
+        ref = p.solve(dt=dt, nsteps=nsteps, precision=32, seed=i)
+        # FP32 flight: same trajectories; the field sums in another order
+        assert field_err(ref, again) < 1e-5
+
+
+def test_batched_films_workload_shape():
+    from montecarlocpp_gb300.workloads import batched_films
+    specs = batched_films(0)
+    assert len(specs) == 64
+    n = np.array([s.nemit for s in specs])
+    th = np.array([s.thickness for s in specs])
+    assert n.min() >= 10_000 and n.max() <= 1_000_000
+    assert (np.diff(n[np.argsort(th)]) >= 0).all()
