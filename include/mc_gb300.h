@@ -207,6 +207,67 @@ int mc_batch_stats(mc_batch_h b, mc_stats* st);
 size_t mc_batch_state_bytes(mc_batch_h b);
 void mc_batch_destroy(mc_batch_h b);
 
+/* ------------------------------------------------------------ serving */
+/* A request loop on a library thread. Submitted solves are admitted against
+ * an HBM budget (phonon state in flight at once); every tick advances one
+ * round of every admitted solve -- its own Material, Domain, phonon count
+ * and Philox key -- in one persistent batched launch, so requests that
+ * arrive while others run join the next tick. A round splits its phonons
+ * into `groups` batch means; a solve completes when the standard error of
+ * kappa = -<q_axis> / gradT_axis is at most target_rel_se of its mean. */
+typedef struct mc_server_s* mc_server_h;
+
+typedef struct {
+    double dt;              /* time step, s                                 */
+    long nsteps;            /* horizon of each round = nsteps * dt          */
+    int precision;          /* 32 or 64                                     */
+    size_t hbm_budget;      /* bytes of phonon state admitted at once       */
+    int max_active;         /* solves per tick (<= 512)                     */
+    int groups;             /* batch means per round, 2..8                  */
+    double target_rel_se;   /* e.g. 0.01                                    */
+    int min_rounds;         /* rounds before the stopping rule applies     */
+    int max_rounds;         /* give up (status MC_ERR_BUSY) after this many */
+    int block_size;         /* 0 -> 256                                     */
+} mc_server_desc;
+
+typedef struct {
+    mc_material_h mat;      /* kept alive by the caller until completion    */
+    mc_domain_h dom;
+    int problem;            /* MC_FLUX or MC_MULTI                          */
+    long nemit;             /* phonons per round                            */
+    long maxscat, maxloop;
+    uint64_t seed;          /* round r uses seed + r                        */
+    int axis;               /* flux / gradient axis                         */
+    double volume;          /* averaging volume (0: sum of cell volumes)    */
+    double gradient;        /* gradT along the axis (0: the first subdomain's) */
+} mc_request;
+
+typedef struct {
+    double kappa, kappa_se; /* W / m / K                                    */
+    long rounds, phonons;
+    double phonon_steps;
+    double t_submit, t_admit, t_done;  /* seconds on the server clock       */
+    int status;             /* MC_OK, or MC_ERR_BUSY if max_rounds ran out  */
+} mc_result;
+
+typedef struct {
+    long submitted, admitted, completed, queued, active, ticks;
+    double busy_s, uptime_s, phonon_steps;
+} mc_server_counters;
+
+int mc_server_create(const mc_server_desc* d, mc_server_h* out);
+/* Thread-safe; returns at once with a ticket. */
+int mc_server_submit(mc_server_h s, const mc_request* r, long* ticket);
+/* 1 if done (result and, if field != NULL, the mean field rows x cols are
+ * written), 0 if pending, < 0 on error. */
+int mc_server_poll(mc_server_h s, long ticket, mc_result* res, double* field);
+/* Block up to timeout_s; same return values as mc_server_poll. */
+int mc_server_wait(mc_server_h s, long ticket, double timeout_s, mc_result* res, double* field);
+int mc_server_stats(mc_server_h s, mc_server_counters* st);
+/* Seconds on the server clock (the t_* fields of mc_result). */
+double mc_server_clock(mc_server_h s);
+void mc_server_destroy(mc_server_h s);
+
 #ifdef __cplusplus
 }
 #endif

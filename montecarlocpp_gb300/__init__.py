@@ -7,6 +7,7 @@ ABI in include/mc_gb300.h). This package mirrors the reference's host API
 """
 
 from .batch import Batch
+from .serve import Server
 from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PERI, RIG, SPEC, TOP, BulkDomain,
                       CrossPlaneFilmDomain, Domain, FilmDomain, Pair, Parallelepiped, PoreCellDomain)
 from .materials import SiliconModel, silicon_tables, write_material_files
@@ -18,5 +19,5 @@ __all__ = [
     "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "Pair",
     "Parallelepiped", "SiliconModel", "silicon_tables", "write_material_files", "Material",
     "TempProblem", "FluxProblem", "MultiProblem", "Session", "TEMP", "FLUX", "MULTI",
-    "kappa_from_flux", "Batch",
+    "kappa_from_flux", "Batch", "Server",
 ]

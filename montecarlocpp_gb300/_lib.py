@@ -60,6 +60,36 @@ class BatchDesc(C.Structure):
                 ("use_graph", C.c_int), ("stream", C.c_void_p)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("dt", C.c_double), ("nsteps", C.c_long), ("precision", C.c_int), ("hbm_budget", C.c_size_t),
+                ("max_active", C.c_int), ("groups", C.c_int), ("target_rel_se", C.c_double),
+                ("min_rounds", C.c_int), ("max_rounds", C.c_int), ("block_size", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("mat", C.c_void_p), ("dom", C.c_void_p), ("problem", C.c_int), ("nemit", C.c_long),
+                ("maxscat", C.c_long), ("maxloop", C.c_long), ("seed", C.c_uint64), ("axis", C.c_int),
+                ("volume", C.c_double), ("gradient", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("kappa", C.c_double), ("kappa_se", C.c_double), ("rounds", C.c_long), ("phonons", C.c_long),
+                ("phonon_steps", C.c_double), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [("submitted", C.c_long), ("admitted", C.c_long), ("completed", C.c_long), ("queued", C.c_long),
+                ("active", C.c_long), ("ticks", C.c_long), ("busy_s", C.c_double), ("uptime_s", C.c_double),
+                ("phonon_steps", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # every symbol declared in include/mc_gb300.h
 SYMBOLS = [
     "mc_last_error", "mc_version",
@@ -71,6 +101,8 @@ SYMBOLS = [
     "mc_session_state_bytes", "mc_session_destroy",
     "mc_batch_create", "mc_batch_run", "mc_batch_result", "mc_batch_stats", "mc_batch_state_bytes",
     "mc_batch_destroy",
+    "mc_server_create", "mc_server_submit", "mc_server_poll", "mc_server_wait", "mc_server_stats",
+    "mc_server_clock", "mc_server_destroy",
 ]
 
 _lib = None
@@ -122,6 +154,14 @@ def lib(build_if_missing: bool = True):
     L.mc_batch_state_bytes.restype = C.c_size_t
     L.mc_batch_state_bytes.argtypes = [C.c_void_p]
     L.mc_batch_destroy.argtypes = [C.c_void_p]
+    L.mc_server_create.argtypes = [P(ServerDesc), P(C.c_void_p)]
+    L.mc_server_submit.argtypes = [C.c_void_p, P(Request), P(C.c_long)]
+    L.mc_server_poll.argtypes = [C.c_void_p, C.c_long, P(Result), P(C.c_double)]
+    L.mc_server_wait.argtypes = [C.c_void_p, C.c_long, C.c_double, P(Result), P(C.c_double)]
+    L.mc_server_stats.argtypes = [C.c_void_p, P(ServerCounters)]
+    L.mc_server_clock.restype = C.c_double
+    L.mc_server_clock.argtypes = [C.c_void_p]
+    L.mc_server_destroy.argtypes = [C.c_void_p]
     _lib = L
     return L
 

@@ -12,7 +12,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -966,6 +974,8 @@ int setupBatch(mc_batch_s* B) {
         for (const auto& sd : D.sd) oneD = oneD || (sd.accum >= 0 && sd.accum <= 2);
         I.gdif = oneD ? f + (size_t)I.rows * I.cols : nullptr;
         I.csum = f + (size_t)I.rows * I.cols + (size_t)I.rows * (I.cols + 1);
+        I.groups = 1;
+        I.gstride = 0;
         for (int r = 0; r < 4; ++r) {
             const bool timeRow = (pd.problem == MC_TEMP || pd.problem == MC_MULTI) && r == 0;
             const double q = std::ldexp(window * (timeRow ? 1.0 : vmax) * 1.0001, -61);
@@ -1005,6 +1015,7 @@ int setupBatch(mc_batch_s* B) {
     P.insts = (const InstD<R>*)B->insts;
     P.islot = B->islot;
     P.ninst = n;
+    P.maxGroups = 1;
     if (batchSmemBytes<R>(n) > 200 * 1024) return fail(MC_ERR_UNSUPPORTED, "too many instances in one batch");
     B->block = B->bd.block_size > 0 ? B->bd.block_size : 256;
     if (B->block % 32 || B->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
@@ -1080,6 +1091,315 @@ int batchCounters(mc_batch_s* B, mc_stats* st) {
 }
 
 }  // namespace
+
+// ================================================================ serving
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// One submitted solve.
+struct SrvJob {
+    long ticket = 0;
+    mc_request req{};
+    double tSubmit = 0., tAdmit = -1., tDone = -1.;
+    // resident device data
+    void* tables = nullptr;
+    void* sd = nullptr;
+    EmitterD* em = nullptr;
+    long long* cdf = nullptr;
+    double* fields = nullptr;  // groups x [tally rows*cols | difference rows*(cols+1)], then 4 checksums
+    double* acc = nullptr;     // running sum of round fields, rows*cols
+    long nemit = 0;
+    double power = 0., vmax = 0.;
+    int rows = 1, cols = 0, fluxRow0 = 0;
+    bool oneD = false;
+    double grad = 0., volume = 0.;
+    unsigned char image[512];  // host InstD<R> without the per-tick fields
+    // statistics over the batch-mean samples
+    long rounds = 0, samples = 0;
+    double mean = 0., m2 = 0.;
+    int status = MC_OK;
+    bool done = false;
+    std::vector<double> field;  // mean field at completion
+};
+
+struct ServerBase {
+    virtual ~ServerBase() = default;
+    virtual void loop() = 0;
+    mc_server_desc d{};
+    int dev = 0;
+    Clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable cv, cvDone;
+    std::deque<SrvJob*> pending;
+    std::vector<SrvJob*> active;
+    std::map<long, SrvJob*> jobs;
+    long nextTicket = 1;
+    long capacity = 0, inflight = 0;
+    bool stop = false;
+    mc_server_counters st{};
+    std::thread th;
+    std::string err;
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+void freeJobDevice(SrvJob* j) {
+    void* ps[] = {j->tables, j->sd, j->em, j->cdf, j->fields, j->acc};
+    for (void* p : ps) if (p) cudaFree(p);
+    j->tables = j->sd = nullptr; j->em = nullptr; j->cdf = nullptr; j->fields = nullptr; j->acc = nullptr;
+}
+
+template <typename R>
+struct ServerT : ServerBase {
+    void* state = nullptr;
+    unsigned long long* cnt = nullptr;
+    unsigned int* status = nullptr;
+    InstD<R>* insts_d = nullptr;
+    long long* islot_d = nullptr;
+    double** accs_d = nullptr;
+    double* gsum_d = nullptr;
+    cudaStream_t stream = nullptr;
+    int block = 256, grid = 0;
+    Params<R> base{};
+
+    int init() {
+        CK(cudaGetDevice(&dev));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        using V4 = typename Vec4<R>::T;
+        const size_t per = 2 * sizeof(V4) + sizeof(uint4);
+        capacity = (long)(d.hbm_budget / per);
+        if (capacity < 1024) return fail(MC_ERR_ARG, "hbm_budget too small");
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t cap = (size_t)capacity;
+        CK(cudaMalloc(&state, 2 * al(sizeof(V4) * cap) + al(sizeof(uint4) * cap)));
+        char* sb = (char*)state;
+        base.P0in = base.P0out = (V4*)sb; sb += al(sizeof(V4) * cap);
+        base.P1in = base.P1out = (V4*)sb; sb += al(sizeof(V4) * cap);
+        base.P2in = base.P2out = (uint4*)sb;
+        CK(cudaMalloc(&cnt, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
+        CK(cudaMalloc(&status, sizeof(unsigned int)));
+        CK(cudaMalloc(&insts_d, sizeof(InstD<R>) * d.max_active));
+        CK(cudaMalloc(&islot_d, sizeof(long long) * (d.max_active + 1)));
+        CK(cudaMalloc(&accs_d, sizeof(double*) * d.max_active));
+        CK(cudaMalloc(&gsum_d, sizeof(double) * d.max_active * MAX_GROUPS * 4));
+        base.counters = cnt;
+        base.status = status;
+        base.live_in = cnt + C_NCOUNTERS;
+        base.live_out = cnt + C_NCOUNTERS + 1;
+        base.dt = (R)d.dt;
+        base.nsteps = (int)d.nsteps;
+        base.ksteps = (int)d.nsteps;
+        base.insts = insts_d;
+        base.islot = islot_d;
+        base.maxGroups = d.groups;
+        block = d.block_size > 0 ? d.block_size : 256;
+        if (block % 32 || block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+        int nsm = 0;
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        const int occ = advanceBatchOccupancy<R>(d.max_active, block);
+        if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
+        grid = occ * nsm;
+        return MC_OK;
+    }
+
+    ~ServerT() override {
+        void* ps[] = {state, cnt, status, insts_d, islot_d, accs_d, gsum_d};
+        for (void* p : ps) if (p) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // upload a job's tables and domain, allocate its fields
+    int admit(SrvJob* j) {
+        const mc_material_s& m = *j->req.mat;
+        const mc_domain_s& D = *j->req.dom;
+        Params<R> P{};
+        int rc = uploadMaterial<R>(m, &j->tables, P, j->vmax);
+        if (rc) return rc;
+        rc = uploadDomain<R>(D, m.fluxSum, j->req.nemit, &j->sd, &j->em, &j->cdf, P, j->nemit, j->power);
+        if (rc) return rc;
+        j->rows = j->req.problem == MC_FLUX ? 3 : 4;
+        j->fluxRow0 = j->req.problem == MC_FLUX ? 0 : 1;
+        j->cols = (int)D.cols;
+        for (const auto& s : D.sd) j->oneD = j->oneD || (s.accum >= 0 && s.accum <= 2);
+        const size_t gstride = (size_t)j->rows * j->cols + (size_t)j->rows * (j->cols + 1);
+        CK(cudaMalloc(&j->fields, sizeof(double) * (gstride * d.groups + 4)));
+        CK(cudaMalloc(&j->acc, sizeof(double) * (size_t)j->rows * j->cols));
+        CK(cudaMemset(j->acc, 0, sizeof(double) * (size_t)j->rows * j->cols));
+        double vol = 0.;
+        for (double v : D.cellVol) vol += v;
+        j->volume = j->req.volume > 0. ? j->req.volume : vol;
+        j->grad = j->req.gradient != 0. ? j->req.gradient : D.pp[0].gradT[j->req.axis];
+        if (j->grad == 0.) return fail(MC_ERR_ARG, "no temperature gradient along the kappa axis");
+        InstD<R> I;
+        std::memset(&I, 0, sizeof(I));
+        I.vel = P.vel; I.vt = P.vt; I.wthr = P.wthr; I.wguide = P.wguide; I.pthr = P.pthr;
+        I.fwthr = P.fwthr; I.fpthr = P.fpthr;
+        I.sd = P.sd; I.em = P.em; I.emitCdf = P.emitCdf;
+        I.nw = P.nw; I.np = P.np; I.nem = P.nem; I.nsd = P.nsd;
+        I.problem = j->req.problem; I.rows = j->rows; I.cols = j->cols;
+        I.maxscat = j->req.maxscat;
+        I.maxloop = j->req.maxloop != 0 ? j->req.maxloop : 100 * j->req.maxscat;
+        I.nemit = j->nemit;
+        I.tally = j->fields;
+        I.gdif = j->oneD ? j->fields + (size_t)j->rows * j->cols : nullptr;
+        I.csum = j->fields + gstride * d.groups;
+        I.groups = d.groups;
+        I.gstride = (long long)gstride;
+        const double window = (double)d.nsteps * d.dt;
+        for (int r = 0; r < 4; ++r) {
+            const bool timeRow = j->req.problem == MC_MULTI && r == 0;
+            const double q = std::ldexp(window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
+            I.tq[r] = q;
+            I.tqinv[r] = (R)(1.0 / q);
+        }
+        static_assert(sizeof(InstD<R>) <= sizeof(j->image), "instance image");
+        std::memcpy(j->image, &I, sizeof(I));
+        return MC_OK;
+    }
+
+    int tick() {
+        const int n = (int)active.size();
+        std::vector<InstD<R>> inst(n);
+        std::vector<long long> islot(n + 1, 0);
+        std::vector<double*> accs(n);
+        for (int i = 0; i < n; ++i) {
+            SrvJob* j = active[i];
+            std::memcpy(&inst[i], j->image, sizeof(InstD<R>));
+            inst[i].inst = i;
+            inst[i].slot0 = islot[i];
+            const uint64_t seed = j->req.seed + (uint64_t)j->rounds;
+            inst[i].key0 = (uint32_t)seed;
+            inst[i].key1 = (uint32_t)(seed >> 32);
+            islot[i + 1] = islot[i] + j->nemit;
+            accs[i] = j->acc;
+            const size_t gstride = (size_t)inst[i].gstride;
+            CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * (gstride * d.groups + 4), stream));
+        }
+        CK(cudaMemcpyAsync(insts_d, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(islot_d, islot.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(accs_d, accs.data(), sizeof(double*) * n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(gsum_d, 0, sizeof(double) * n * MAX_GROUPS * 4, stream));
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), stream));
+        CK(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
+        Params<R> P = base;
+        P.cap = (unsigned long long)islot[n];
+        P.ninst = n;
+        P.step0 = 0;
+        CK(launchEmitBatch<R>(P, stream));
+        CK(launchAdvanceBatch<R>(P, grid, block, stream));
+        CK(launchDifPrefix<R>(P, stream));
+        CK(launchRoundReduce<R>(P, accs_d, gsum_d, stream));
+        std::vector<double> gsum((size_t)n * MAX_GROUPS * 4);
+        std::vector<unsigned long long> c(C_NCOUNTERS + 4);
+        CK(cudaMemcpyAsync(gsum.data(), gsum_d, sizeof(double) * gsum.size(), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(c.data(), cnt, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        st.phonon_steps += (double)c[C_PHONON_STEPS];
+        const int G = d.groups;
+        for (int i = 0; i < n; ++i) {
+            SrvJob* j = active[i];
+            j->rounds++;
+            for (int g = 0; g < G; ++g) {
+                const double q = G * j->power * gsum[((size_t)i * MAX_GROUPS + g) * 4 + j->fluxRow0 + j->req.axis] /
+                                 j->volume;
+                const double kappa = -q / j->grad;
+                // Welford (montecarlo/field.cpp:323-330)
+                j->samples++;
+                const double dlt = kappa - j->mean;
+                j->mean += dlt / (double)j->samples;
+                j->m2 += dlt * (kappa - j->mean);
+            }
+        }
+        return MC_OK;
+    }
+
+    void complete(SrvJob* j, int status) {
+        j->status = status;
+        // mean field: (sum of round tallies) / rounds, post-processed
+        const mc_material_s& m = *j->req.mat;
+        const mc_domain_s& D = *j->req.dom;
+        std::vector<double> a((size_t)j->rows * j->cols, 0.);
+        if (j->acc && j->rounds > 0)
+            cudaMemcpy(a.data(), j->acc, sizeof(double) * a.size(), cudaMemcpyDeviceToHost);
+        j->field.assign(a.size(), 0.);
+        for (int c = 0; c < j->cols; ++c)
+            for (int r = 0; r < j->rows; ++r) {
+                double v = a[(size_t)c * j->rows + r] / std::max(1L, j->rounds);
+                if (j->req.problem == MC_MULTI && r == 0) v /= m.energySum;
+                j->field[(size_t)c * j->rows + r] = j->power * (v / D.cellVol[c]);
+            }
+        freeJobDevice(j);
+        j->tDone = now();
+    }
+
+    void loop() override {
+        cudaSetDevice(dev);
+        for (;;) {
+            std::vector<SrvJob*> toAdmit;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                if (stop) break;
+                while (!pending.empty() && (int)(active.size() + toAdmit.size()) < d.max_active) {
+                    SrvJob* j = pending.front();
+                    const long need = j->req.nemit + 64;
+                    if (inflight + need > capacity && !(active.empty() && toAdmit.empty())) break;
+                    pending.pop_front();
+                    toAdmit.push_back(j);
+                    inflight += need;
+                }
+                if (active.empty() && toAdmit.empty()) {
+                    cv.wait_for(lk, std::chrono::milliseconds(5));
+                    continue;
+                }
+            }
+            for (SrvJob* j : toAdmit) {
+                int rc = (j->req.nemit + 64 > capacity) ? fail(MC_ERR_BUSY, "request larger than the HBM budget")
+                                                         : admit(j);
+                std::lock_guard<std::mutex> lk(mu);
+                if (rc) {
+                    freeJobDevice(j);
+                    j->status = rc;
+                    j->done = true;
+                    j->tDone = now();
+                    inflight -= j->req.nemit + 64;
+                    st.completed++;
+                    cvDone.notify_all();
+                    continue;
+                }
+                j->tAdmit = now();
+                active.push_back(j);
+                st.admitted++;
+            }
+            const double tb = now();
+            int rc = tick();
+            std::lock_guard<std::mutex> lk(mu);
+            st.ticks++;
+            st.busy_s += now() - tb;
+            std::vector<SrvJob*> keep;
+            for (SrvJob* j : active) {
+                const double se = j->samples > 1 ? std::sqrt(j->m2 / (double)(j->samples - 1) / (double)j->samples) : 1e300;
+                const bool conv = j->rounds >= d.min_rounds && se <= d.target_rel_se * std::fabs(j->mean);
+                const bool giveUp = j->rounds >= d.max_rounds;
+                if (rc || conv || giveUp) {
+                    complete(j, rc ? rc : (conv ? MC_OK : MC_ERR_BUSY));
+                    j->done = true;
+                    inflight -= j->req.nemit + 64;
+                    st.completed++;
+                } else {
+                    keep.push_back(j);
+                }
+            }
+            active.swap(keep);
+            cvDone.notify_all();
+        }
+    }
+};
+
+}  // namespace
+
+struct mc_server_s {
+    std::unique_ptr<ServerBase> impl;
+};
 
 // ================================================================== C ABI
 extern "C" {
@@ -1286,5 +1606,110 @@ size_t mc_batch_state_bytes(mc_batch_h b) { return b ? b->stateBytes : 0; }
 
 void mc_batch_destroy(mc_batch_h b) { freeBatch(b); }
 
+int mc_server_create(const mc_server_desc* d, mc_server_h* out) {
+    if (!d || !out) return fail(MC_ERR_ARG, "null argument");
+    if (!(d->dt > 0.) || d->nsteps <= 0 || d->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
+    if (d->precision != 32 && d->precision != 64) return fail(MC_ERR_ARG, "precision must be 32 or 64");
+    if (d->groups < 2 || d->groups > MAX_GROUPS) return fail(MC_ERR_ARG, "groups must be in 2..8");
+    if (d->max_active < 1 || d->max_active > 512) return fail(MC_ERR_ARG, "max_active must be in 1..512");
+    if (!(d->target_rel_se > 0.) || d->max_rounds < 1 || d->min_rounds < 1) return fail(MC_ERR_ARG, "invalid stopping rule");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    std::unique_ptr<ServerBase> impl;
+    if (d->precision == 32) { auto* t = new ServerT<float>; t->d = *d; impl.reset(t); rc = t->init(); }
+    else { auto* t = new ServerT<double>; t->d = *d; impl.reset(t); rc = t->init(); }
+    if (rc) return rc;
+    impl->t0 = Clock::now();
+    ServerBase* b = impl.get();
+    b->th = std::thread([b] { b->loop(); });
+    *out = new mc_server_s{std::move(impl)};
+    return MC_OK;
+}
+
+int mc_server_submit(mc_server_h s, const mc_request* r, long* ticket) {
+    if (!s || !r || !ticket) return fail(MC_ERR_ARG, "null argument");
+    if (!r->mat || !r->dom || r->nemit <= 0 || r->maxscat <= 0 || r->maxloop < 0 || r->axis < 0 || r->axis > 2)
+        return fail(MC_ERR_ARG, "invalid request");
+    if (r->problem != MC_FLUX && r->problem != MC_MULTI) return fail(MC_ERR_ARG, "kappa needs a flux problem");
+    ServerBase* b = s->impl.get();
+    SrvJob* j = new SrvJob;
+    j->req = *r;
+    std::lock_guard<std::mutex> lk(b->mu);
+    j->ticket = b->nextTicket++;
+    j->tSubmit = b->now();
+    b->jobs[j->ticket] = j;
+    b->pending.push_back(j);
+    b->st.submitted++;
+    *ticket = j->ticket;
+    b->cv.notify_all();
+    return MC_OK;
+}
+
+static int pollLocked(ServerBase* b, long ticket, mc_result* res, double* field) {
+    auto it = b->jobs.find(ticket);
+    if (it == b->jobs.end()) return fail(MC_ERR_ARG, "unknown ticket");
+    SrvJob* j = it->second;
+    if (!j->done) return 0;
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->kappa = j->mean;
+        res->kappa_se = j->samples > 1 ? std::sqrt(j->m2 / (double)(j->samples - 1) / (double)j->samples) : 0.;
+        res->rounds = j->rounds;
+        res->phonons = j->rounds * j->nemit;
+        res->phonon_steps = (double)j->rounds * (double)j->nemit * (double)b->d.nsteps;
+        res->t_submit = j->tSubmit;
+        res->t_admit = j->tAdmit;
+        res->t_done = j->tDone;
+        res->status = j->status;
+    }
+    if (field && !j->field.empty()) std::memcpy(field, j->field.data(), sizeof(double) * j->field.size());
+    return 1;
+}
+
+int mc_server_poll(mc_server_h s, long ticket, mc_result* res, double* field) {
+    if (!s) return fail(MC_ERR_ARG, "null server");
+    std::lock_guard<std::mutex> lk(s->impl->mu);
+    return pollLocked(s->impl.get(), ticket, res, field);
+}
+
+int mc_server_wait(mc_server_h s, long ticket, double timeout_s, mc_result* res, double* field) {
+    if (!s) return fail(MC_ERR_ARG, "null server");
+    ServerBase* b = s->impl.get();
+    std::unique_lock<std::mutex> lk(b->mu);
+    const auto until = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(timeout_s));
+    for (;;) {
+        int rc = pollLocked(b, ticket, res, field);
+        if (rc != 0) return rc;
+        if (b->cvDone.wait_until(lk, until) == std::cv_status::timeout) return pollLocked(b, ticket, res, field);
+    }
+}
+
+int mc_server_stats(mc_server_h s, mc_server_counters* st) {
+    if (!s || !st) return fail(MC_ERR_ARG, "null argument");
+    ServerBase* b = s->impl.get();
+    std::lock_guard<std::mutex> lk(b->mu);
+    *st = b->st;
+    st->queued = (long)b->pending.size();
+    st->active = (long)b->active.size();
+    st->uptime_s = b->now();
+    return MC_OK;
+}
+
+double mc_server_clock(mc_server_h s) { return s ? s->impl->now() : 0.; }
+
+void mc_server_destroy(mc_server_h s) {
+    if (!s) return;
+    ServerBase* b = s->impl.get();
+    {
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->stop = true;
+        b->cv.notify_all();
+    }
+    if (b->th.joinable()) b->th.join();
+    for (auto& kv : b->jobs) { freeJobDevice(kv.second); delete kv.second; }
+    delete s;
+}
+
 }  // extern "C"
+
 

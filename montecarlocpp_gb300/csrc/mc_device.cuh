@@ -101,6 +101,7 @@ struct Params {
     const InstD<R>* insts;
     const long long* islot;
     int ninst;
+    int maxGroups;  // largest field-copy count of the instances
 };
 
 // One problem instance as the advance loop sees it: material tables,
@@ -129,6 +130,9 @@ struct InstD {
     double* tally;                    // global field, rows x cols column-major
     double* gdif;                     // global difference array, rows x (cols + 1), or null
     double* csum;                     // per-row checksum
+    int groups;                       // phonon id % groups picks a field copy
+    int pad2;
+    long long gstride;                // doubles between field copies (tally and gdif)
     R tqinv[4];
     double tq[4];
 };

@@ -66,6 +66,7 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         I->tal = TM == TM_SHARED ? tal : nullptr;
         I->dif = TM == TM_SHARED ? tal + (size_t)P.rows * P.cols : nullptr;
         I->tally = P.tally; I->gdif = nullptr; I->csum = P.csum;
+        I->groups = 1; I->gstride = 0;
         for (int r = 0; r < 4; ++r) { I->tqinv[r] = P.tqinv[r]; I->tq[r] = P.tq[r]; }
     }
     return I;
@@ -371,16 +372,17 @@ __host__ __device__ inline size_t batchSmemBytes(int ninst) {
     return sizeof(InstD<R>) * (size_t)ninst + sizeof(long long) * ((size_t)ninst + 1);
 }
 
-// Global difference arrays -> field: block (i, r) prefix-sums row r of
-// instance i and adds it to the instance's field.
+// Global difference arrays -> field: block (i, y) prefix-sums row y % 4 of
+// field copy y / 4 of instance i and adds it to that copy.
 template <typename R>
 __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
     const InstD<R>& I = P.insts[blockIdx.x];
-    const int r = blockIdx.y;
-    if (r >= I.rows || I.gdif == nullptr) return;
+    const int r = blockIdx.y & 3, grp = blockIdx.y >> 2;
+    if (r >= I.rows || grp >= I.groups || I.gdif == nullptr) return;
+    const long long go = (long long)grp * I.gstride;
     const int lane = threadIdx.x;
     double carry = 0.0;
-    const double* dr = I.gdif + (size_t)r * (I.cols + 1);
+    const double* dr = I.gdif + go + (size_t)r * (I.cols + 1);
     for (int c0 = 0; c0 < I.cols; c0 += 32) {
         const int c = c0 + lane;
         double x = c < I.cols ? dr[c] : 0.0;
@@ -389,9 +391,51 @@ __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
             if (lane >= o) x += y;
         }
         x += carry;
-        if (c < I.cols) I.tally[(size_t)c * I.rows + r] += x;
+        if (c < I.cols) I.tally[go + (size_t)c * I.rows + r] += x;
         carry = __shfl_sync(0xFFFFFFFFu, x, 31);
     }
+}
+
+// End of a served round, block (x, i): over instance i's field copies,
+// acc += sum of the copies, and gsum[i][g][r] = sum over cells of row r of
+// copy g (the batch-mean samples), one atomic per warp and (g, r).
+constexpr int MAX_GROUPS = 8;
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_round_reduce(Params<R> P, double* const* accs, double* gsum) {
+    const InstD<R>& I = P.insts[blockIdx.y];
+    const int n = I.rows * I.cols;
+    const int G = I.groups;
+    double part[MAX_GROUPS][4];
+#pragma unroll
+    for (int g = 0; g < MAX_GROUPS; ++g)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) part[g][r] = 0.0;
+    double* a = accs[blockIdx.y];
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const int r = e % I.rows;
+        double s = 0.0;
+#pragma unroll
+        for (int g = 0; g < MAX_GROUPS; ++g) {
+            if (g < G) {
+                const double v = I.tally[(long long)g * I.gstride + e];
+                s += v;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q == r) part[g][q] += v;
+            }
+        }
+        a[e] += s;
+    }
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int g = 0; g < MAX_GROUPS; ++g)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            double x = part[g][r];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+            if (lane == 0 && g < G && r < I.rows && x != 0.0) atomicAdd(&gsum[((long long)blockIdx.y * MAX_GROUPS + g) * 4 + r], x);
+        }
 }
 
 // Stream compaction of the live slots of a dynamic-kernel state into the

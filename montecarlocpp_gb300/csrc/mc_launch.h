@@ -28,6 +28,9 @@ template <typename R>
 cudaError_t launchDifPrefix(const Params<R>& p, cudaStream_t s);
 template <typename R>
 int advanceBatchOccupancy(int ninst, int block);
+template <typename R>
+cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
+                              cudaStream_t s);
 
 // Maximum resident blocks per SM of the advance kernel for this
 // configuration (0 if it cannot launch).

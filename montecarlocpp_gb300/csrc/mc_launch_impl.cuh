@@ -65,7 +65,14 @@ cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int grid, int 
 
 template <>
 cudaError_t launchDifPrefix<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
-    k_difprefix<MC_REAL><<<dim3((unsigned)p.ninst, 4), 32, 0, s>>>(p);
+    k_difprefix<MC_REAL><<<dim3((unsigned)p.ninst, 4u * (unsigned)p.maxGroups), 32, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launchRoundReduce<MC_REAL>(const Params<MC_REAL>& p, double* const* accs, double* gsum,
+                                       cudaStream_t s) {
+    k_round_reduce<MC_REAL><<<dim3(64, (unsigned)p.ninst), 256, 0, s>>>(p, accs, gsum);
     return cudaGetLastError();
 }
 

@@ -93,6 +93,7 @@ __device__ __forceinline__ double toDouble(double v) { return v; }
 template <typename R, int TM>
 struct Tally {
     const InstD<R>* I;
+    long long goff;  // offset of the phonon's field copy (global layouts)
     // amount per metre of flight, rows entries: Temp sign/v; Flux sign*d
     R rho[4];
 
@@ -110,7 +111,7 @@ struct Tally {
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < I->rows) atomicAdd(&I->tally[(size_t)col * I->rows + r], toDouble(rho[r] * t));
+            if (r < I->rows) atomicAdd(&I->tally[goff + (size_t)col * I->rows + r], toDouble(rho[r] * t));
     }
     // interior cells [c0, c1) of a 1-D walk (stride 1) each with path t
     __device__ __forceinline__ void addGlobalRange(int c0, int c1, R t) const {
@@ -119,8 +120,8 @@ struct Tally {
             for (int r = 0; r < 4; ++r) {
                 if (r < I->rows) {
                     const double v = toDouble(rho[r] * t);
-                    atomicAdd(&I->gdif[(size_t)r * (I->cols + 1) + c0], v);
-                    atomicAdd(&I->gdif[(size_t)r * (I->cols + 1) + c1], -v);
+                    atomicAdd(&I->gdif[goff + (size_t)r * (I->cols + 1) + c0], v);
+                    atomicAdd(&I->gdif[goff + (size_t)r * (I->cols + 1) + c1], -v);
                 }
             }
         } else {
@@ -418,6 +419,7 @@ struct Walker {
     R tnext;       // time to the next event after the window end
     int nev;
     int stop;      // 0 alive, else the counter of the stop reason
+    long long goff;  // field copy of this phonon (batch means)
     Rng<REPLAY> g;
 
     __device__ __forceinline__ void load(const Params<R>& P, const InstD<R>* inst, const Window<R>& W,
@@ -443,6 +445,7 @@ struct Walker {
         stop = 0;
         nev = 0;
         tnext = R(0);
+        goff = I->groups > 1 ? (long long)(ph.id % (uint32_t)I->groups) * I->gstride : 0;
     }
 
     __device__ __forceinline__ void pack(typename Vec4<R>::T& A0, typename Vec4<R>::T& A1, uint4& A2) const {
@@ -473,6 +476,7 @@ struct Walker {
         // tally amounts per metre (montecarlo/problem.cpp:473-544)
         Tally<R, TM> T;
         T.I = I;
+        T.goff = goff;
         if (I->problem == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
         else if (I->problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
         else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }

@@ -1,0 +1,98 @@
+"""The serving loop: completion by the stopping rule, isolation (a result is
+the same alone and in the mix), HBM-budget admission, and kappa against the
+FP64 oracle."""
+
+import numpy as np
+import pytest
+
+import montecarlocpp_gb300 as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+DT, NSTEPS = 0.5e-12, 1000
+
+
+@pytest.fixture(scope="module")
+def mats():
+    return {T: M.Material.silicon(T) for T in (150.0, 300.0)}
+
+
+def test_one_round_equals_single_solve(mats):
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 50)
+    srv = M.Server(dt=DT, nsteps=NSTEPS, precision=64, groups=4, min_rounds=1, max_rounds=1)
+    t = srv.submit(mats[300.0], dom, 20000, problem=M.MULTI, seed=77)
+    r = srv.wait(t)
+    srv.close()
+    assert r["rounds"] == 1
+    P = M.MultiProblem(mats[300.0], dom, 20000, 10**6)
+    f = P.solve(dt=DT, nsteps=NSTEPS, precision=64, seed=77)
+    kappa = M.kappa_from_flux(f, dom, 0, flux_row0=1)
+    assert r["kappa"] == pytest.approx(kappa, rel=1e-9)
+    assert np.allclose(r["field"], f, rtol=1e-9, atol=1e-9 * np.abs(f).max())
+
+
+def _requests(mats):
+    return [
+        (mats[300.0], M.FilmDomain.from_cli(1e-7, 1e-7, 50), 60000, 1),
+        (mats[150.0], M.FilmDomain.from_cli(1e-7, 3e-8, 30), 40000, 2),
+        (mats[300.0], M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4)), 50000, 3),
+        (mats[150.0], M.FilmDomain.from_cli(1e-7, 5e-7, 100), 30000, 4),
+    ]
+
+
+def test_isolation_alone_and_in_the_mix(mats):
+    reqs = _requests(mats)
+    kw = dict(dt=DT, nsteps=NSTEPS, precision=32, groups=8, target_rel_se=0.03, min_rounds=1, max_rounds=50)
+    alone = []
+    for mat, dom, n, seed in reqs:
+        srv = M.Server(**kw)
+        alone.append(srv.wait(srv.submit(mat, dom, n, seed=seed)))
+        srv.close()
+    srv = M.Server(**kw)
+    tickets = [srv.submit(mat, dom, n, seed=seed) for mat, dom, n, seed in reqs]
+    mixed = [srv.wait(t) for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs)
+    for a, b in zip(alone, mixed):
+        assert a["status"] == b["status"] == 0
+        assert a["rounds"] == b["rounds"]
+        # same phonons, same trajectories; only the FP64 atomic order differs
+        assert b["kappa"] == pytest.approx(a["kappa"], rel=1e-9)
+        assert b["kappa_se"] <= 0.03 * abs(b["kappa"])
+
+
+def test_hbm_budget_queues_and_completes(mats):
+    reqs = _requests(mats)
+    # room for about one request's phonon state at a time
+    srv = M.Server(dt=DT, nsteps=NSTEPS, precision=32, hbm_budget=70000 * 48, groups=4, target_rel_se=0.05,
+                   max_rounds=40)
+    tickets = [srv.submit(mat, dom, n, seed=seed) for mat, dom, n, seed in reqs]
+    res = [srv.wait(t) for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert all(r["status"] == 0 for r in res)
+    assert st["admitted"] == st["completed"] == len(reqs)
+    # admission was serial: each request was admitted after the previous finished
+    ends = sorted(r["t_done"] for r in res)
+    admits = sorted(r["t_admit"] for r in res)
+    assert all(a >= e - 1e-6 for a, e in zip(admits[1:], ends[:-1]))
+
+
+def test_kappa_against_fp64_oracle(mats):
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 20)
+    srv = M.Server(dt=DT, nsteps=NSTEPS, precision=32, groups=8, target_rel_se=0.01, max_rounds=200)
+    r = srv.wait(srv.submit(mats[300.0], dom, 100000, seed=5))
+    srv.close()
+    assert r["status"] == 0 and r["kappa_se"] <= 0.01 * r["kappa"]
+    omat = O.OMaterial(*M.silicon_tables(), 300.0)
+    od = O.ODomain(dom)
+    ks = []
+    for s in range(8):
+        o, _, _ = O.solve(omat, od, O.FLUX, nemit=40000, maxscat=10**6, dt=DT, horizon=DT * NSTEPS, rng=O.RNG_MT,
+                          nchunk=8, seed=1000 * s)
+        ks.append(M.kappa_from_flux(o, dom, 0, flux_row0=0))
+    ks = np.array(ks)
+    se = np.sqrt(ks.var(ddof=1) / len(ks) + r["kappa_se"] ** 2)
+    assert abs(ks.mean() - r["kappa"]) < 3 * se
