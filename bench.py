@@ -35,6 +35,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
@@ -183,6 +185,11 @@ def main():
     ap.add_argument("--k", type=int, default=0, help="dt-steps per launch (0: tuned)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-duration", type=float, default=5.0)
+    ap.add_argument("--serve-drain", type=float, default=20.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="one device-resident solve of the workload (for ncu), no JSON line")
     args = ap.parse_args()
@@ -308,6 +315,10 @@ def main():
 
     if not args.no_plain:
         line["plain_kernel"] = plain_kernel(prob, W, stream, peak, peak_kind)
+    if not args.no_batched:
+        line["batched"] = bench_batched(stream)
+    if not args.no_served:
+        line["served"] = bench_served(rate=args.serve_rate, duration=args.serve_duration, drain=args.serve_drain)
     if rank == 0 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_baseline(W, int(os.environ.get("MC_CPU_SAMPLE", 400_000)))
@@ -318,6 +329,120 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def bench_batched(stream, reps=2, plain=True):
+    """Config 3: 64 in-plane films (thickness log-U(10 nm, 10 um), T_eq U(100,
+    400 K), phonons proportional to thickness, 1e4..1e6), 100 cells each,
+    dt 0.5 ps x 4000 steps, FP32 flight / FP64 tallies. solves/s of one
+    batched run (one persistent launch, CUDA graph) against the same 64
+    solves one at a time with the plain per-dt-step kernel and with the
+    fused single-instance kernel; kappa of the FP32 batch against an FP64
+    batch of the same phonons."""
+    import torch
+
+    import montecarlocpp_gb300 as M
+    from montecarlocpp_gb300.workloads import batched_films
+    specs = batched_films(0)
+    dt, nsteps = 0.5e-12, 4000
+    mats = {}
+    probs = []
+    for sp in specs:
+        T = round(sp.T, 6)
+        if T not in mats:
+            mats[T] = M.Material.silicon(T)
+        probs.append(M.MultiProblem(mats[T], M.FilmDomain.from_cli(1e-7, sp.thickness, sp.cells), sp.nemit,
+                                    1_000_000))
+    seeds = list(range(len(probs)))
+    B = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=32, use_graph=True,
+                stream=stream.cuda_stream)
+    B.run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        B.run()
+        st = B.stats()  # synchronises
+        times.append(time.perf_counter() - t0)
+    tb = min(times)
+    k32 = [M.kappa_from_flux(B.result(i)[0], probs[i].dom, 0, flux_row0=1) for i in range(len(probs))]
+    out = {"workload": "64 films, thickness log-U(10 nm, 10 um), T U(100, 400 K), 1e4..1e6 phonons, 100 cells, "
+                       "dt 0.5 ps x 4000 steps",
+           "phonons": int(st["nemit"]), "phonon_steps": st["phonon_steps"],
+           "batched_s": tb, "batched_solves_per_s": len(probs) / tb,
+           "batched_phonon_steps_per_s": st["phonon_steps"] / tb, "launches_per_run": st["launches"]}
+    B.close()
+    B64 = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=64, use_graph=False)
+    B64.run()
+    k64 = [M.kappa_from_flux(B64.result(i)[0], probs[i].dom, 0, flux_row0=1) for i in range(len(probs))]
+    B64.close()
+    out["kappa_fp32_vs_fp64_max_rel"] = float(max(abs(a - b) / abs(b) for a, b in zip(k32, k64)))
+    out["kappa_range"] = [float(min(k32)), float(max(k32))]
+    t0 = time.perf_counter()
+    for p, s in zip(probs, seeds):
+        p.solve(dt=dt, nsteps=nsteps, precision=32, seed=s)
+    tf = time.perf_counter() - t0
+    out["fused_single_s"] = tf
+    out["fused_single_solves_per_s"] = len(probs) / tf
+    if plain:
+        t0 = time.perf_counter()
+        for p, s in zip(probs, seeds):
+            p.solve(dt=dt, nsteps=nsteps, precision=32, seed=s, steps_per_launch=1, schedule=1)
+        tp = time.perf_counter() - t0
+        out["plain_s"] = tp
+        out["plain_solves_per_s"] = len(probs) / tp
+        out["batched_vs_plain"] = tp / tb
+    return out
+
+
+def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budget_gb=64.0):
+    """Config 4: Poisson requests (film or pore cell, size log-U(20 nm, 2 um),
+    T U(100, 400 K), phonons per round log-U(1e4, 1e7)) submitted at their
+    arrival times to the serving loop; each solve runs until kappa has a 1%
+    standard error. Reports completed solves/s and p50/p99 latency."""
+    import montecarlocpp_gb300 as M
+    from montecarlocpp_gb300.workloads import served_requests
+    reqs = served_requests(seed, rate, duration)
+    srv = M.Server(dt=0.5e-12, nsteps=nsteps, precision=32, hbm_budget=int(budget_gb * (1 << 30)), max_active=256,
+                   groups=8, target_rel_se=0.01, min_rounds=1, max_rounds=2000)
+    mats = {}
+    doms = []
+    for r in reqs:
+        T = round(r.T, 3)
+        if T not in mats:
+            mats[T] = M.Material.silicon(T)
+        if r.geometry == "film":
+            doms.append((M.FilmDomain.from_cli(1e-7, r.size, 100), 0.0))
+        else:
+            doms.append((M.PoreCellDomain(r.size, r.size / 2, (12, 26, 12)), r.size ** 3))
+    for d, _ in doms:
+        M.problem._handle(d)  # library images built before the clock starts
+    t0 = time.perf_counter()
+    c0 = srv.clock()
+    tickets = []
+    for r, (d, vol) in zip(reqs, doms):
+        while time.perf_counter() - t0 < r.t_arrival:
+            time.sleep(0.0005)
+        tickets.append(srv.submit(mats[round(r.T, 3)], d, r.nemit, seed=len(tickets), volume=vol))
+    deadline = time.perf_counter() + drain
+    done = []
+    for t in tickets:
+        res = srv.wait(t, max(0.0, deadline - time.perf_counter()))
+        if res is not None:
+            done.append(res)
+    st = srv.stats()
+    srv.close()
+    lat = sorted(r["t_done"] - r["t_submit"] for r in done)
+    span = (max(r["t_done"] for r in done) - c0) if done else float("nan")
+    pct = (lambda q: float(np.percentile(lat, q))) if lat else (lambda q: None)
+    return {"workload": f"Poisson {rate:g}/s for {duration:g} s, film or pore cell, size log-U(20 nm, 2 um), "
+                        f"T U(100, 400 K), 1e4..1e7 phonons per round, dt 0.5 ps x {nsteps} steps, "
+                        "until SE(kappa) <= 1%",
+            "offered": len(reqs), "completed": len(done), "solves_per_s": len(done) / span if done else 0.0,
+            "p50_s": pct(50), "p99_s": pct(99), "ticks": st["ticks"], "busy_s": st["busy_s"],
+            "phonon_steps_per_s": st["phonon_steps"] / max(st["busy_s"], 1e-9),
+            "converged": sum(1 for r in done if r["status"] == 0),
+            "saturated": len(done) < len(reqs)}
 
 
 def profile_case(args):
