@@ -156,6 +156,41 @@ typedef struct {
  * power * postProc(tally) / cellVol. Host buffers; synchronous. */
 int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st);
 
+/* Size of the fixed device scratch array behind mc_solve_noalloc: 32 MiB,
+ * held on every device that loads this library until the process exits. */
+#define MC_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* No counterpart in the reference: an extra entry point of this library.
+ *
+ * mc_solve without any device allocation. It is for callers that cannot
+ * call cudaMalloc / cudaFree: a process whose device memory is already
+ * owned by another allocator (a framework's caching pool, a runtime that
+ * reserves most of the GPU at start-up), where a fresh cudaMalloc can fail
+ * although that pool has room, and loops that cannot take the implicit
+ * device-wide synchronisation of cudaFree. It calls no cudaMalloc,
+ * cudaFree or other allocating routine: every device buffer of the solve
+ * (tables, subdomain images, phonon state, counters, tally) is placed in
+ * one file-scope device array of MC_NOALLOC_SCRATCH_BYTES. A problem that
+ * needs more (48 B per phonon with FP32 flight, 80 B with FP64, plus the
+ * tables and rows x cols x 8 B of tally) is rejected with MC_ERR_ARG
+ * before any work is queued.
+ *
+ * Arguments, output and results are those of mc_solve, except: replay
+ * streams and trajectory logs are rejected (MC_ERR_UNSUPPORTED); the
+ * schedule is always the in-place dynamic one (p->schedule and
+ * p->compact_interval are ignored); a NULL p->stream means the legacy
+ * default stream; st->kernel_ms is 0. Synchronous.
+ *
+ * The first call on a device looks up the array's device address there
+ * (which can also load this library's device code on that device): make
+ * that first call before any stream capture begins. All calls on a device
+ * share the one array, which keeps the last call's contents; each call
+ * clears what must start at zero (counters, status word, tally, checksum)
+ * and overwrites the rest before reading it. Calls whose GPU work overlaps
+ * (from two host threads, say) race on the array and corrupt each other's
+ * results: serialise them. */
+int mc_solve_noalloc(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st);
+
 /* ---------------------------------------------- device-resident session */
 typedef struct mc_session_s* mc_session_h;
 

@@ -1401,6 +1401,189 @@ struct mc_server_s {
     std::unique_ptr<ServerBase> impl;
 };
 
+// ====================================================== no-allocation solve
+// The one device array behind mc_solve_noalloc. Host code must not pass
+// its name to a kernel (on the host it is only a stand-in for the symbol):
+// noallocScratch() asks the runtime for its device address on the current
+// device and the kernels receive that.
+static __device__ __align__(256) unsigned char g_noallocScratch[MC_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noallocMu;
+void* g_noallocPtr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noallocScratch on the current device, looked up once
+// per device (the lookup can load this file's device code on that device).
+int noallocScratch(void** out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return fail(MC_ERR_UNSUPPORTED, "mc_solve_noalloc: device ordinal above 63");
+    std::lock_guard<std::mutex> lk(g_noallocMu);
+    if (!g_noallocPtr[dev]) {
+        void* p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noallocScratch));
+        if (!p) return fail(MC_ERR_CUDA, "mc_solve_noalloc: no device address for the scratch array");
+        g_noallocPtr[dev] = p;
+    }
+    *out = g_noallocPtr[dev];
+    return MC_OK;
+}
+
+// setupSession's buffers placed in `base` (cap bytes) instead of allocated:
+// material tables, subdomain images, emitters, one half of the phonon state
+// (the in-place dynamic schedule without compaction never touches the
+// other), counters, status word, tally and checksum. The size check comes
+// before any copy. Counters, status, tally and checksum are cleared by
+// emitT; everything else is written here or by the emission kernel.
+template <typename R>
+int placeSession(mc_session_s* S, char* base, size_t cap) {
+    const mc_material_s& m = *S->mat;
+    const mc_domain_s& D = *S->dom;
+    using V4 = typename Vec4<R>::T;
+    // phonon allocation (montecarlo/problem.cpp:315-342), as in uploadDomain
+    const long ne = (long)D.em.size();
+    if (ne == 0) return fail(MC_ERR_ARG, "No phonons to emit");
+    double wsum = 0.;
+    for (double w : D.emWeight) wsum += w;
+    std::vector<long long> cdf(ne);
+    long long tot = 0;
+    for (long i = 0; i < ne; ++i) {
+        if (!(D.emWeight[i] > 0.)) return fail(MC_ERR_ARG, "No phonons to emit");
+        const double rounded = std::ceil(D.emWeight[i] / wsum * S->desc.nemit - 0.5);
+        tot += std::max(1LL, (long long)rounded);
+        cdf[i] = tot;
+    }
+    S->nemit = (long)tot;
+    S->power = wsum / (double)tot * m.fluxSum / 4.;
+    S->rows = S->desc.problem == MC_TEMP ? 1 : (S->desc.problem == MC_FLUX ? 3 : 4);
+    const size_t nt = (size_t)m.nw * m.np, n = (size_t)S->nemit;
+    const size_t nval = (size_t)S->rows * std::max(D.cols, 1L);
+    size_t off = 0;
+    auto take = [&off](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t oVel = take(sizeof(R) * nt);
+    const size_t oVt = take(sizeof(R) * nt);
+    const size_t oWthr = take(8 * (size_t)m.nw);
+    const size_t oPthr = take(8 * nt);
+    const size_t oFwthr = take(8 * (size_t)m.nw);
+    const size_t oFpthr = take(8 * nt);
+    const size_t oGuide = take(2 * GUIDE);
+    const size_t oSd = take(sizeof(SdomD<R>) * D.sd.size());
+    const size_t oEm = take(sizeof(EmitterD) * ne);
+    const size_t oCdf = take(sizeof(long long) * ne);
+    const size_t oP0 = take(sizeof(V4) * n);
+    const size_t oP1 = take(sizeof(V4) * n);
+    const size_t oP2 = take(sizeof(uint4) * n);
+    const size_t oCnt = take(sizeof(unsigned long long) * (C_NCOUNTERS + 4));
+    const size_t oStatus = take(sizeof(unsigned int));
+    const size_t oTally = take(sizeof(double) * nval);
+    const size_t oCsum = take(sizeof(double) * 4);
+    if (off > cap) {
+        char msg[320];
+        std::snprintf(msg, sizeof msg,
+                      "mc_solve_noalloc: this problem needs %zu bytes of device scratch (%ld phonons x %zu B, "
+                      "tables, %zu tally values), above the fixed maximum MC_NOALLOC_SCRATCH_BYTES = %zu; "
+                      "use mc_solve or fewer phonons", off, S->nemit, 2 * sizeof(V4) + sizeof(uint4), nval, cap);
+        return fail(MC_ERR_ARG, msg);
+    }
+    cudaStream_t s = S->stream;
+    Params<R> P{};
+    // material tables in the flight precision (as uploadMaterial)
+    std::vector<R> vel(nt), vt(nt);
+    double vmax = 0.;
+    for (size_t i = 0; i < nt; ++i) {
+        vel[i] = (R)m.vel[i];
+        vt[i] = (R)(m.vel[i] * m.tau[i]);
+        vmax = std::max(vmax, m.vel[i]);
+    }
+    S->vmax = vmax;
+    std::vector<uint16_t> guide(GUIDE);
+    for (int k = 0; k < GUIDE; ++k) {
+        const unsigned long long x = (unsigned long long)k << (32 - GUIDE_BITS);
+        long i = 0;
+        while (i < m.nw - 1 && x >= m.swthr[i]) ++i;
+        guide[k] = (uint16_t)i;
+    }
+    std::vector<SdomD<R>> sd(D.sd.size());
+    for (size_t i = 0; i < sd.size(); ++i) castSdom(D.sd[i], sd[i], sizeof(R) == 4);
+    CK(cudaMemcpyAsync(base + oVel, vel.data(), sizeof(R) * nt, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oVt, vt.data(), sizeof(R) * nt, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oWthr, m.swthr.data(), 8 * m.nw, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oPthr, m.spthr.data(), 8 * nt, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oFwthr, m.fwthr.data(), 8 * m.nw, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oFpthr, m.fpthr.data(), 8 * nt, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oGuide, guide.data(), 2 * GUIDE, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oSd, sd.data(), sizeof(SdomD<R>) * sd.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oEm, D.em.data(), sizeof(EmitterD) * ne, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(base + oCdf, cdf.data(), sizeof(long long) * ne, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the host vectors above end with this function
+    P.vel = (const R*)(base + oVel);
+    P.vt = (const R*)(base + oVt);
+    P.wthr = (const unsigned long long*)(base + oWthr);
+    P.pthr = (const unsigned long long*)(base + oPthr);
+    P.fwthr = (const unsigned long long*)(base + oFwthr);
+    P.fpthr = (const unsigned long long*)(base + oFpthr);
+    P.wguide = (const uint16_t*)(base + oGuide);
+    P.nw = (int)m.nw;
+    P.np = (int)m.np;
+    P.sd = (const SdomD<R>*)(base + oSd);
+    P.nsd = (int)D.sd.size();
+    P.em = (const EmitterD*)(base + oEm);
+    P.emitCdf = (const long long*)(base + oCdf);
+    P.nem = (int)ne;
+    // one state half: P*out alias P*in
+    P.P0in = P.P0out = (V4*)(base + oP0);
+    P.P1in = P.P1out = (V4*)(base + oP1);
+    P.P2in = P.P2out = (uint4*)(base + oP2);
+    S->cnt_d = (unsigned long long*)(base + oCnt);
+    S->status_d = (unsigned int*)(base + oStatus);
+    S->tally_d = (double*)(base + oTally);
+    S->csum_d = (double*)(base + oCsum);
+    P.problem = S->desc.problem; P.rows = S->rows; P.cols = (int)D.cols;
+    P.nemit = S->nemit;
+    P.maxscat = S->desc.maxscat;
+    P.maxloop = S->maxloop;
+    P.dt = (R)S->desc.dt;
+    P.nsteps = (int)S->desc.nsteps;
+    P.ksteps = S->desc.steps_per_launch;
+    P.key0 = (uint32_t)S->desc.seed;
+    P.key1 = (uint32_t)(S->desc.seed >> 32);
+    P.counters = S->cnt_d;
+    P.cap = (unsigned long long)S->nemit;
+    P.status = S->status_d;
+    P.tally = S->tally_d;
+    P.csum = S->csum_d;
+    // launch configuration (as setupSession)
+    const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
+    S->tm = S->desc.tally_mode;
+    if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
+    {
+        const int nsdShared = sizeof(SdomD<R>) * D.sd.size() <= SD_SHARED_MAX ? (int)D.sd.size() : 0;
+        SmemLayout L;
+        L.init<R>((int)m.nw, (int)m.np, nsdShared, S->rows, (int)D.cols, S->tm == TM_SHARED);
+        S->smem = L.total;
+    }
+    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
+    S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
+    if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int occ = advanceOccupancy<R>(true, false, false, S->tm, S->block, S->smem);
+    if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
+    S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    paramsOf<R>(S) = P;
+    return MC_OK;
+}
+
+}  // namespace
+
 // ================================================================== C ABI
 extern "C" {
 
@@ -1528,6 +1711,46 @@ int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* o
     cudaEventDestroy(e1);
     std::string msg = g_err;
     mc_session_destroy(s);
+    g_err = msg;
+    return rc;
+}
+
+// The solve of mc_solve with every device buffer inside g_noallocScratch:
+// a session object on the host stack whose pointers lead into the array,
+// driven through the same emission, advance and result steps. Nothing is
+// allocated on the device and nothing is freed.
+int mc_solve_noalloc(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st) {
+    if (!m || !d || !p) return fail(MC_ERR_ARG, "null argument");
+    if (p->problem < MC_TEMP || p->problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+    if (p->nemit <= 0 || p->maxscat <= 0 || p->maxloop < 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
+    if (!(p->dt > 0.) || p->nsteps <= 0 || p->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
+    if (p->steps_per_launch <= 0) return fail(MC_ERR_ARG, "steps_per_launch must be >= 1");
+    if (p->precision != 32 && p->precision != 64) return fail(MC_ERR_ARG, "precision must be 32 or 64");
+    if (p->replay_words || p->replay_offsets || p->log)
+        return fail(MC_ERR_UNSUPPORTED, "mc_solve_noalloc: replay streams and trajectory logs are not supported; use mc_solve");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    void* scratch = nullptr;
+    rc = noallocScratch(&scratch);
+    if (rc) return rc;
+    mc_session_s S;
+    S.mat = m; S.dom = d; S.desc = *p;
+    S.desc.schedule = MC_SCHED_DYNAMIC;
+    S.desc.compact_interval = 0;
+    S.prec = p->precision;
+    S.dyn = true;
+    S.maxloop = p->maxloop != 0 ? p->maxloop : 100 * p->maxscat;
+    S.stream = (cudaStream_t)p->stream;
+    const bool f32 = S.prec == 32;
+    rc = f32 ? placeSession<float>(&S, (char*)scratch, MC_NOALLOC_SCRATCH_BYTES)
+             : placeSession<double>(&S, (char*)scratch, MC_NOALLOC_SCRATCH_BYTES);
+    if (!rc) rc = f32 ? emitT<float>(&S) : emitT<double>(&S);
+    int done = 0;
+    while (!rc && !done) rc = f32 ? advanceT<float>(&S, 64, &done) : advanceT<double>(&S, 64, &done);
+    if (!rc) return resultImpl(&S, out, st);
+    // no launch of this call may still write the array after it returns
+    std::string msg = g_err;
+    cudaStreamSynchronize(S.stream);
     g_err = msg;
     return rc;
 }
