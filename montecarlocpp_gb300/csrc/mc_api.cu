@@ -897,6 +897,10 @@ struct mc_batch_s {
     unsigned int* status = nullptr;
     long long cap = 0;
     int block = 256, grid = 0;
+    SegD* segs = nullptr;           // work segments of the advance launches
+    int* home = nullptr;            // first segment of each block
+    unsigned long long* segNext = nullptr;
+    int nseg = 0;
     cudaStream_t stream = nullptr;
     bool ownStream = false;
     cudaGraphExec_t exec = nullptr;
@@ -907,13 +911,79 @@ struct mc_batch_s {
 
 namespace {
 
+// Work segments of a batched advance: instance i's slots split into its
+// field copies (groupedId's layout), then each of `grid` blocks given a
+// first segment in proportion to the segments' slots.
+void planSegments(const std::vector<long long>& slot0, const std::vector<long>& nemit,
+                  const std::vector<int>& groups, int grid, std::vector<SegD>& segs, std::vector<int>& home) {
+    segs.clear();
+    for (size_t i = 0; i < slot0.size(); ++i) {
+        const long long n = nemit[i];
+        const int G = std::max(1, groups[i]);
+        const long long q = n / G, rem = n % G;
+        long long off = 0;
+        for (int g = 0; g < G; ++g) {
+            const long long sz = q + (g < rem ? 1 : 0);
+            if (sz > 0) segs.push_back(SegD{slot0[i] + off, slot0[i] + off + sz, (int)i, g});
+            off += sz;
+        }
+    }
+    long long total = 0;
+    for (const SegD& g : segs) total += g.end - g.beg;
+    home.assign((size_t)std::max(grid, 1), 0);
+    size_t k = 0;
+    long long before = 0;
+    for (int b = 0; b < grid && !segs.empty(); ++b) {
+        const double pos = ((double)b + 0.5) / (double)grid * (double)total;
+        while (k + 1 < segs.size() && (double)(before + (segs[k].end - segs[k].beg)) <= pos) {
+            before += segs[k].end - segs[k].beg;
+            ++k;
+        }
+        home[b] = (int)k;
+    }
+}
+
+// What a batched block stages per instance (InstD::flags) and the launch's
+// shared-memory capacities: fixed-point fields up to TAL_BATCH_MAX bytes,
+// subdomain images while the block stays within BATCH_SMEM_F32 (twice that
+// in FP64). `inst` must hold nw, np, nsd, rows and cols.
+template <typename R>
+int batchCaps(std::vector<InstD<R>>& inst, Params<R>& P) {
+    int bNt = 0, bNw = 0, bTal = 0;
+    for (auto& I : inst) {
+        bNt = std::max(bNt, I.nw * I.np);
+        bNw = std::max(bNw, I.nw);
+        const size_t talE = (size_t)I.rows * (2 * (size_t)I.cols + 1);
+        I.flags = 0;
+        if (talE * sizeof(long long) <= TAL_BATCH_MAX) {
+            I.flags |= IF_TAL_SHARED;
+            bTal = std::max(bTal, (int)talE);
+        }
+    }
+    BatchSmem L;
+    L.init<R>(bNt, bNw, 0, bTal);
+    const size_t limit = sizeof(R) == 4 ? BATCH_SMEM_F32 : 2 * BATCH_SMEM_F32;
+    const size_t budget = L.total < limit ? limit - L.total : 0;
+    int bSd = 0;
+    for (auto& I : inst) {
+        const size_t sdB = sizeof(SdomD<R>) * (size_t)I.nsd;
+        if (sdB <= budget && sdB <= SD_SHARED_MAX) {
+            I.flags |= IF_SD_SHARED;
+            bSd = std::max(bSd, (int)sdB);
+        }
+    }
+    P.bNt = bNt; P.bNw = bNw; P.bTal = bTal; P.bSdBytes = bSd;
+    if (batchSmemBytes<R>(P) > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "batched shared-memory tables exceed 227 KB");
+    return MC_OK;
+}
+
 void freeBatch(mc_batch_s* B) {
     if (!B) return;
     for (void* p : B->tables) if (p) cudaFree(p);
     for (void* p : B->sd) if (p) cudaFree(p);
     for (auto* p : B->em) if (p) cudaFree(p);
     for (auto* p : B->cdf) if (p) cudaFree(p);
-    void* ps[] = {B->fields, B->insts, B->islot, B->state, B->cnt, B->status};
+    void* ps[] = {B->fields, B->insts, B->islot, B->state, B->cnt, B->status, B->segs, B->home, B->segNext};
     for (void* p : ps) if (p) cudaFree(p);
     if (B->exec) cudaGraphExecDestroy(B->exec);
     if (B->ownStream && B->stream) cudaStreamDestroy(B->stream);
@@ -976,9 +1046,10 @@ int setupBatch(mc_batch_s* B) {
         I.csum = f + (size_t)I.rows * I.cols + (size_t)I.rows * (I.cols + 1);
         I.groups = 1;
         I.gstride = 0;
+        // a block's shared field takes at most the instance's phonons
         for (int r = 0; r < 4; ++r) {
             const bool timeRow = (pd.problem == MC_TEMP || pd.problem == MC_MULTI) && r == 0;
-            const double q = std::ldexp(window * (timeRow ? 1.0 : vmax) * 1.0001, -61);
+            const double q = std::ldexp((double)B->nemit[i] * window * (timeRow ? 1.0 : vmax) * 1.0001, -61);
             I.tq[r] = q;
             I.tqinv[r] = (R)(1.0 / q);
         }
@@ -986,6 +1057,14 @@ int setupBatch(mc_batch_s* B) {
         if (pd.problem < MC_TEMP || pd.problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
     }
     B->cap = islot[n];
+    Params<R>& P = batchParams<R>(B);
+    P = Params<R>{};
+    {
+        int rc = batchCaps<R>(inst, P);
+        if (rc) return rc;
+        for (auto& I : inst)
+            if (I.flags & IF_TAL_SHARED) I.gdif = nullptr;
+    }
     CK(cudaMalloc(&B->insts, sizeof(InstD<R>) * n));
     CK(cudaMemcpy(B->insts, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice));
     CK(cudaMalloc(&B->islot, sizeof(long long) * (n + 1)));
@@ -997,8 +1076,6 @@ int setupBatch(mc_batch_s* B) {
     B->stateBytes = (2 * sizeof(V4) + sizeof(uint4)) * cap;
     CK(cudaMalloc(&B->state, 2 * al(sizeof(V4) * cap) + al(sizeof(uint4) * cap)));
     char* sb = (char*)B->state;
-    Params<R>& P = batchParams<R>(B);
-    P = Params<R>{};
     P.P0in = P.P0out = (V4*)sb; sb += al(sizeof(V4) * cap);
     P.P1in = P.P1out = (V4*)sb; sb += al(sizeof(V4) * cap);
     P.P2in = P.P2out = (uint4*)sb;
@@ -1016,15 +1093,28 @@ int setupBatch(mc_batch_s* B) {
     P.islot = B->islot;
     P.ninst = n;
     P.maxGroups = 1;
-    if (batchSmemBytes<R>(n) > 200 * 1024) return fail(MC_ERR_UNSUPPORTED, "too many instances in one batch");
     B->block = B->bd.block_size > 0 ? B->bd.block_size : 256;
     if (B->block % 32 || B->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int occ = advanceBatchOccupancy<R>(n, B->block);
+    const int occ = advanceBatchOccupancy<R>(batchSmemBytes<R>(P), B->block);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
     B->grid = B->bd.grid_blocks > 0 ? B->bd.grid_blocks : occ * nsm;
+    std::vector<SegD> segs;
+    std::vector<int> home;
+    std::vector<long long> slot0(islot.begin(), islot.end() - 1);
+    planSegments(slot0, B->nemit, std::vector<int>(n, 1), B->grid, segs, home);
+    B->nseg = (int)segs.size();
+    CK(cudaMalloc(&B->segs, sizeof(SegD) * std::max<size_t>(segs.size(), 1)));
+    CK(cudaMalloc(&B->home, sizeof(int) * home.size()));
+    CK(cudaMalloc(&B->segNext, sizeof(unsigned long long) * std::max<size_t>(segs.size(), 1)));
+    if (!segs.empty()) CK(cudaMemcpy(B->segs, segs.data(), sizeof(SegD) * segs.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B->home, home.data(), sizeof(int) * home.size(), cudaMemcpyHostToDevice));
+    P.segs = B->segs;
+    P.home = B->home;
+    P.segNext = B->segNext;
+    P.nseg = B->nseg;
     return MC_OK;
 }
 
@@ -1041,6 +1131,7 @@ int enqueueBatch(mc_batch_s* B) {
     for (int step = 0; step < (int)B->bd.nsteps; step += P.ksteps) {
         P.step0 = step;
         CK(cudaMemsetAsync(B->cnt + C_NCOUNTERS + 1, 0, sizeof(unsigned long long), B->stream));
+        CK(cudaMemsetAsync(B->segNext, 0, sizeof(unsigned long long) * std::max(B->nseg, 1), B->stream));
         CK(launchAdvanceBatch<R>(P, B->grid, B->block, B->stream));
         ++launches;
     }
@@ -1158,8 +1249,11 @@ struct ServerT : ServerBase {
     long long* islot_d = nullptr;
     double** accs_d = nullptr;
     double* gsum_d = nullptr;
+    SegD* segs_d = nullptr;
+    int* home_d = nullptr;
+    unsigned long long* segNext_d = nullptr;
     cudaStream_t stream = nullptr;
-    int block = 256, grid = 0;
+    int block = 256, nsm = 0;
     Params<R> base{};
 
     int init() {
@@ -1182,6 +1276,8 @@ struct ServerT : ServerBase {
         CK(cudaMalloc(&islot_d, sizeof(long long) * (d.max_active + 1)));
         CK(cudaMalloc(&accs_d, sizeof(double*) * d.max_active));
         CK(cudaMalloc(&gsum_d, sizeof(double) * d.max_active * MAX_GROUPS * 4));
+        CK(cudaMalloc(&segs_d, sizeof(SegD) * d.max_active * MAX_GROUPS));
+        CK(cudaMalloc(&segNext_d, sizeof(unsigned long long) * d.max_active * MAX_GROUPS));
         base.counters = cnt;
         base.status = status;
         base.live_in = cnt + C_NCOUNTERS;
@@ -1194,16 +1290,14 @@ struct ServerT : ServerBase {
         base.maxGroups = d.groups;
         block = d.block_size > 0 ? d.block_size : 256;
         if (block % 32 || block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
-        int nsm = 0;
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        const int occ = advanceBatchOccupancy<R>(d.max_active, block);
-        if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
-        grid = occ * nsm;
+        // at most 2048 / 32 blocks of a warp or more per SM
+        CK(cudaMalloc(&home_d, sizeof(int) * (size_t)nsm * 64));
         return MC_OK;
     }
 
     ~ServerT() override {
-        void* ps[] = {state, cnt, status, insts_d, islot_d, accs_d, gsum_d};
+        void* ps[] = {state, cnt, status, insts_d, islot_d, accs_d, gsum_d, segs_d, home_d, segNext_d};
         for (void* p : ps) if (p) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -1246,9 +1340,11 @@ struct ServerT : ServerBase {
         I.groups = d.groups;
         I.gstride = (long long)gstride;
         const double window = (double)d.nsteps * d.dt;
+        // a block's shared field takes at most one field copy's phonons
+        const double perCopy = (double)((j->nemit + d.groups - 1) / d.groups);
         for (int r = 0; r < 4; ++r) {
             const bool timeRow = j->req.problem == MC_MULTI && r == 0;
-            const double q = std::ldexp(window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
+            const double q = std::ldexp(perCopy * window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
             I.tq[r] = q;
             I.tqinv[r] = (R)(1.0 / q);
         }
@@ -1275,13 +1371,36 @@ struct ServerT : ServerBase {
             const size_t gstride = (size_t)inst[i].gstride;
             CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * (gstride * d.groups + 4), stream));
         }
+        Params<R> P = base;
+        {
+            int rc = batchCaps<R>(inst, P);
+            if (rc) return rc;
+            for (auto& I : inst)
+                if (I.flags & IF_TAL_SHARED) I.gdif = nullptr;
+        }
+        const int occ = advanceBatchOccupancy<R>(batchSmemBytes<R>(P), block);
+        if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
+        const int grid = std::min(occ, 64) * nsm;
+        std::vector<SegD> segs;
+        std::vector<int> home;
+        std::vector<long long> slot0(islot.begin(), islot.end() - 1);
+        std::vector<long> nem(n);
+        for (int i = 0; i < n; ++i) nem[i] = active[i]->nemit;
+        planSegments(slot0, nem, std::vector<int>(n, d.groups), grid, segs, home);
+        if (!segs.empty())
+            CK(cudaMemcpyAsync(segs_d, segs.data(), sizeof(SegD) * segs.size(), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(home_d, home.data(), sizeof(int) * home.size(), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(segNext_d, 0, sizeof(unsigned long long) * std::max<size_t>(segs.size(), 1), stream));
+        P.segs = segs_d;
+        P.home = home_d;
+        P.segNext = segNext_d;
+        P.nseg = (int)segs.size();
         CK(cudaMemcpyAsync(insts_d, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(islot_d, islot.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(accs_d, accs.data(), sizeof(double*) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemsetAsync(gsum_d, 0, sizeof(double) * n * MAX_GROUPS * 4, stream));
         CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), stream));
         CK(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
-        Params<R> P = base;
         P.cap = (unsigned long long)islot[n];
         P.ninst = n;
         P.step0 = 0;

@@ -48,6 +48,16 @@ template <> struct Lim<double> {
 // ------------------------------------------------------------------ params
 template <typename R> struct InstD;
 
+// A work segment of a batched advance: the slots [beg, end) of one
+// instance whose phonons all add to one field copy (batch-mean group).
+struct SegD {
+    long long beg, end;
+    int inst, group;
+};
+
+// InstD::flags
+enum { IF_TAL_SHARED = 1, IF_SD_SHARED = 2 };
+
 template <typename R>
 struct Params {
     const SdomD<R>* sd;
@@ -102,6 +112,16 @@ struct Params {
     const long long* islot;
     int ninst;
     int maxGroups;  // largest field-copy count of the instances
+    // work segments of a batched advance: each block starts on segment
+    // home[block] and moves on to any segment with slots left; segNext[s]
+    // counts the slots of segment s already claimed
+    const SegD* segs;
+    const int* home;
+    unsigned long long* segNext;
+    int nseg;
+    // shared-memory capacities of a batched block (largest instance that
+    // stages its tables / subdomains / fixed-point field there)
+    int bNt, bNw, bSdBytes, bTal;
 };
 
 // One problem instance as the advance loop sees it: material tables,
@@ -131,7 +151,7 @@ struct InstD {
     double* gdif;                     // global difference array, rows x (cols + 1), or null
     double* csum;                     // per-row checksum
     int groups;                       // phonon id % groups picks a field copy
-    int pad2;
+    int flags;                        // IF_*: what a batched block stages
     long long gstride;                // doubles between field copies (tally and gdif)
     R tqinv[4];
     double tq[4];

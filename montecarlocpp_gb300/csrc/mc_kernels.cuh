@@ -153,14 +153,33 @@ __device__ __forceinline__ int instanceOf(const long long* islot, int ninst, lon
     return lo < ninst ? lo : ninst - 1;
 }
 
+// Phonon id of slot `local` of an instance whose n phonons are split into
+// G field copies stored one after the other: copy g holds the ids equal to
+// g mod G (the first n % G copies one more than the others), so that every
+// copy samples all emitters alike.
+__host__ __device__ __forceinline__ long long groupedId(long long local, long long n, int G) {
+    if (G <= 1) return local;
+    const long long q = n / G, rem = n % G;
+    long long g, j;
+    if (local < rem * (q + 1)) {
+        g = local / (q + 1);
+        j = local - g * (q + 1);
+    } else {
+        const long long t = local - rem * (q + 1);
+        g = rem + t / q;
+        j = t - (g - rem) * q;
+    }
+    return j * G + g;
+}
+
 // Emission of every instance of a batch: slot n belongs to the instance whose
-// slot range holds it; its phonon id is n - slot0.
+// slot range holds it; its phonon id follows from the slot by groupedId.
 template <typename R>
 __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= (long long)P.cap) return;
     const InstD<R>& I = P.insts[instanceOf(P.islot, P.ninst, n)];
-    const long long id = n - I.slot0;
+    const long long id = groupedId(n - I.slot0, I.nemit, I.groups);
     Rng<false> g;
     g.init(I.key0, I.key1, (uint32_t)id, &P);
     Phn<R> ph;
@@ -230,23 +249,21 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     closeBlock<R, TM>(P, *I, C, csum);
 }
 
-// Dynamic schedule shared by the single-instance and batched kernels: block
-// b owns slots [b C, (b + 1) C) of [0, n); each warp keeps its lanes busy by
-// refilling finished lanes from the block's queue whenever at least REFILL
+// Dynamic schedule shared by the single-instance and batched kernels: the
+// warps of a block take slots of [qbeg, qend) from the counter *qnext
+// (shared for a block's own chunk, global for a batched segment); each warp
+// keeps its lanes busy by refilling finished lanes whenever at least REFILL
 // of them are idle, so a long phonon no longer holds up its warp. Survivors
 // are written back in place; dead slots get PROP_DEAD (skipped until the
-// host compacts). `inst(slot)` gives a slot's instance descriptor; BATCH
-// flushes each phonon's checksum to its instance when its window ends.
+// host compacts).
 constexpr int REFILL = 8;
 
-template <typename R, bool REPLAY, bool LOG, int TM, bool BATCH, typename InstOf>
-__device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long n, unsigned long long* qnext,
-                                            InstOf inst, const Window<R>& W, Counts& C, long long csum[4]) {
+template <typename R, bool REPLAY, bool LOG, int TM>
+__device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
+                                            unsigned long long qbeg, unsigned long long qend,
+                                            const InstD<R>* I, const Window<R>& W, Counts& C, long long csum[4]) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
-    const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
-    const unsigned long long qend = min(qbeg + chunk, n);
     Walker<R, REPLAY, LOG, TM> wk;
     bool have = false;
     unsigned long long slot = 0;
@@ -267,10 +284,9 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
                     if (!(A2.y & PROP_DEAD)) {
                         ld4(P.P0in + my, A0);
                         ld4(P.P1in + my, A1);
-                        wk.load(P, inst(my), W, A0, A1, A2);
+                        wk.load(P, I, W, A0, A1, A2);
                         have = true;
                         slot = my;
-                        if (BATCH) csum[0] = csum[1] = csum[2] = csum[3] = 0;
                     }
                 }
             }
@@ -280,11 +296,6 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
             continue;
         }
         if (have && wk.iterate(P, W, C, csum)) {
-            if (BATCH) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    if (r < wk.I->rows && csum[r]) atomicAdd(&wk.I->csum[r], (double)csum[r] * wk.I->tq[r]);
-            }
             typename Vec4<R>::T A0, A1;
             uint4 A2;
             if (wk.finish(P, W, C)) {
@@ -307,22 +318,7 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
     if (lane == 0 && x) atomicAdd(&P.live_out[0], x);
 }
 
-template <typename R>
-struct SingleInst {
-    const InstD<R>* I;
-    __device__ __forceinline__ const InstD<R>* operator()(unsigned long long) const { return I; }
-};
-
-template <typename R>
-struct BatchInst {
-    const InstD<R>* sI;
-    const long long* sSlot;
-    int ninst;
-    __device__ __forceinline__ const InstD<R>* operator()(unsigned long long slot) const {
-        return &sI[instanceOf(sSlot, ninst, (long long)slot)];
-    }
-};
-
+// Block b owns the live slots [b C, (b + 1) C) of the launch.
 template <typename R, bool REPLAY, bool LOG, int TM>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -334,42 +330,158 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     W.init(P);
     long long csum[4] = {0, 0, 0, 0};
     Counts C;
-    dynamicLoop<R, REPLAY, LOG, TM, false>(P, P.live_in[0], &qnext, SingleInst<R>{I}, W, C, csum);
+    const unsigned long long n = P.live_in[0];
+    const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
+    const unsigned long long qend = min(qbeg + chunk, n);
+    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, I, W, C, csum);
     closeBlock<R, TM>(P, *I, C, csum);
 }
 
-// Batched kernel: the dynamic schedule over the slots of many instances at
-// once (slots [islot[i], islot[i+1]) belong to instance i). Each lane runs
-// its phonon against its instance's tables, domain and field. Fields are
-// FP64 global atomics with global difference arrays (k_difprefix finishes
-// them).
+// The current instance of a batched block, staged in shared memory: its
+// descriptor, velocity and scatter tables, and (flags permitting) its
+// subdomain images and a zeroed fixed-point field with difference array.
+template <typename R>
+__device__ __forceinline__ void stageInstance(const Params<R>& P, int inst, unsigned char* smraw,
+                                              const BatchSmem& L) {
+    const InstD<R>& G = P.insts[inst];
+    InstD<R>* I = reinterpret_cast<InstD<R>*>(smraw + L.inst);
+    R* vel = reinterpret_cast<R*>(smraw + L.vel);
+    R* vt = reinterpret_cast<R*>(smraw + L.vt);
+    unsigned long long* wthr = reinterpret_cast<unsigned long long*>(smraw + L.wthr);
+    uint16_t* wguide = reinterpret_cast<uint16_t*>(smraw + L.guide);
+    long long* tal = reinterpret_cast<long long*>(smraw + L.tal);
+    const int nt = G.nw * G.np;
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        vel[i] = G.vel[i];
+        vt[i] = G.vt[i];
+    }
+    for (int i = threadIdx.x; i < G.nw; i += blockDim.x) wthr[i] = G.wthr[i];
+    for (int i = threadIdx.x; i < GUIDE; i += blockDim.x) wguide[i] = G.wguide[i];
+    const bool sdS = (G.flags & IF_SD_SHARED) != 0;
+    if (sdS) {
+        const int nw4 = (int)(sizeof(SdomD<R>) * (size_t)G.nsd / 4);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smraw + L.sd);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(G.sd);
+        for (int i = threadIdx.x; i < nw4; i += blockDim.x) dst[i] = src[i];
+    }
+    const bool talS = (G.flags & IF_TAL_SHARED) != 0;
+    if (talS) {
+        const int nz = G.rows * (2 * G.cols + 1);
+        for (int i = threadIdx.x; i < nz; i += blockDim.x) tal[i] = 0;
+    }
+    if (threadIdx.x == 0) {
+        *I = G;
+        I->vel = vel; I->vt = vt; I->wthr = wthr; I->wguide = wguide;
+        if (sdS) I->sd = reinterpret_cast<const SdomD<R>*>(smraw + L.sd);
+        I->tal = talS ? tal : nullptr;
+        I->dif = talS ? tal + (size_t)G.rows * G.cols : nullptr;
+    }
+}
+
+// End of a batched block's binding to (instance, group): checksums (one
+// atomic per warp and row), then the shared field, if any, turned from
+// difference form into cells, flushed into field copy `group` as FP64
+// atomics and cleared. Called by all threads after the binding's barrier.
+template <typename R>
+__device__ __forceinline__ void flushBinding(const InstD<R>& I, int group, long long csum[4]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        long long x = csum[r];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+        if (lane == 0 && r < I.rows && x != 0) atomicAdd(&I.csum[r], (double)x * I.tq[r]);
+        csum[r] = 0;
+    }
+    if (I.tal == nullptr) return;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int r = warp; r < I.rows; r += nwarps) {
+        long long carry = 0;
+        long long* dr = I.dif + r * (I.cols + 1);
+        for (int c0 = 0; c0 < I.cols; c0 += 32) {
+            const int c = c0 + lane;
+            long long x = c < I.cols ? dr[c] : 0;
+            if (c < I.cols) dr[c] = 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            x += carry;
+            if (c < I.cols) I.tal[r * I.cols + c] += x;
+            carry = __shfl_sync(0xFFFFFFFFu, x, 31);
+        }
+        if (lane == 0) dr[I.cols] = 0;
+    }
+    __syncthreads();
+    const int tot = I.rows * I.cols;
+    double* dst = I.tally + (long long)group * I.gstride;
+    for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+        const long long x = I.tal[q];
+        if (x != 0) {
+            const int r = q / I.cols, c = q - r * I.cols;
+            atomicAdd(&dst[(size_t)c * I.rows + r], (double)x * I.tq[r]);
+            I.tal[q] = 0;
+        }
+    }
+}
+
+// Batched kernel: every block binds to one work segment at a time (one
+// instance, one field copy), stages that instance in shared memory and runs
+// the dynamic schedule over the segment's slots together with every other
+// block bound to it; when the segment has no slots left the block flushes
+// its field and moves on to the next segment with work, so that a few
+// expensive instances end up spread over the whole GPU. A block starts on
+// segment home[block] (the host spreads blocks over segments by size).
 template <typename R>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_batch(Params<R> P) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ unsigned long long qnext;
-    InstD<R>* sI = reinterpret_cast<InstD<R>*>(smraw);
-    long long* sSlot = reinterpret_cast<long long*>(smraw + sizeof(InstD<R>) * P.ninst);
-    {
-        const int nw4 = (int)(sizeof(InstD<R>) * P.ninst / 4);
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(P.insts);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(sI);
-        for (int i = threadIdx.x; i < nw4; i += blockDim.x) dst[i] = src[i];
-        for (int i = threadIdx.x; i <= P.ninst; i += blockDim.x) sSlot[i] = P.islot[i];
-    }
-    if (threadIdx.x == 0) qnext = 0;
-    __syncthreads();
+    __shared__ int sSeg;
+    BatchSmem L;
+    L.init<R>(P.bNt, P.bNw, P.bSdBytes, P.bTal);
+    const InstD<R>* I = reinterpret_cast<const InstD<R>*>(smraw + L.inst);
     Window<R> W;
     W.init(P);
     long long csum[4] = {0, 0, 0, 0};
     Counts C;
-    dynamicLoop<R, false, false, TM_GLOBAL, true>(P, P.cap, &qnext, BatchInst<R>{sI, sSlot, P.ninst}, W, C, csum);
+    int cur = P.home[blockIdx.x];
+    int curInst = -1;
+    for (int bind = 0; bind < (1 << 30); ++bind) {
+        if (threadIdx.x == 0) {
+            int pick = -1;
+            for (int k = 0; k < P.nseg; ++k) {
+                int sg = cur + k;
+                if (sg >= P.nseg) sg -= P.nseg;
+                const SegD& G = P.segs[sg];
+                const unsigned long long taken = *reinterpret_cast<volatile unsigned long long*>(P.segNext + sg);
+                if (taken < (unsigned long long)(G.end - G.beg)) { pick = sg; break; }
+            }
+            sSeg = pick;
+        }
+        __syncthreads();
+        const int sg = sSeg;
+        if (sg < 0) break;
+        cur = sg;
+        const SegD S = P.segs[sg];
+        if (S.inst != curInst) {
+            stageInstance<R>(P, S.inst, smraw, L);
+            curInst = S.inst;
+        }
+        __syncthreads();
+        dynamicLoop<R, false, false, TM_AUTO>(P, P.segNext + sg, (unsigned long long)S.beg,
+                                              (unsigned long long)S.end, I, W, C, csum);
+        __syncthreads();
+        flushBinding<R>(*I, S.group, csum);
+        __syncthreads();
+    }
     flushCounts(P.counters, C);
 }
 
 // Shared memory of the batched kernel.
 template <typename R>
-__host__ __device__ inline size_t batchSmemBytes(int ninst) {
-    return sizeof(InstD<R>) * (size_t)ninst + sizeof(long long) * ((size_t)ninst + 1);
+__host__ __device__ inline size_t batchSmemBytes(const Params<R>& P) {
+    BatchSmem L;
+    L.init<R>(P.bNt, P.bNw, P.bSdBytes, P.bTal);
+    return L.total;
 }
 
 // Global difference arrays -> field: block (i, y) prefix-sums row y % 4 of

@@ -27,7 +27,7 @@ cudaError_t launchAdvanceBatch(const Params<R>& p, int grid, int block, cudaStre
 template <typename R>
 cudaError_t launchDifPrefix(const Params<R>& p, cudaStream_t s);
 template <typename R>
-int advanceBatchOccupancy(int ninst, int block);
+int advanceBatchOccupancy(size_t smem, int block);
 template <typename R>
 cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
                               cudaStream_t s);

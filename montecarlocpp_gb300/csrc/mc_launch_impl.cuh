@@ -56,7 +56,7 @@ cudaError_t launchEmitBatch<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
 
 template <>
 cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int grid, int block, cudaStream_t s) {
-    const size_t smem = batchSmemBytes<MC_REAL>(p.ninst);
+    const size_t smem = batchSmemBytes<MC_REAL>(p);
     cudaError_t e = prepare(k_advance_batch<MC_REAL>, smem);
     if (e != cudaSuccess) return e;
     k_advance_batch<MC_REAL><<<grid, block, smem, s>>>(p);
@@ -77,8 +77,7 @@ cudaError_t launchRoundReduce<MC_REAL>(const Params<MC_REAL>& p, double* const* 
 }
 
 template <>
-int advanceBatchOccupancy<MC_REAL>(int ninst, int block) {
-    const size_t smem = batchSmemBytes<MC_REAL>(ninst);
+int advanceBatchOccupancy<MC_REAL>(size_t smem, int block) {
     if (prepare(k_advance_batch<MC_REAL>, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_advance_batch<MC_REAL>, block, smem) != cudaSuccess)

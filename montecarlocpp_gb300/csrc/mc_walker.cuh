@@ -31,15 +31,41 @@ struct SmemLayout {
 // Subdomain images staged in shared memory up to this many bytes.
 constexpr size_t SD_SHARED_MAX = 32 * 1024;
 
+// Shared memory of a batched block: the current instance's descriptor and
+// tables, and room for the largest subdomain images and fixed-point field
+// that any instance of the launch stages.
+struct BatchSmem {
+    size_t inst = 0, vel = 0, vt = 0, wthr = 0, guide = 0, sd = 0, tal = 0, total = 0;
+    template <typename R>
+    __host__ __device__ void init(int nt, int nw, int sdBytes, int talEntries) {
+        auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+        inst = 0;
+        vel = al(sizeof(InstD<R>));
+        vt = al(vel + sizeof(R) * (size_t)nt);
+        wthr = al(vt + sizeof(R) * (size_t)nt);
+        guide = al(wthr + sizeof(unsigned long long) * (size_t)nw);
+        sd = al(guide + sizeof(uint16_t) * GUIDE);
+        tal = al(sd + (size_t)sdBytes);
+        total = tal + sizeof(long long) * (size_t)talEntries;
+    }
+};
+
+// Fixed-point fields a batched block keeps in shared memory up to this size
+// (larger ones go straight to the global field).
+constexpr size_t TAL_BATCH_MAX = 32 * 1024;
+// Shared memory a batched FP32 block may use with subdomains staged (four
+// resident blocks per SM); FP64 blocks (two per SM) may use twice this.
+constexpr size_t BATCH_SMEM_F32 = 56 * 1024;
+
 __host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
     return sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1);
 }
 
 // Tally modes: per-block shared histogram (64-bit fixed point, exact and
 // order-independent adds) flushed with FP64 atomics, or FP64 atomics
-// straight to the global field (fields too large for shared memory, and
-// batched launches).
-enum { TM_SHARED = 0, TM_GLOBAL = 1 };
+// straight to the global field (fields too large for shared memory), or
+// either per instance (batched launches: shared when InstD::tal is set).
+enum { TM_SHARED = 0, TM_GLOBAL = 1, TM_AUTO = 2 };
 
 // Hard cap on events one thread processes in one launch (a guard: a
 // phonon that reaches it is killed and flagged non-finite).
@@ -98,6 +124,9 @@ struct Tally {
     R rho[4];
 
     __device__ __forceinline__ int rows() const { return I->rows; }
+    __device__ __forceinline__ bool shared() const {
+        return TM == TM_SHARED || (TM == TM_AUTO && I->tal != nullptr);
+    }
     // fixed-point amount of row r for path length t
     __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * I->tqinv[r])); }
     __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
@@ -179,7 +208,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
         if (r >= T.rows()) break;
         const long long V = T.fixedOf(r, s);
         csum[r] += V;
-        if (TM == TM_SHARED) {
+        if (T.shared()) {
             if (e == b) {
                 T.atomShared(r, cb + b * stride, V);
             } else {
@@ -192,7 +221,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
             }
         }
     }
-    if (TM == TM_GLOBAL) {
+    if (!T.shared()) {
         if (e == b) {
             T.addGlobal(cb + b * stride, s);
         } else {
@@ -225,9 +254,9 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
             if (r >= T.rows()) break;
             const long long V = T.fixedOf(r, s);
             csum[r] += V;
-            if (acc == -1 && TM == TM_SHARED) T.atomShared(r, cb, V);
+            if (acc == -1 && T.shared()) T.atomShared(r, cb, V);
         }
-        if (acc == -1 && TM == TM_GLOBAL) T.addGlobal(cb, s);
+        if (acc == -1 && !T.shared()) T.addGlobal(cb, s);
 #pragma unroll
         for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
         return;
@@ -253,7 +282,7 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         }
         tmin = fmax(tmin, R(0));
         const int col = cb + ph.idx[0] * S.tstride[0] + ph.idx[1] * s0 + ph.idx[2] * s01;
-        if (TM == TM_SHARED) {
+        if (T.shared()) {
 #pragma unroll
             for (int r = 0; r < 4; ++r)
                 if (r < T.rows()) T.atomShared(r, col, T.fixedOf(r, tmin));
