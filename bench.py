@@ -395,11 +395,12 @@ def bench_batched(stream, reps=2, plain=True):
     return out
 
 
-def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budget_gb=64.0):
+def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budget_gb=8.0):
     """Config 4: Poisson requests (film or pore cell, size log-U(20 nm, 2 um),
-    T U(100, 400 K), phonons per round log-U(1e4, 1e7)) submitted at their
+    T U(100, 400 K), first-round phonons log-U(1e4, 1e7)) submitted at their
     arrival times to the serving loop; each solve runs until kappa has a 1%
-    standard error. Reports completed solves/s and p50/p99 latency."""
+    standard error (kappa-only requests: no per-cell field). Reports
+    completed solves/s and p50/p99 latency."""
     import montecarlocpp_gb300 as M
     from montecarlocpp_gb300.workloads import served_requests
     reqs = served_requests(seed, rate, duration)
@@ -423,7 +424,7 @@ def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budg
     for r, (d, vol) in zip(reqs, doms):
         while time.perf_counter() - t0 < r.t_arrival:
             time.sleep(0.0005)
-        tickets.append(srv.submit(mats[round(r.T, 3)], d, r.nemit, seed=len(tickets), volume=vol))
+        tickets.append(srv.submit(mats[round(r.T, 3)], d, r.nemit, seed=len(tickets), volume=vol, field=False))
     deadline = time.perf_counter() + drain
     done = []
     for t in tickets:

@@ -244,12 +244,16 @@ void mc_batch_destroy(mc_batch_h b);
 
 /* ------------------------------------------------------------ serving */
 /* A request loop on a library thread. Submitted solves are admitted against
- * an HBM budget (phonon state in flight at once); every tick advances one
- * round of every admitted solve -- its own Material, Domain, phonon count
- * and Philox key -- in one persistent batched launch, so requests that
- * arrive while others run join the next tick. A round splits its phonons
- * into `groups` batch means; a solve completes when the standard error of
- * kappa = -<q_axis> / gradT_axis is at most target_rel_se of its mean. */
+ * an HBM budget (phonon state of the rounds in flight at once); every tick
+ * advances one round of every admitted solve that fits -- its own
+ * Material, Domain, phonon count and Philox key -- in one persistent
+ * batched launch, so requests that arrive while others run join the next
+ * tick. A round splits its phonons into `groups` batch means; a solve
+ * completes when the standard error of kappa = -<q_axis> / gradT_axis is at
+ * most target_rel_se of its mean. The first round has the requested
+ * phonons; each later round the estimated remainder to the target (at
+ * least the requested count, at most a quarter of the budget), and the
+ * error pools the rounds' batch means weighted by their phonons. */
 typedef struct mc_server_s* mc_server_h;
 
 typedef struct {
@@ -269,12 +273,15 @@ typedef struct {
     mc_material_h mat;      /* kept alive by the caller until completion    */
     mc_domain_h dom;
     int problem;            /* MC_FLUX or MC_MULTI                          */
-    long nemit;             /* phonons per round                            */
+    long nemit;             /* phonons of the first round                   */
     long maxscat, maxloop;
     uint64_t seed;          /* round r uses seed + r                        */
     int axis;               /* flux / gradient axis                         */
     double volume;          /* averaging volume (0: sum of cell volumes)    */
     double gradient;        /* gradT along the axis (0: the first subdomain's) */
+    int field;              /* 1: keep the mean field (returned at the end);
+                               0: kappa only -- flights are not split over
+                               cells, kappa comes from the per-flight sums  */
 } mc_request;
 
 typedef struct {

@@ -69,7 +69,7 @@ class ServerDesc(C.Structure):
 class Request(C.Structure):
     _fields_ = [("mat", C.c_void_p), ("dom", C.c_void_p), ("problem", C.c_int), ("nemit", C.c_long),
                 ("maxscat", C.c_long), ("maxloop", C.c_long), ("seed", C.c_uint64), ("axis", C.c_int),
-                ("volume", C.c_double), ("gradient", C.c_double)]
+                ("volume", C.c_double), ("gradient", C.c_double), ("field", C.c_int)]
 
 
 class Result(C.Structure):

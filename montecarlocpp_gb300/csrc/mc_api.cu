@@ -1188,6 +1188,21 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Phonons per emitter for a requested count (montecarlo/problem.cpp:315-342,
+// as in uploadDomain): cumulative counts into cdf, returns the total.
+long long allocEmitters(const std::vector<double>& w, long nemitReq, std::vector<long long>& cdf) {
+    double wsum = 0.;
+    for (double x : w) wsum += x;
+    cdf.assign(w.size(), 0);
+    long long tot = 0;
+    for (size_t i = 0; i < w.size(); ++i) {
+        const double rounded = std::ceil(w[i] / wsum * nemitReq - 0.5);
+        tot += std::max(1LL, (long long)rounded);
+        cdf[i] = tot;
+    }
+    return tot;
+}
+
 // One submitted solve.
 struct SrvJob {
     long ticket = 0;
@@ -1198,20 +1213,27 @@ struct SrvJob {
     void* sd = nullptr;
     EmitterD* em = nullptr;
     long long* cdf = nullptr;
-    double* fields = nullptr;  // groups x [tally rows*cols | difference rows*(cols+1)], then 4 checksums
-    double* acc = nullptr;     // running sum of round fields, rows*cols
-    long nemit = 0;
-    double power = 0., vmax = 0.;
+    double* fields = nullptr;  // groups x [tally rows*cols | difference rows*(cols+1)], then groups x 4 checksums
+    double* acc = nullptr;     // running sum of the rounds' fields, rows*cols (field requests)
+    long nemit = 0;            // phonons of the current round
+    long nextReq = 0;          // requested phonons of the next round
+    double wflux = 0.;         // power x phonons of a round: sum of emitter weights x fluxSum / 4
+    double vmax = 0.;
     int rows = 1, cols = 0, fluxRow0 = 0;
     bool oneD = false;
     double grad = 0., volume = 0.;
+    std::vector<double> emW;   // emitter weights
     unsigned char image[512];  // host InstD<R> without the per-tick fields
-    // statistics over the batch-mean samples
-    long rounds = 0, samples = 0;
-    double mean = 0., m2 = 0.;
+    // pooled batch-mean statistics over rounds of unequal size: round r
+    // gives `groups` estimates from N_r / groups phonons each
+    long rounds = 0;
+    double sumN = 0., sumNK = 0., ss = 0., steps = 0.;
+    long dof = 0;
     int status = MC_OK;
     bool done = false;
     std::vector<double> field;  // mean field at completion
+    double kappa() const { return sumN > 0. ? sumNK / sumN : 0.; }
+    double se() const { return dof > 0 && sumN > 0. ? std::sqrt(ss / (double)dof / sumN) : 1e300; }
 };
 
 struct ServerBase {
@@ -1254,6 +1276,7 @@ struct ServerT : ServerBase {
     unsigned long long* segNext_d = nullptr;
     cudaStream_t stream = nullptr;
     int block = 256, nsm = 0;
+    long maxRound = 0;  // largest round a solve grows to (a server constant)
     Params<R> base{};
 
     int init() {
@@ -1263,6 +1286,7 @@ struct ServerT : ServerBase {
         const size_t per = 2 * sizeof(V4) + sizeof(uint4);
         capacity = (long)(d.hbm_budget / per);
         if (capacity < 1024) return fail(MC_ERR_ARG, "hbm_budget too small");
+        maxRound = std::max(1L, capacity / 4 - 64);  // never above capacity - 64
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
         const size_t cap = (size_t)capacity;
         CK(cudaMalloc(&state, 2 * al(sizeof(V4) * cap) + al(sizeof(uint4) * cap)));
@@ -1302,6 +1326,30 @@ struct ServerT : ServerBase {
         if (stream) cudaStreamDestroy(stream);
     }
 
+    // Size the job's next round at `want` requested phonons: emitter counts,
+    // the instance image's phonon count and fixed-point quanta.
+    int setRound(SrvJob* j, long want) {
+        std::vector<long long> cdf;
+        const long long tot = allocEmitters(j->emW, want, cdf);
+        CK(cudaMemcpyAsync(j->cdf, cdf.data(), sizeof(long long) * cdf.size(), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));  // cdf lives on this stack
+        j->nemit = (long)tot;
+        InstD<R> I;
+        std::memcpy(&I, j->image, sizeof(I));
+        I.nemit = j->nemit;
+        const double window = (double)d.nsteps * d.dt;
+        // a block's shared field takes at most one field copy's phonons
+        const double perCopy = (double)((j->nemit + d.groups - 1) / d.groups);
+        for (int r = 0; r < 4; ++r) {
+            const bool timeRow = j->req.problem == MC_MULTI && r == 0;
+            const double q = std::ldexp(perCopy * window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
+            I.tq[r] = q;
+            I.tqinv[r] = (R)(1.0 / q);
+        }
+        std::memcpy(j->image, &I, sizeof(I));
+        return MC_OK;
+    }
+
     // upload a job's tables and domain, allocate its fields
     int admit(SrvJob* j) {
         const mc_material_s& m = *j->req.mat;
@@ -1309,16 +1357,22 @@ struct ServerT : ServerBase {
         Params<R> P{};
         int rc = uploadMaterial<R>(m, &j->tables, P, j->vmax);
         if (rc) return rc;
-        rc = uploadDomain<R>(D, m.fluxSum, j->req.nemit, &j->sd, &j->em, &j->cdf, P, j->nemit, j->power);
+        double power = 0.;
+        rc = uploadDomain<R>(D, m.fluxSum, j->req.nemit, &j->sd, &j->em, &j->cdf, P, j->nemit, power);
         if (rc) return rc;
+        j->emW = D.emWeight;
+        j->wflux = power * (double)j->nemit;
         j->rows = j->req.problem == MC_FLUX ? 3 : 4;
         j->fluxRow0 = j->req.problem == MC_FLUX ? 0 : 1;
         j->cols = (int)D.cols;
         for (const auto& s : D.sd) j->oneD = j->oneD || (s.accum >= 0 && s.accum <= 2);
         const size_t gstride = (size_t)j->rows * j->cols + (size_t)j->rows * (j->cols + 1);
-        CK(cudaMalloc(&j->fields, sizeof(double) * (gstride * d.groups + 4)));
-        CK(cudaMalloc(&j->acc, sizeof(double) * (size_t)j->rows * j->cols));
-        CK(cudaMemset(j->acc, 0, sizeof(double) * (size_t)j->rows * j->cols));
+        const bool wantField = j->req.field != 0;
+        CK(cudaMalloc(&j->fields, sizeof(double) * (wantField ? gstride * d.groups : 0) + sizeof(double) * 4 * d.groups));
+        if (wantField) {
+            CK(cudaMalloc(&j->acc, sizeof(double) * (size_t)j->rows * j->cols));
+            CK(cudaMemset(j->acc, 0, sizeof(double) * (size_t)j->rows * j->cols));
+        }
         double vol = 0.;
         for (double v : D.cellVol) vol += v;
         j->volume = j->req.volume > 0. ? j->req.volume : vol;
@@ -1330,36 +1384,27 @@ struct ServerT : ServerBase {
         I.fwthr = P.fwthr; I.fpthr = P.fpthr;
         I.sd = P.sd; I.em = P.em; I.emitCdf = P.emitCdf;
         I.nw = P.nw; I.np = P.np; I.nem = P.nem; I.nsd = P.nsd;
-        I.problem = j->req.problem; I.rows = j->rows; I.cols = j->cols;
+        I.problem = j->req.problem; I.rows = j->rows; I.cols = wantField ? j->cols : 0;
         I.maxscat = j->req.maxscat;
         I.maxloop = j->req.maxloop != 0 ? j->req.maxloop : 100 * j->req.maxscat;
-        I.nemit = j->nemit;
-        I.tally = j->fields;
-        I.gdif = j->oneD ? j->fields + (size_t)j->rows * j->cols : nullptr;
-        I.csum = j->fields + gstride * d.groups;
+        I.tally = wantField ? j->fields : nullptr;
+        I.gdif = wantField && j->oneD ? j->fields + (size_t)j->rows * j->cols : nullptr;
+        I.csum = j->fields + (wantField ? gstride * d.groups : 0);
         I.groups = d.groups;
-        I.gstride = (long long)gstride;
-        const double window = (double)d.nsteps * d.dt;
-        // a block's shared field takes at most one field copy's phonons
-        const double perCopy = (double)((j->nemit + d.groups - 1) / d.groups);
-        for (int r = 0; r < 4; ++r) {
-            const bool timeRow = j->req.problem == MC_MULTI && r == 0;
-            const double q = std::ldexp(perCopy * window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
-            I.tq[r] = q;
-            I.tqinv[r] = (R)(1.0 / q);
-        }
+        I.gstride = wantField ? (long long)gstride : 0;
         static_assert(sizeof(InstD<R>) <= sizeof(j->image), "instance image");
         std::memcpy(j->image, &I, sizeof(I));
-        return MC_OK;
+        j->nextReq = j->req.nemit;
+        return setRound(j, j->req.nemit);
     }
 
-    int tick() {
-        const int n = (int)active.size();
+    int tick(const std::vector<SrvJob*>& run) {
+        const int n = (int)run.size();
         std::vector<InstD<R>> inst(n);
         std::vector<long long> islot(n + 1, 0);
         std::vector<double*> accs(n);
         for (int i = 0; i < n; ++i) {
-            SrvJob* j = active[i];
+            SrvJob* j = run[i];
             std::memcpy(&inst[i], j->image, sizeof(InstD<R>));
             inst[i].inst = i;
             inst[i].slot0 = islot[i];
@@ -1368,15 +1413,17 @@ struct ServerT : ServerBase {
             inst[i].key1 = (uint32_t)(seed >> 32);
             islot[i + 1] = islot[i] + j->nemit;
             accs[i] = j->acc;
-            const size_t gstride = (size_t)inst[i].gstride;
-            CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * (gstride * d.groups + 4), stream));
+            const size_t fieldD = (size_t)inst[i].gstride * d.groups + 4 * (size_t)d.groups;
+            CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * fieldD, stream));
         }
         Params<R> P = base;
         {
             int rc = batchCaps<R>(inst, P);
             if (rc) return rc;
-            for (auto& I : inst)
+            for (auto& I : inst) {
                 if (I.flags & IF_TAL_SHARED) I.gdif = nullptr;
+                if (I.tally == nullptr) I.flags |= IF_NO_FIELD;
+            }
         }
         const int occ = advanceBatchOccupancy<R>(batchSmemBytes<R>(P), block);
         if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
@@ -1385,7 +1432,7 @@ struct ServerT : ServerBase {
         std::vector<int> home;
         std::vector<long long> slot0(islot.begin(), islot.end() - 1);
         std::vector<long> nem(n);
-        for (int i = 0; i < n; ++i) nem[i] = active[i]->nemit;
+        for (int i = 0; i < n; ++i) nem[i] = run[i]->nemit;
         planSegments(slot0, nem, std::vector<int>(n, d.groups), grid, segs, home);
         if (!segs.empty())
             CK(cudaMemcpyAsync(segs_d, segs.data(), sizeof(SegD) * segs.size(), cudaMemcpyHostToDevice, stream));
@@ -1398,7 +1445,6 @@ struct ServerT : ServerBase {
         CK(cudaMemcpyAsync(insts_d, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(islot_d, islot.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
         CK(cudaMemcpyAsync(accs_d, accs.data(), sizeof(double*) * n, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemsetAsync(gsum_d, 0, sizeof(double) * n * MAX_GROUPS * 4, stream));
         CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), stream));
         CK(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
         P.cap = (unsigned long long)islot[n];
@@ -1410,54 +1456,78 @@ struct ServerT : ServerBase {
         CK(launchRoundReduce<R>(P, accs_d, gsum_d, stream));
         std::vector<double> gsum((size_t)n * MAX_GROUPS * 4);
         std::vector<unsigned long long> c(C_NCOUNTERS + 4);
+        unsigned int stat = 0;
         CK(cudaMemcpyAsync(gsum.data(), gsum_d, sizeof(double) * gsum.size(), cudaMemcpyDeviceToHost, stream));
         CK(cudaMemcpyAsync(c.data(), cnt, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(&stat, status, sizeof(stat), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
+        if (stat & S_NONFINITE) return fail(MC_ERR_NONFINITE, "non-finite phonon state");
         st.phonon_steps += (double)c[C_PHONON_STEPS];
         const int G = d.groups;
         for (int i = 0; i < n; ++i) {
-            SrvJob* j = active[i];
+            SrvJob* j = run[i];
             j->rounds++;
+            // group g holds N / G phonons: kappa_g = -G power q_g / (V gradT)
+            const double N = (double)j->nemit;
+            double k[MAX_GROUPS], kbar = 0.;
             for (int g = 0; g < G; ++g) {
-                const double q = G * j->power * gsum[((size_t)i * MAX_GROUPS + g) * 4 + j->fluxRow0 + j->req.axis] /
+                const double q = (double)G * (j->wflux / N) * gsum[((size_t)i * MAX_GROUPS + g) * 4 + j->fluxRow0 + j->req.axis] /
                                  j->volume;
-                const double kappa = -q / j->grad;
-                // Welford (montecarlo/field.cpp:323-330)
-                j->samples++;
-                const double dlt = kappa - j->mean;
-                j->mean += dlt / (double)j->samples;
-                j->m2 += dlt * (kappa - j->mean);
+                k[g] = -q / j->grad;
+                kbar += k[g] / (double)G;
             }
+            for (int g = 0; g < G; ++g) j->ss += N / (double)G * (k[g] - kbar) * (k[g] - kbar);
+            j->dof += G - 1;
+            j->sumN += N;
+            j->sumNK += N * kbar;
+            j->steps += N * (double)d.nsteps;
         }
         return MC_OK;
     }
 
     void complete(SrvJob* j, int status) {
         j->status = status;
-        // mean field: (sum of round tallies) / rounds, post-processed
+        // mean field over the rounds' phonons: (power x N) / sum N x sum of
+        // the rounds' tallies, post-processed (montecarlo/problem.cpp:439-444)
         const mc_material_s& m = *j->req.mat;
         const mc_domain_s& D = *j->req.dom;
-        std::vector<double> a((size_t)j->rows * j->cols, 0.);
-        if (j->acc && j->rounds > 0)
+        if (j->acc && j->rounds > 0) {
+            std::vector<double> a((size_t)j->rows * j->cols, 0.);
             cudaMemcpy(a.data(), j->acc, sizeof(double) * a.size(), cudaMemcpyDeviceToHost);
-        j->field.assign(a.size(), 0.);
-        for (int c = 0; c < j->cols; ++c)
-            for (int r = 0; r < j->rows; ++r) {
-                double v = a[(size_t)c * j->rows + r] / std::max(1L, j->rounds);
-                if (j->req.problem == MC_MULTI && r == 0) v /= m.energySum;
-                j->field[(size_t)c * j->rows + r] = j->power * (v / D.cellVol[c]);
-            }
+            j->field.assign(a.size(), 0.);
+            for (int c = 0; c < j->cols; ++c)
+                for (int r = 0; r < j->rows; ++r) {
+                    double v = a[(size_t)c * j->rows + r];
+                    if (j->req.problem == MC_MULTI && r == 0) v /= m.energySum;
+                    j->field[(size_t)c * j->rows + r] = j->wflux / j->sumN * (v / D.cellVol[c]);
+                }
+        }
         freeJobDevice(j);
         j->tDone = now();
+    }
+
+    // Phonons of the job's next round: the estimated remainder to reach the
+    // target error (10% margin), at least the requested round, and at most
+    // the larger of the requested round and a quarter of the budget.
+    long nextRound(const SrvJob* j) const {
+        const double target = d.target_rel_se * std::fabs(j->kappa());
+        const double se = j->se();
+        double need = (double)j->req.nemit;
+        if (target > 0. && se < 1e299) need = j->sumN * ((se / target) * (se / target) * 1.1 - 1.0);
+        need = std::max(need, (double)j->req.nemit);
+        return (long)std::min(need, (double)std::max(maxRound, j->req.nemit));
     }
 
     void loop() override {
         cudaSetDevice(dev);
         for (;;) {
-            std::vector<SrvJob*> toAdmit;
+            std::vector<SrvJob*> toAdmit, run;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 if (stop) break;
+                // admission: the rounds of the admitted solves fit the budget
+                inflight = 0;
+                for (SrvJob* j : active) inflight += j->nemit + 64;
                 while (!pending.empty() && (int)(active.size() + toAdmit.size()) < d.max_active) {
                     SrvJob* j = pending.front();
                     const long need = j->req.nemit + 64;
@@ -1480,7 +1550,6 @@ struct ServerT : ServerBase {
                     j->status = rc;
                     j->done = true;
                     j->tDone = now();
-                    inflight -= j->req.nemit + 64;
                     st.completed++;
                     cvDone.notify_all();
                     continue;
@@ -1489,24 +1558,47 @@ struct ServerT : ServerBase {
                 active.push_back(j);
                 st.admitted++;
             }
+            // this tick: the oldest solves whose rounds fit the state buffer
+            long used = 0;
+            for (SrvJob* j : active) {
+                if (used + j->nemit + 64 > capacity) continue;
+                used += j->nemit + 64;
+                run.push_back(j);
+            }
+            if (run.empty()) continue;
             const double tb = now();
-            int rc = tick();
+            int rc = tick(run);
+            // each solve's next step (outside the lock: setRound copies)
+            std::vector<int> fate(run.size(), 0);  // 0 next round, 1 converged, 2 gave up, 3 error
+            for (size_t i = 0; i < run.size(); ++i) {
+                SrvJob* j = run[i];
+                const bool conv = j->rounds >= d.min_rounds && j->se() <= d.target_rel_se * std::fabs(j->kappa());
+                if (rc) fate[i] = 3;
+                else if (conv) fate[i] = 1;
+                else if (j->rounds >= d.max_rounds) fate[i] = 2;
+                else {
+                    const long want = nextRound(j);
+                    if (want != j->nextReq) {
+                        j->nextReq = want;
+                        if (setRound(j, want)) fate[i] = 3;
+                    }
+                }
+            }
             std::lock_guard<std::mutex> lk(mu);
             st.ticks++;
             st.busy_s += now() - tb;
             std::vector<SrvJob*> keep;
+            size_t ri = 0;
             for (SrvJob* j : active) {
-                const double se = j->samples > 1 ? std::sqrt(j->m2 / (double)(j->samples - 1) / (double)j->samples) : 1e300;
-                const bool conv = j->rounds >= d.min_rounds && se <= d.target_rel_se * std::fabs(j->mean);
-                const bool giveUp = j->rounds >= d.max_rounds;
-                if (rc || conv || giveUp) {
-                    complete(j, rc ? rc : (conv ? MC_OK : MC_ERR_BUSY));
+                const bool ran = ri < run.size() && run[ri] == j;
+                const int f = ran ? fate[ri++] : 0;
+                if (f != 0) {
+                    complete(j, f == 1 ? MC_OK : (f == 2 ? MC_ERR_BUSY : (rc ? rc : MC_ERR_CUDA)));
                     j->done = true;
-                    inflight -= j->req.nemit + 64;
                     st.completed++;
-                } else {
-                    keep.push_back(j);
+                    continue;
                 }
+                keep.push_back(j);
             }
             active.swap(keep);
             cvDone.notify_all();
@@ -1994,11 +2086,11 @@ static int pollLocked(ServerBase* b, long ticket, mc_result* res, double* field)
     if (!j->done) return 0;
     if (res) {
         std::memset(res, 0, sizeof(*res));
-        res->kappa = j->mean;
-        res->kappa_se = j->samples > 1 ? std::sqrt(j->m2 / (double)(j->samples - 1) / (double)j->samples) : 0.;
+        res->kappa = j->kappa();
+        res->kappa_se = j->dof > 0 ? j->se() : 0.;
         res->rounds = j->rounds;
-        res->phonons = j->rounds * j->nemit;
-        res->phonon_steps = (double)j->rounds * (double)j->nemit * (double)b->d.nsteps;
+        res->phonons = (long)j->sumN;
+        res->phonon_steps = j->steps;
         res->t_submit = j->tSubmit;
         res->t_admit = j->tAdmit;
         res->t_done = j->tDone;

@@ -55,8 +55,10 @@ struct SegD {
     int inst, group;
 };
 
-// InstD::flags
-enum { IF_TAL_SHARED = 1, IF_SD_SHARED = 2 };
+// InstD::flags: a batched block stages the fixed-point field / the
+// subdomain images in shared memory; the instance keeps no field (only the
+// per-flight checksums, e.g. for kappa alone)
+enum { IF_TAL_SHARED = 1, IF_SD_SHARED = 2, IF_NO_FIELD = 4 };
 
 template <typename R>
 struct Params {
@@ -149,7 +151,7 @@ struct InstD {
     long long* dif;                   // its difference array
     double* tally;                    // global field, rows x cols column-major
     double* gdif;                     // global difference array, rows x (cols + 1), or null
-    double* csum;                     // per-row checksum
+    double* csum;                     // per-row checksums, 4 per field copy
     int groups;                       // phonon id % groups picks a field copy
     int flags;                        // IF_*: what a batched block stages
     long long gstride;                // doubles between field copies (tally and gdif)

@@ -66,7 +66,7 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         I->tal = TM == TM_SHARED ? tal : nullptr;
         I->dif = TM == TM_SHARED ? tal + (size_t)P.rows * P.cols : nullptr;
         I->tally = P.tally; I->gdif = nullptr; I->csum = P.csum;
-        I->groups = 1; I->gstride = 0;
+        I->groups = 1; I->gstride = 0; I->flags = 0;
         for (int r = 0; r < 4; ++r) { I->tqinv[r] = P.tqinv[r]; I->tq[r] = P.tq[r]; }
     }
     return I;
@@ -390,7 +390,7 @@ __device__ __forceinline__ void flushBinding(const InstD<R>& I, int group, long 
     for (int r = 0; r < 4; ++r) {
         long long x = csum[r];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && r < I.rows && x != 0) atomicAdd(&I.csum[r], (double)x * I.tq[r]);
+        if (lane == 0 && r < I.rows && x != 0) atomicAdd(&I.csum[4 * group + r], (double)x * I.tq[r]);
         csum[r] = 0;
     }
     if (I.tal == nullptr) return;
@@ -508,46 +508,27 @@ __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
     }
 }
 
-// End of a served round, block (x, i): over instance i's field copies,
-// acc += sum of the copies, and gsum[i][g][r] = sum over cells of row r of
-// copy g (the batch-mean samples), one atomic per warp and (g, r).
+// End of a served round, block (x, i): gsum[i][g][r] = checksum of row r
+// of field copy g (the batch-mean samples: the amount of every flight of the
+// copy's phonons, equal to the copy's field summed over cells), and, for a
+// solve that keeps its field, acc += the sum of its field copies.
 constexpr int MAX_GROUPS = 8;
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_round_reduce(Params<R> P, double* const* accs, double* gsum) {
     const InstD<R>& I = P.insts[blockIdx.y];
-    const int n = I.rows * I.cols;
-    const int G = I.groups;
-    double part[MAX_GROUPS][4];
-#pragma unroll
-    for (int g = 0; g < MAX_GROUPS; ++g)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) part[g][r] = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x < 4 * MAX_GROUPS) {
+        const int g = threadIdx.x >> 2, r = threadIdx.x & 3;
+        gsum[(long long)blockIdx.y * MAX_GROUPS * 4 + threadIdx.x] = (g < I.groups && r < I.rows) ? I.csum[threadIdx.x] : 0.0;
+    }
     double* a = accs[blockIdx.y];
+    if (a == nullptr || I.tally == nullptr) return;
+    const int n = I.rows * I.cols;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const int r = e % I.rows;
         double s = 0.0;
-#pragma unroll
-        for (int g = 0; g < MAX_GROUPS; ++g) {
-            if (g < G) {
-                const double v = I.tally[(long long)g * I.gstride + e];
-                s += v;
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (q == r) part[g][q] += v;
-            }
-        }
+        for (int g = 0; g < I.groups; ++g) s += I.tally[(long long)g * I.gstride + e];
         a[e] += s;
     }
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int g = 0; g < MAX_GROUPS; ++g)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            double x = part[g][r];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-            if (lane == 0 && g < G && r < I.rows && x != 0.0) atomicAdd(&gsum[((long long)blockIdx.y * MAX_GROUPS + g) * 4 + r], x);
-        }
 }
 
 // Stream compaction of the live slots of a dynamic-kernel state into the

@@ -245,7 +245,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
 template <typename R, int TM>
 __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
                                    Tally<R, TM>& T, long long csum[4]) {
-    const int acc = S.accum;
+    const int acc = (TM == TM_AUTO && (T.I->flags & IF_NO_FIELD)) ? -2 : S.accum;
     const int cb = S.colbeg;
     if (acc < 0) {
         // a single field column (or none): move only

@@ -6,8 +6,9 @@ round of every admitted solve per tick in one persistent batched launch.
 Each round splits its phonons into batch-mean groups; a solve completes when
 the standard error of kappa = -<q_axis>/gradT_axis is within the target.
 The error estimate is the reference's replica statistics
-(montecarlo/main.cpp:181-210, Welford montecarlo/field.cpp:323-330) over
-groups instead of whole repeated runs.
+(montecarlo/main.cpp:181-210, montecarlo/field.cpp:323-330) over groups
+instead of whole repeated runs, pooled over rounds of unequal size: the
+first round has the requested phonons, later ones the estimated remainder.
 """
 
 from __future__ import annotations
@@ -31,13 +32,15 @@ class Server:
         self._keep = {}
 
     def submit(self, mat, dom, nemit, *, problem=FLUX, maxscat=10**6, maxloop=0, seed=0, axis=0, volume=0.0,
-               gradient=0.0):
+               gradient=0.0, field=True):
+        """Queue a kappa solve with `nemit` phonons in its first round;
+        field=False skips the per-cell field (kappa only)."""
         handle = _handle(dom)
         r = _lib.Request(mat.h.value, handle.h.value, problem, int(nemit), int(maxscat), int(maxloop), int(seed),
-                         int(axis), float(volume), float(gradient))
+                         int(axis), float(volume), float(gradient), int(bool(field)))
         t = C.c_long()
         _lib.check(_lib.lib().mc_server_submit(self.h, C.byref(r), C.byref(t)))
-        self._keep[t.value] = (mat, handle, problem)
+        self._keep[t.value] = (mat, handle, problem, bool(field))
         return t.value
 
     def _result(self, ticket, rc, res, field):
@@ -46,9 +49,9 @@ class Server:
         if rc == 0:
             return None
         out = res.as_dict()
-        mat, handle, problem = self._keep.pop(ticket)
+        mat, handle, problem, keep_field = self._keep.pop(ticket)
         rows = 3 if problem == FLUX else 4
-        out["field"] = field[: rows * handle.cols].reshape(rows, handle.cols, order="F").copy()
+        out["field"] = field[: rows * handle.cols].reshape(rows, handle.cols, order="F").copy() if keep_field else None
         return out
 
     def poll(self, ticket):

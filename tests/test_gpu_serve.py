@@ -1,6 +1,6 @@
 """The serving loop: completion by the stopping rule, isolation (a result is
-the same alone and in the mix), HBM-budget admission, and kappa against the
-FP64 oracle."""
+the same alone and in the mix), HBM-budget admission, kappa-only requests,
+growing rounds, and kappa against the FP64 oracle."""
 
 import numpy as np
 import pytest
@@ -96,3 +96,36 @@ def test_kappa_against_fp64_oracle(mats):
     ks = np.array(ks)
     se = np.sqrt(ks.var(ddof=1) / len(ks) + r["kappa_se"] ** 2)
     assert abs(ks.mean() - r["kappa"]) < 3 * se
+
+
+def test_kappa_only_requests(mats):
+    """field=False skips the cell split; kappa comes from the same per-flight
+    sums. On a film (1-D field) the trajectories are those of a field
+    request, so kappa agrees to the FP64 summation order; on the pore cell
+    (3-D walk) the moves round differently, so kappa agrees statistically."""
+    kw = dict(dt=DT, nsteps=NSTEPS, precision=64, groups=8, target_rel_se=0.05, min_rounds=1, max_rounds=20)
+    film = M.FilmDomain.from_cli(1e-7, 1e-7, 50)
+    pore = M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4))
+    out = {}
+    for field in (True, False):
+        srv = M.Server(**kw)
+        tf = srv.submit(mats[300.0], film, 30000, problem=M.MULTI, seed=11, field=field)
+        tp = srv.submit(mats[300.0], pore, 30000, problem=M.MULTI, seed=12, field=field, volume=(5e-7) ** 3)
+        out[field] = (srv.wait(tf), srv.wait(tp))
+        srv.close()
+    (fa, pa), (fb, pb) = out[True], out[False]
+    assert fb["field"] is None and fa["field"] is not None
+    assert fa["rounds"] == fb["rounds"]
+    assert fb["kappa"] == pytest.approx(fa["kappa"], rel=1e-9)
+    assert pa["status"] == pb["status"] == 0
+    assert abs(pa["kappa"] - pb["kappa"]) < 3 * np.hypot(pa["kappa_se"], pb["kappa_se"])
+
+
+def test_rounds_grow_to_the_target(mats):
+    """A small first round is followed by a round sized for the target: the
+    solve needs far fewer rounds than repeats of its first round would."""
+    srv = M.Server(dt=DT, nsteps=NSTEPS, precision=32, groups=8, target_rel_se=0.01, min_rounds=1, max_rounds=100)
+    r = srv.wait(srv.submit(mats[300.0], M.FilmDomain.from_cli(1e-7, 1e-7, 50), 2000, seed=3, field=False))
+    srv.close()
+    assert r["status"] == 0 and r["kappa_se"] <= 0.01 * abs(r["kappa"])
+    assert r["rounds"] <= 4 and r["phonons"] > 20 * 2000
