@@ -734,11 +734,16 @@ int emitT(mc_session_s* S) {
     return MC_OK;
 }
 
-// Fixed-point quantum of the per-block shared tally: a block's partial of
-// any cell is bounded by (phonons the block handles) x (largest amount one
-// phonon can add in a window: the window itself for time rows, vmax x
-// window for displacement rows); 2^-61 of that bound keeps every partial
-// and difference entry inside int64.
+// Fixed-point quantum of the tallies for one row. `flight` bounds what one
+// phonon adds in a window (the window itself for time rows, vmax x window
+// for displacement rows). FP32 flight: 2^-30 of it, so that every flight's
+// amount converts to a 32-bit integer; a block's sums (at most `perBlock`
+// phonons x 2^30) stay inside int64. FP64 flight: 2^-61 of perBlock x
+// flight, converted to 64 bits.
+double tallyQuantum(bool f32, double flight, double perBlock) {
+    return f32 ? std::ldexp(flight * 1.0001, -30) : std::ldexp(perBlock * flight * 1.0001, -61);
+}
+
 template <typename R>
 void setQuanta(const mc_session_s* S, Params<R>& P) {
     const int keff = (int)std::min<long>(S->desc.steps_per_launch, S->desc.nsteps - S->step);
@@ -746,8 +751,7 @@ void setQuanta(const mc_session_s* S, Params<R>& P) {
     const double perBlock = std::ceil((double)S->nemit / ((double)S->grid * S->block)) * S->block;
     for (int r = 0; r < 4; ++r) {
         const bool timeRow = (S->desc.problem == MC_TEMP && r == 0) || (S->desc.problem == MC_MULTI && r == 0);
-        const double bound = perBlock * window * (timeRow ? 1.0 : S->vmax) * 1.0001;
-        const double q = std::ldexp(bound, -61);
+        const double q = tallyQuantum(sizeof(R) == 4, window * (timeRow ? 1.0 : S->vmax), perBlock);
         P.tq[r] = q;
         P.tqinv[r] = (R)(1.0 / q);
     }
@@ -1049,7 +1053,7 @@ int setupBatch(mc_batch_s* B) {
         // a block's shared field takes at most the instance's phonons
         for (int r = 0; r < 4; ++r) {
             const bool timeRow = (pd.problem == MC_TEMP || pd.problem == MC_MULTI) && r == 0;
-            const double q = std::ldexp((double)B->nemit[i] * window * (timeRow ? 1.0 : vmax) * 1.0001, -61);
+            const double q = tallyQuantum(sizeof(R) == 4, window * (timeRow ? 1.0 : vmax), (double)B->nemit[i]);
             I.tq[r] = q;
             I.tqinv[r] = (R)(1.0 / q);
         }
@@ -1342,7 +1346,7 @@ struct ServerT : ServerBase {
         const double perCopy = (double)((j->nemit + d.groups - 1) / d.groups);
         for (int r = 0; r < 4; ++r) {
             const bool timeRow = j->req.problem == MC_MULTI && r == 0;
-            const double q = std::ldexp(perCopy * window * (timeRow ? 1.0 : j->vmax) * 1.0001, -61);
+            const double q = tallyQuantum(sizeof(R) == 4, window * (timeRow ? 1.0 : j->vmax), perCopy);
             I.tq[r] = q;
             I.tqinv[r] = (R)(1.0 / q);
         }

@@ -72,48 +72,64 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
     return I;
 }
 
-// End of a single-instance launch: counters and checksums (one atomic per
-// warp), then the block's difference array turned into cell values and the
-// fixed-point field flushed as FP64 atomics.
-template <typename R, int TM>
-__device__ __forceinline__ void closeBlock(const Params<R>& P, const InstD<R>& I, const Counts& C,
-                                           const long long csum[4]) {
+// Sum row r of the block's shared fixed-point field (cells) into the
+// block checksums: the field holds every flight amount that did not go to
+// g_blk.csum directly. Then flush the cells as FP64 atomics into `dst`
+// (rows x cols column-major) and clear them. All threads, after a barrier.
+template <typename R>
+__device__ __forceinline__ void flushSharedField(const InstD<R>& I, double* dst) {
     const int lane = threadIdx.x & 31;
-    flushCounts(P.counters, C);
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // difference rows -> cells
+    for (int r = warp; r < I.rows; r += nwarps) {
+        long long carry = 0;
+        long long* dr = I.dif + r * (I.cols + 1);
+        for (int c0 = 0; c0 < I.cols; c0 += 32) {
+            const int c = c0 + lane;
+            long long x = c < I.cols ? dr[c] : 0;
+            if (c < I.cols) dr[c] = 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            x += carry;
+            if (c < I.cols) I.tal[r * I.cols + c] += x;
+            carry = __shfl_sync(0xFFFFFFFFu, x, 31);
+        }
+        if (lane == 0) dr[I.cols] = 0;
+    }
+    __syncthreads();
+    long long part[4] = {0, 0, 0, 0};
+    const int tot = I.rows * I.cols;
+    for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+        const long long x = I.tal[q];
+        if (x != 0) {
+            const int r = q / I.cols, c = q - r * I.cols;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k == r) part[k] += x;
+            atomicAdd(&dst[(size_t)c * I.rows + r], (double)x * I.tq[r]);
+            I.tal[q] = 0;
+        }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        long long x = csum[r];
+        long long x = part[r];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && r < P.rows && x != 0) atomicAdd(&P.csum[r], (double)x * P.tq[r]);
+        if (lane == 0 && x != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g_blk.csum[r]), (unsigned long long)x);
     }
-    if (TM == TM_SHARED) {
-        __syncthreads();
-        const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-        for (int r = warp; r < P.rows; r += nwarps) {
-            long long carry = 0;
-            const long long* dr = I.dif + r * (P.cols + 1);
-            for (int c0 = 0; c0 < P.cols; c0 += 32) {
-                const int c = c0 + lane;
-                long long x = c < P.cols ? dr[c] : 0;
-                for (int o = 1; o < 32; o <<= 1) {
-                    long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                    if (lane >= o) x += y;
-                }
-                x += carry;
-                if (c < P.cols) I.tal[r * P.cols + c] += x;
-                carry = __shfl_sync(0xFFFFFFFFu, x, 31);
-            }
-        }
-        __syncthreads();
-        const int tot = P.rows * P.cols;
-        for (int q = threadIdx.x; q < tot; q += blockDim.x) {
-            const long long x = I.tal[q];
-            if (x != 0) {
-                const int r = q / P.cols, c = q - r * P.cols;
-                atomicAdd(&P.tally[(size_t)c * P.rows + r], (double)x * P.tq[r]);
-            }
-        }
-    }
+}
+
+// End of a single-instance launch: the shared field flushed into the global
+// one, the block checksums and counters added to the launch's.
+template <typename R, int TM>
+__device__ __forceinline__ void closeBlock(const Params<R>& P, const InstD<R>& I) {
+    __syncthreads();
+    if (TM == TM_SHARED) flushSharedField<R>(I, P.tally);
+    __syncthreads();
+    if (threadIdx.x < I.rows && g_blk.csum[threadIdx.x] != 0)
+        atomicAdd(&P.csum[threadIdx.x], (double)g_blk.csum[threadIdx.x] * I.tq[threadIdx.x]);
+    flushCounts(P.counters);
 }
 
 // -------------------------------------------------------------- emission
@@ -197,17 +213,18 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // survivors are compacted to the two ends of the other half of the
 // ping-pong state (front: next event inside the next window).
 template <typename R, bool REPLAY, bool LOG, int TM>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance(Params<R> P) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2) k_advance(Params<R> P) {
     extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ unsigned sWarp[2][8];
+    __shared__ unsigned long long sBase[2];
     InstD<R>* I = stageTables<R, TM>(P, smraw);
+    blkZero();
     __syncthreads();
 
     const unsigned long long nf = P.live_in[0], nb = P.live_in[1];
     const unsigned long long n = nf + nb;
     Window<R> W;
     W.init(P);
-    long long csum[4] = {0, 0, 0, 0};
-    Counts C;
     const int lane = threadIdx.x & 31;
 
     for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n;
@@ -223,21 +240,30 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
             A2 = __ldcs(P.P2in + slot);
             Walker<R, REPLAY, LOG, TM> wk;
             wk.load(P, I, W, A0, A1, A2);
-            while (!wk.iterate(P, W, C, csum)) {}
-            alive = wk.finish(P, W, C);
+            while (!wk.iterate(P, W)) {}
+            alive = wk.finish(P, W);
             soon = wk.tnext < W.next;
             if (alive) wk.pack(A0, A1, A2);
         }
-        // fused compaction into two ends: one atomic per warp and end
+        // fused compaction into two ends: warp counts scanned in shared
+        // memory, one atomic per block pass and end
         const unsigned mf = __ballot_sync(0xFFFFFFFFu, alive && soon);
         const unsigned mb = __ballot_sync(0xFFFFFFFFu, alive && !soon);
-        unsigned long long bf = 0, bb = 0;
-        if (lane == 0) {
-            if (mf) bf = atomicAdd(&P.live_out[0], (unsigned long long)__popc(mf));
-            if (mb) bb = atomicAdd(&P.live_out[1], (unsigned long long)__popc(mb));
+        const int warp = threadIdx.x >> 5;
+        if (lane == 0) { sWarp[0][warp] = (unsigned)__popc(mf); sWarp[1][warp] = (unsigned)__popc(mb); }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tf = 0, tb = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const unsigned f = sWarp[0][w], b = sWarp[1][w];
+                sWarp[0][w] = tf; sWarp[1][w] = tb;
+                tf += f; tb += b;
+            }
+            sBase[0] = tf ? atomicAdd(&P.live_out[0], (unsigned long long)tf) : 0ull;
+            sBase[1] = tb ? atomicAdd(&P.live_out[1], (unsigned long long)tb) : 0ull;
         }
-        bf = __shfl_sync(0xFFFFFFFFu, bf, 0);
-        bb = __shfl_sync(0xFFFFFFFFu, bb, 0);
+        __syncthreads();
+        const unsigned long long bf = sBase[0] + sWarp[0][warp], bb = sBase[1] + sWarp[1][warp];
         if (alive) {
             const unsigned lt = (1u << lane) - 1u;
             const unsigned long long o = soon ? bf + __popc(mf & lt) : P.cap - 1 - (bb + __popc(mb & lt));
@@ -246,7 +272,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
             __stcs(P.P2out + o, A2);
         }
     }
-    closeBlock<R, TM>(P, *I, C, csum);
+    closeBlock<R, TM>(P, *I);
 }
 
 // Dynamic schedule shared by the single-instance and batched kernels: the
@@ -261,7 +287,7 @@ constexpr int REFILL = 8;
 template <typename R, bool REPLAY, bool LOG, int TM>
 __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
                                             unsigned long long qbeg, unsigned long long qend,
-                                            const InstD<R>* I, const Window<R>& W, Counts& C, long long csum[4]) {
+                                            const InstD<R>* I, const Window<R>& W) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Walker<R, REPLAY, LOG, TM> wk;
@@ -295,10 +321,10 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
             if (drained) break;
             continue;
         }
-        if (have && wk.iterate(P, W, C, csum)) {
+        if (have && wk.iterate(P, W)) {
             typename Vec4<R>::T A0, A1;
             uint4 A2;
-            if (wk.finish(P, W, C)) {
+            if (wk.finish(P, W)) {
                 wk.pack(A0, A1, A2);
                 st4(P.P0out + slot, A0);
                 st4(P.P1out + slot, A1);
@@ -324,18 +350,17 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ unsigned long long qnext;
     InstD<R>* I = stageTables<R, TM>(P, smraw);
+    blkZero();
     if (threadIdx.x == 0) qnext = 0;
     __syncthreads();
     Window<R> W;
     W.init(P);
-    long long csum[4] = {0, 0, 0, 0};
-    Counts C;
     const unsigned long long n = P.live_in[0];
     const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
     const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
     const unsigned long long qend = min(qbeg + chunk, n);
-    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, I, W, C, csum);
-    closeBlock<R, TM>(P, *I, C, csum);
+    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, I, W);
+    closeBlock<R, TM>(P, *I);
 }
 
 // The current instance of a batched block, staged in shared memory: its
@@ -379,49 +404,17 @@ __device__ __forceinline__ void stageInstance(const Params<R>& P, int inst, unsi
     }
 }
 
-// End of a batched block's binding to (instance, group): checksums (one
-// atomic per warp and row), then the shared field, if any, turned from
-// difference form into cells, flushed into field copy `group` as FP64
-// atomics and cleared. Called by all threads after the binding's barrier.
+// End of a batched block's binding to (instance, group): the shared field,
+// if any, flushed into field copy `group`, and the binding's checksums added
+// to the copy's. All threads, after the binding's barrier.
 template <typename R>
-__device__ __forceinline__ void flushBinding(const InstD<R>& I, int group, long long csum[4]) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        long long x = csum[r];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && r < I.rows && x != 0) atomicAdd(&I.csum[4 * group + r], (double)x * I.tq[r]);
-        csum[r] = 0;
-    }
-    if (I.tal == nullptr) return;
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int r = warp; r < I.rows; r += nwarps) {
-        long long carry = 0;
-        long long* dr = I.dif + r * (I.cols + 1);
-        for (int c0 = 0; c0 < I.cols; c0 += 32) {
-            const int c = c0 + lane;
-            long long x = c < I.cols ? dr[c] : 0;
-            if (c < I.cols) dr[c] = 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                if (lane >= o) x += y;
-            }
-            x += carry;
-            if (c < I.cols) I.tal[r * I.cols + c] += x;
-            carry = __shfl_sync(0xFFFFFFFFu, x, 31);
-        }
-        if (lane == 0) dr[I.cols] = 0;
-    }
+__device__ __forceinline__ void flushBinding(const InstD<R>& I, int group) {
+    if (I.tal != nullptr) flushSharedField<R>(I, I.tally + (long long)group * I.gstride);
     __syncthreads();
-    const int tot = I.rows * I.cols;
-    double* dst = I.tally + (long long)group * I.gstride;
-    for (int q = threadIdx.x; q < tot; q += blockDim.x) {
-        const long long x = I.tal[q];
-        if (x != 0) {
-            const int r = q / I.cols, c = q - r * I.cols;
-            atomicAdd(&dst[(size_t)c * I.rows + r], (double)x * I.tq[r]);
-            I.tal[q] = 0;
-        }
+    if (threadIdx.x < 4) {
+        const long long x = g_blk.csum[threadIdx.x];
+        if (threadIdx.x < I.rows && x != 0) atomicAdd(&I.csum[4 * group + threadIdx.x], (double)x * I.tq[threadIdx.x]);
+        g_blk.csum[threadIdx.x] = 0;
     }
 }
 
@@ -441,8 +434,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     const InstD<R>* I = reinterpret_cast<const InstD<R>*>(smraw + L.inst);
     Window<R> W;
     W.init(P);
-    long long csum[4] = {0, 0, 0, 0};
-    Counts C;
+    blkZero();
     int cur = P.home[blockIdx.x];
     int curInst = -1;
     for (int bind = 0; bind < (1 << 30); ++bind) {
@@ -468,12 +460,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
         }
         __syncthreads();
         dynamicLoop<R, false, false, TM_AUTO>(P, P.segNext + sg, (unsigned long long)S.beg,
-                                              (unsigned long long)S.end, I, W, C, csum);
+                                              (unsigned long long)S.end, I, W);
         __syncthreads();
-        flushBinding<R>(*I, S.group, csum);
+        flushBinding<R>(*I, S.group);
         __syncthreads();
     }
-    flushCounts(P.counters, C);
+    flushCounts(P.counters);
 }
 
 // Shared memory of the batched kernel.

@@ -72,9 +72,16 @@ enum { TM_SHARED = 0, TM_GLOBAL = 1, TM_AUTO = 2 };
 constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 
 // Resident blocks of 256 threads per SM the FP32 advance kernels are
-// compiled for (register budget 65536 / (256 x this)).
+// compiled for (register budget 65536 / (256 x this)): three (80
+// registers) measured faster than four (64, with spills) on the fused
+// kernels.
 #ifndef MC_MIN_BLOCKS_F32
-#define MC_MIN_BLOCKS_F32 4
+#define MC_MIN_BLOCKS_F32 3
+#endif
+// The one-phonon-per-thread static kernel waits on its state loads and is
+// compiled for four resident blocks.
+#ifndef MC_MIN_BLOCKS_STATIC_F32
+#define MC_MIN_BLOCKS_STATIC_F32 4
 #endif
 
 template <typename R>
@@ -89,18 +96,11 @@ struct Phn {
     uint32_t nscat, nloop, id;
 };
 
-// Round a float to the nearest int64 with integer instructions only (the
-// float -> int64 conversion runs on GB300's narrow FP64 pipe). |v| < 2^61.
-__device__ __forceinline__ long long toFixed(float v) {
-    const uint32_t b = __float_as_uint(v);
-    const int e = (int)((b >> 23) & 0xFFu) - 150;  // v = m * 2^e
-    const long long m = (long long)((b & 0x7FFFFFu) | 0x800000u);
-    long long r;
-    if (e >= 0) r = m << e;
-    else if (e > -25) r = (m + (1LL << (-e - 1))) >> (-e);
-    else r = 0;
-    return (b >> 31) ? -r : r;
-}
+// Fixed-point amount of a flight. FP32 flight: the quantum gives the
+// largest single flight 2^30 units, so one 32-bit round-to-nearest
+// conversion suffices (|v| < 2^31); sums are kept in 64 bits. FP64 flight:
+// 64-bit conversion against a quantum sized for a block's total.
+__device__ __forceinline__ long long toFixed(float v) { return (long long)__float2int_rn(v); }
 __device__ __forceinline__ long long toFixed(double v) { return __double2ll_rn(v); }
 
 // float -> double by moving the bits (the conversion instruction runs on
@@ -114,6 +114,45 @@ __device__ __forceinline__ double toDouble(float v) {
     return __hiloint2double((int)hi, (int)(m << 29));
 }
 __device__ __forceinline__ double toDouble(double v) { return v; }
+
+// Per-block accumulators in shared memory: the launch counters and the
+// rows' fixed-point checksums of the flights whose field amount does not go
+// into the block's shared field (those are summed from it at the end).
+struct BlockAcc {
+    unsigned long long cnt[C_NCOUNTERS];
+    long long csum[4];
+};
+static __shared__ BlockAcc g_blk;
+
+// Add n to block counter c, summed first over the lanes of the warp that
+// reach this point together with the same c (one shared atomic per group).
+__device__ __forceinline__ void blkCount(int c, unsigned n) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, c);
+    const unsigned tot = __reduce_add_sync(peers, n);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(&g_blk.cnt[c], (unsigned long long)tot);
+}
+
+// Add v to the block checksum of row r, summed first over the lanes that
+// reach this point together (all with the same r): three 22-bit limbs keep
+// the 32-bit warp sums exact.
+__device__ __forceinline__ void blkCsum(int r, long long v) {
+    const unsigned act = __activemask();
+    const unsigned long long u = (unsigned long long)v;
+    const int s0 = __reduce_add_sync(act, (int)(u & 0x3FFFFFull));
+    const int s1 = __reduce_add_sync(act, (int)((u >> 22) & 0x3FFFFFull));
+    const int s2 = __reduce_add_sync(act, (int)(v >> 44));
+    if ((int)(threadIdx.x & 31) == __ffs(act) - 1) {
+        const long long t = (long long)s0 + (long long)s1 * (1LL << 22) + (long long)s2 * (1LL << 44);
+        if (t != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g_blk.csum[r]), (unsigned long long)t);
+    }
+}
+
+// Zero the block accumulators (all threads; a barrier must follow).
+__device__ __forceinline__ void blkZero() {
+    unsigned long long* z = reinterpret_cast<unsigned long long*>(&g_blk);
+    for (int i = threadIdx.x; i < (int)(sizeof(BlockAcc) / 8); i += blockDim.x) z[i] = 0ull;
+}
 
 // Field accumulation for one flight of one instance.
 template <typename R, int TM>
@@ -129,6 +168,8 @@ struct Tally {
     }
     // fixed-point amount of row r for path length t
     __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * I->tqinv[r])); }
+    // a flight's amount that does not enter the shared field
+    __device__ __forceinline__ void csumAdd(int r, long long v) const { blkCsum(r, v); }
     __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
         atomicAdd(reinterpret_cast<unsigned long long*>(&I->tal[r * I->cols + col]), (unsigned long long)v);
     }
@@ -191,7 +232,7 @@ __device__ __forceinline__ void moveAxis(Phn<R>& ph, const SdomD<R>& S, int k, R
 // takes the integer remainder, so the cells add up to V exactly.
 template <typename R, int TM, int K>
 __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                      Tally<R, TM>& T, long long csum[4]) {
+                                      Tally<R, TM>& T) {
     const int cb = S.colbeg;
     const int b = ph.idx[K];
     const int n = S.shape[K];
@@ -207,7 +248,6 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
     for (int r = 0; r < 4; ++r) {
         if (r >= T.rows()) break;
         const long long V = T.fixedOf(r, s);
-        csum[r] += V;
         if (T.shared()) {
             if (e == b) {
                 T.atomShared(r, cb + b * stride, V);
@@ -219,6 +259,8 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
                 if (stride == 1) { if (hi - lo > 1) T.atomRange(r, cb + lo + 1, cb + hi, I); }
                 else for (int c = lo + 1; c < hi; ++c) T.atomShared(r, cb + c * stride, I);
             }
+        } else {
+            T.csumAdd(r, V);
         }
     }
     if (!T.shared()) {
@@ -244,7 +286,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
 // the flight's fixed-point amount to the checksums.
 template <typename R, int TM>
 __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                   Tally<R, TM>& T, long long csum[4]) {
+                                   Tally<R, TM>& T) {
     const int acc = (TM == TM_AUTO && (T.I->flags & IF_NO_FIELD)) ? -2 : S.accum;
     const int cb = S.colbeg;
     if (acc < 0) {
@@ -253,21 +295,24 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         for (int r = 0; r < 4; ++r) {
             if (r >= T.rows()) break;
             const long long V = T.fixedOf(r, s);
-            csum[r] += V;
             if (acc == -1 && T.shared()) T.atomShared(r, cb, V);
+            else T.csumAdd(r, V);
         }
         if (acc == -1 && !T.shared()) T.addGlobal(cb, s);
 #pragma unroll
         for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
         return;
     }
-    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, ia, s, T, csum); return; }
-    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, ia, s, T, csum); return; }
-    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, ia, s, T, csum); return; }
-    // 2-D / 3-D: walk the cells (Amanatides-Woo)
+    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, ia, s, T); return; }
+    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, ia, s, T); return; }
+    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, ia, s, T); return; }
+    // 2-D / 3-D: walk the cells (Amanatides-Woo); a shared field gives the
+    // checksum as the sum of its cells, a global one the flight's amount
+    if (!T.shared()) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
-        if (r < T.rows()) csum[r] += T.fixedOf(r, s);
+        for (int r = 0; r < 4; ++r)
+            if (r < T.rows()) T.csumAdd(r, T.fixedOf(r, s));
+    }
     R rem = s;
     const int s0 = S.tstride[1], s01 = S.tstride[2];
     for (int guard = 0; guard < 3 * MAX_SHAPE + 4; ++guard) {
@@ -425,10 +470,10 @@ struct Window {
     }
 };
 
-// Per-thread counters, reduced once per launch.
-struct Counts {
-    uint32_t steps = 0, events = 0, scat = 0, esc = 0, hor = 0, maxs = 0, maxl = 0, abs = 0, bad = 0;
-};
+// Walker state that only the replay kernels carry.
+struct NoReplay {};
+template <bool REPLAY> struct ReplayState { using T = NoReplay; };
+template <> struct ReplayState<true> { using T = Rng<true>; };
 
 // Dead marker in the prop word of a slot written back in place.
 constexpr uint32_t PROP_DEAD = 1u << 25;
@@ -443,13 +488,14 @@ struct Walker {
     const InstD<R>* I;
     const SdomD<R>* S;
     R a[3], ia[3];
-    R v, iv, sg;
+    R v, iv;
     R budget;
     R tnext;       // time to the next event after the window end
-    int nev;
+    int nev;       // events in this window
     int stop;      // 0 alive, else the counter of the stop reason
-    long long goff;  // field copy of this phonon (batch means)
-    Rng<REPLAY> g;
+    // the replay stream's position persists across events; a Philox stream
+    // is set up afresh at each event from (key, phonon id, event index)
+    typename ReplayState<REPLAY>::T rg;
 
     __device__ __forceinline__ void load(const Params<R>& P, const InstD<R>* inst, const Window<R>& W,
                                          const typename Vec4<R>::T& A0, const typename Vec4<R>::T& A1,
@@ -464,17 +510,15 @@ struct Walker {
         ph.neg = (A2.y >> 24) & 1u;
         ph.nscat = A2.z;
         ph.nloop = A2.w;
-        g.init(I->key0, I->key1, ph.id, &P);
+        if constexpr (REPLAY) rg.init(I->key0, I->key1, ph.id, &P);
         budget = W.len;
         S = &I->sd[ph.s];
         reducedVel(*S, ph.d, a, ia);
         v = I->vel[ph.w * I->np + ph.p];
         iv = R(1) / v;
-        sg = ph.neg ? R(-1) : R(1);
         stop = 0;
         nev = 0;
         tnext = R(0);
-        goff = I->groups > 1 ? (long long)(ph.id % (uint32_t)I->groups) * I->gstride : 0;
     }
 
     __device__ __forceinline__ void pack(typename Vec4<R>::T& A0, typename Vec4<R>::T& A1, uint4& A2) const {
@@ -482,7 +526,7 @@ struct Walker {
     }
 
     // returns true when the phonon's window is over (alive or stopped)
-    __device__ __forceinline__ bool iterate(const Params<R>& P, const Window<R>& W, Counts& C, long long csum[4]) {
+    __device__ __forceinline__ bool iterate(const Params<R>& P, const Window<R>& W) {
         // Subdomain::advect (montecarlo/subdomain.cpp:161-192): the
         // approaching face of each axis, in the reference's face order
         // (lower faces 0..2, then upper faces 3..5), against the free path;
@@ -505,13 +549,15 @@ struct Walker {
         // tally amounts per metre (montecarlo/problem.cpp:473-544)
         Tally<R, TM> T;
         T.I = I;
-        T.goff = goff;
+        // field copy of this phonon (batch means), global fields only
+        T.goff = (TM != TM_SHARED && I->groups > 1) ? (long long)(ph.id % (uint32_t)I->groups) * I->gstride : 0;
+        const R sg = ph.neg ? R(-1) : R(1);
         if (I->problem == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
         else if (I->problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
         else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
         const int sBefore = ph.s;
         int cellEnd = 0;
-        fly<R, TM>(ph, *S, a, ia, s, T, csum);
+        fly<R, TM>(ph, *S, a, ia, s, T);
         if (LOG) cellEnd = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
         ph.scatNext -= s;
         if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
@@ -533,6 +579,9 @@ struct Walker {
         }
         double xe[3];
         if (LOG) physPos(*S, ph, xe);
+        Rng<REPLAY> g;
+        if constexpr (REPLAY) g = rg;
+        else g.init(I->key0, I->key1, ph.id, &P);
         g.setEvent(ph.nloop + 1);
         if (face >= 0) {
             const FaceD<R>& F = S->f[face];
@@ -565,13 +614,18 @@ struct Walker {
                 if (F.to < 0) { stop = C_ESCAPES; break; }
                 if (F.tang) {
                     // same axis, tangential cells unchanged: keep the split
-                    // coordinates, move onto the paired face
+                    // coordinates, move onto the paired face (selects on
+                    // every axis: no indexed writes into the phonon state)
                     ph.s = F.to;
                     S = &I->sd[ph.s];
+                    const int tf = F.toface;
+                    const int tax = tf >= 3 ? tf - 3 : tf;
+                    const bool up = tf >= 3;
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
-                        if (F.toface == j) { ph.idx[j] = 0; ph.off[j] = R(0); }
-                        if (F.toface == j + 3) { ph.idx[j] = S->shape[j] - 1; ph.off[j] = R(1); }
+                        const bool on = tax == j;
+                        ph.idx[j] = on ? (up ? S->shape[j] - 1 : 0) : ph.idx[j];
+                        ph.off[j] = on ? (up ? R(1) : R(0)) : ph.off[j];
                     }
                 } else {
                     R u[3], u2[3];
@@ -612,27 +666,30 @@ struct Walker {
             ph.scatNext = drawScatNext<R>(g, I->vt[ph.w * I->np + ph.p]);
             v = I->vel[ph.w * I->np + ph.p];
             iv = R(1) / v;
-            ++C.scat;
+            blkCount(C_SCATTERS, 1);
         }
-        ++C.events;
+        ++nev;
         if (LOG) logEvent(P, ph, sBefore, face, ph.s, xe, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
                           cellEnd);
         ph.nloop++;
-        if (REPLAY && g.exhausted()) { stop = C_REPLAY_EXHAUSTED; return true; }
+        if constexpr (REPLAY) {
+            rg = g;
+            if (g.exhausted()) { stop = C_REPLAY_EXHAUSTED; return true; }
+        }
         if (stop) return true;
         if ((long long)ph.nscat >= I->maxscat) { stop = C_MAXSCAT; return true; }
         if ((long long)ph.nloop >= I->maxloop) { stop = C_MAXLOOP; return true; }
-        if (++nev >= MAX_EVENTS_PER_LAUNCH) { stop = C_BAD; return true; }
+        if (nev >= MAX_EVENTS_PER_LAUNCH) { stop = C_BAD; return true; }
         reducedVel(*S, ph.d, a, ia);
         return false;
     }
 
-    // the phonon's window is over: count its steps and its stop reason;
-    // returns true if it stays alive
-    __device__ __forceinline__ bool finish(const Params<R>& P, const Window<R>& W, Counts& C) {
-        if (REPLAY) g.save();
+    // the phonon's window is over: count its steps, events and stop
+    // reason; returns true if it stays alive
+    __device__ __forceinline__ bool finish(const Params<R>& P, const Window<R>& W) {
+        if constexpr (REPLAY) rg.save();
+        int st = W.keff;
         if (stop == 0) {
-            C.steps += W.keff;
             if (W.last) {
                 stop = C_HORIZON;
                 if (LOG) {
@@ -643,36 +700,22 @@ struct Walker {
             }
         } else {
             R el = W.len - budget;
-            int st = (int)ceil(el * W.invdt);
+            st = (int)ceil(el * W.invdt);
             st = st < 1 ? 1 : (st > W.keff ? W.keff : st);
-            C.steps += st;
         }
-        switch (stop) {
-        case 0: break;
-        case C_ESCAPES: ++C.esc; break;
-        case C_HORIZON: ++C.hor; break;
-        case C_MAXSCAT: ++C.maxs; break;
-        case C_MAXLOOP: ++C.maxl; break;
-        case C_ABSORBED: ++C.abs; break;
-        case C_REPLAY_EXHAUSTED: atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED); break;
-        default: ++C.bad; atomicOr(P.status, (unsigned)S_NONFINITE); break;
-        }
+        blkCount(C_PHONON_STEPS, (unsigned)st);
+        blkCount(C_EVENTS, (unsigned)nev);
+        if (stop == C_REPLAY_EXHAUSTED) atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED);
+        else if (stop == C_BAD) atomicOr(P.status, (unsigned)S_NONFINITE);
+        if (stop != 0 && stop != C_REPLAY_EXHAUSTED) blkCount(stop, 1);
         return stop == 0;
     }
 };
 
-// Reduce the counters (one atomic per warp).
-__device__ __forceinline__ void flushCounts(unsigned long long* counters, const Counts& C) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t cs[9] = {C.steps, C.events, C.scat, C.esc, C.hor, C.maxs, C.maxl, C.abs, C.bad};
-    const int ids[9] = {C_PHONON_STEPS, C_EVENTS, C_SCATTERS, C_ESCAPES, C_HORIZON, C_MAXSCAT,
-                        C_MAXLOOP, C_ABSORBED, C_BAD};
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        unsigned long long x = cs[q];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && x) atomicAdd(&counters[ids[q]], x);
-    }
+// Add the block's counters to the launch counters (after a barrier).
+__device__ __forceinline__ void flushCounts(unsigned long long* counters) {
+    for (int q = threadIdx.x; q < C_NCOUNTERS; q += blockDim.x)
+        if (g_blk.cnt[q]) atomicAdd(&counters[q], g_blk.cnt[q]);
 }
 
 }  // namespace mcg
