@@ -36,6 +36,7 @@ extern "C" {
 #define MC_ERR_REPLAY (-6)       /* replay stream exhausted                */
 #define MC_ERR_NONFINITE (-7)    /* non-finite phonon state                */
 #define MC_ERR_BUSY (-8)         /* admission refused (serving)            */
+#define MC_ERR_TIMEOUT (-9)      /* a bounded device-side wait gave up     */
 
 /* Message of the last error on the calling thread. */
 const char* mc_last_error(void);
@@ -126,9 +127,11 @@ typedef struct {
     long log_cap;
     long log_phonons;
     void* stream;           /* cudaStream_t; NULL -> library stream        */
-    int schedule;           /* MC_SCHED_*: static one-phonon-per-thread
-                               passes with front/back compaction, or
-                               dynamic lane refill with in-place state     */
+    int schedule;           /* MC_SCHED_*: static (state tiles streamed
+                               through shared memory by bulk copies, one
+                               phonon per thread, in place, partitioned by
+                               next event within each tile), or dynamic
+                               lane refill with in-place state             */
     int compact_interval;   /* dynamic schedule: compact dead slots every
                                this many launches (0: never)               */
 } mc_problem_desc;

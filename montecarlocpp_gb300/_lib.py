@@ -15,7 +15,7 @@ from . import build as _build
 MC_OK = 0
 ERRORS = {
     -1: "invalid argument", -2: "CUDA error", -3: "no CUDA device", -4: "unsupported geometry",
-    -5: "I/O error", -6: "replay stream exhausted", -7: "non-finite state", -8: "busy",
+    -5: "I/O error", -6: "replay stream exhausted", -7: "non-finite state", -8: "busy", -9: "device wait timeout",
 }
 
 

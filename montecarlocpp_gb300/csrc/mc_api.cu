@@ -521,6 +521,8 @@ struct mc_session_s {
     uint32_t* rcur_d = nullptr;
     double* log_d = nullptr;
     int* logcnt_d = nullptr;
+    unsigned* reg_d = nullptr;    // static schedule: front / back live counts
+                                  // per block region, one array per half
     int parity = 0;               // which half holds the live phonons
     double vmax = 0.;             // largest group velocity of the material
     Params<float> p32{};
@@ -617,20 +619,6 @@ int setupSession(mc_session_s* S) {
     if (rc) return rc;
     rc = uploadDomain<R>(D, m.fluxSum, S->desc.nemit, &S->dom_d, &S->em_d, &S->cdf_d, P, S->nemit, S->power);
     if (rc) return rc;
-    // state: two halves of (P0, P1, P2)
-    const size_t n = (size_t)S->nemit;
-    using V4 = typename Vec4<R>::T;
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
-    S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
-    CK(cudaMalloc(&S->state, 2 * half));
-    char* sb = (char*)S->state;
-    V4* h0[2]; V4* h1[2]; uint4* h2[2];
-    for (int h = 0; h < 2; ++h) {
-        h0[h] = (V4*)sb; sb += al(sizeof(V4) * n);
-        h1[h] = (V4*)sb; sb += al(sizeof(V4) * n);
-        h2[h] = (uint4*)sb; sb += al(sizeof(uint4) * n);
-    }
     // counters: C_NCOUNTERS + two (front, back) live-count pairs
     CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
     CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
@@ -675,21 +663,43 @@ int setupSession(mc_session_s* S) {
     const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
     S->tm = S->desc.tally_mode;
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
-    {
-        const int nsdShared = sizeof(SdomD<R>) * D.sd.size() <= SD_SHARED_MAX ? (int)D.sd.size() : 0;
-        SmemLayout L;
-        L.init<R>((int)m.nw, (int)m.np, nsdShared, S->rows, (int)D.cols, S->tm == TM_SHARED);
-        S->smem = L.total;
-    }
-    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
     S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
     if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    {
+        const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
+                                             S->tm == TM_SHARED);
+        S->smem = L.total;
+        // static schedule: the state stages after the tables
+        if (!S->dyn) S->smem = staticStageOffset(L.total) + STATIC_STAGES * staticStageBytes<R>(S->block);
+    }
+    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     int occ = advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    // state: two halves of (P0, P1, P2). The static schedule cuts each half
+    // into one region of C slots per block of its (fixed) grid.
+    size_t n = (size_t)S->nemit;
+    if (!S->dyn) {
+        const long long C = (S->nemit + S->grid - 1) / S->grid;
+        n = (size_t)C * (size_t)S->grid;
+        CK(cudaMalloc(&S->reg_d, sizeof(unsigned) * 4 * (size_t)S->grid));
+        P.regCap = C;
+    }
+    using V4 = typename Vec4<R>::T;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
+    S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
+    CK(cudaMalloc(&S->state, 2 * half));
+    char* sb = (char*)S->state;
+    V4* h0[2]; V4* h1[2]; uint4* h2[2];
+    for (int h = 0; h < 2; ++h) {
+        h0[h] = (V4*)sb; sb += al(sizeof(V4) * n);
+        h1[h] = (V4*)sb; sb += al(sizeof(V4) * n);
+        h2[h] = (uint4*)sb; sb += al(sizeof(uint4) * n);
+    }
     // halves
     Params<R>* dst = nullptr;
     if (sizeof(R) == 4) dst = (Params<R>*)&S->p32; else dst = (Params<R>*)&S->p64;
@@ -723,6 +733,11 @@ int emitT(mc_session_s* S) {
     if (S->logging) {
         CK(cudaMemsetAsync(S->logcnt_d, 0, sizeof(int) * std::min<long long>(S->desc.log_phonons, S->nemit), S->stream));
         CK(cudaMemsetAsync(S->log_d, 0xFF, sizeof(double) * 12 * (size_t)std::min<long long>(S->desc.log_phonons, S->nemit) * S->desc.log_cap, S->stream));
+    }
+    if (!S->dyn) {
+        // region counts of the emitted half (the kernel sets the fronts)
+        E.regIn = S->reg_d + 2 * (size_t)S->grid * S->parity;
+        CK(cudaMemsetAsync(E.regIn, 0, sizeof(unsigned) * 2 * (size_t)S->grid, S->stream));
     }
     // live counts of the emitted half: all in front
     unsigned long long n = (unsigned long long)S->nemit;
@@ -795,9 +810,9 @@ int advanceT(mc_session_s* S, int nl, int* done) {
                 S->sinceCompact = 0;
             }
         } else {
-            P.live_in = cur;
-            P.live_out = oth;
-            CK(cudaMemsetAsync(oth, 0, 2 * sizeof(unsigned long long), S->stream));
+            // block regions of the current half -> the other half
+            P.regIn = S->reg_d + 2 * (size_t)S->grid * S->parity;
+            P.regOut = S->reg_d + 2 * (size_t)S->grid * (S->parity ^ 1);
             CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
             S->parity ^= 1;
             S->step += S->desc.steps_per_launch;
@@ -856,6 +871,7 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
         CK(cudaMemcpy(cs, S->csum_d, sizeof(cs), cudaMemcpyDeviceToHost));
         for (int r = 0; r < 4; ++r) st->checksum[r] = cs[r];
     }
+    if (status & S_TIMEOUT) return fail(MC_ERR_TIMEOUT, "a device-side wait exceeded its limit; results discarded");
     if (status & S_REPLAY_EXHAUSTED) return fail(MC_ERR_REPLAY, "replay stream exhausted");
     if (status & S_NONFINITE) return fail(MC_ERR_NONFINITE, "non-finite phonon state");
     return MC_OK;
@@ -864,7 +880,7 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
 void freeSession(mc_session_s* S) {
     if (!S) return;
     void* ps[] = {S->state, S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
-                  S->rwords_d, S->roff_d, S->rcur_d, S->log_d, S->logcnt_d};
+                  S->rwords_d, S->roff_d, S->rcur_d, S->log_d, S->logcnt_d, S->reg_d};
     for (void* p : ps) if (p) cudaFree(p);
     if (S->ev0) cudaEventDestroy(S->ev0);
     if (S->ev1) cudaEventDestroy(S->ev1);
@@ -1779,9 +1795,8 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     S->tm = S->desc.tally_mode;
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
     {
-        const int nsdShared = sizeof(SdomD<R>) * D.sd.size() <= SD_SHARED_MAX ? (int)D.sd.size() : 0;
-        SmemLayout L;
-        L.init<R>((int)m.nw, (int)m.np, nsdShared, S->rows, (int)D.cols, S->tm == TM_SHARED);
+        const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
+                                             S->tm == TM_SHARED);
         S->smem = L.total;
     }
     if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");

@@ -92,6 +92,15 @@ struct Params {
     const unsigned long long* live_in;
     unsigned long long* live_out;
     unsigned long long cap;
+    // static schedule: block b of the (fixed) grid owns the slots
+    // [b regCap, (b + 1) regCap) of each half; its live phonons are the
+    // regIn[2b] slots from the front of its region (next event inside
+    // this window) and the regIn[2b + 1] slots at its back (no event in
+    // it). Survivors go to the same region of the other half, counted in
+    // regOut.
+    unsigned int* regIn;
+    unsigned int* regOut;
+    long long regCap;
     // fixed-point quantum of the per-block shared tally and of the
     // per-thread checksums, per row
     R tqinv[4];

@@ -8,9 +8,12 @@
 // or the relaxation-time scatter (Walker, mc_walker.cuh).
 //
 //   k_emit / k_emit_batch   emission (event 0 of each phonon's stream)
-//   k_advance               static: one phonon per thread per pass; survivors
-//                           compacted by warp ballot to the two ends of the
-//                           other half of the state
+//   k_advance               static: each block streams its region of the
+//                           state through shared memory by bulk copies (one
+//                           producer warp), one phonon per consumer thread;
+//                           survivors go to the region's two ends in the
+//                           other half (next event inside the next window
+//                           at the front)
 //   k_advance_dyn           dynamic: warps refill idle lanes from a
 //                           block-owned queue; state written back in place
 //   k_advance_batch         dynamic, over many instances in one launch
@@ -18,6 +21,7 @@
 //   k_difprefix             global difference arrays -> field (batched)
 #pragma once
 
+#include "mc_async.cuh"
 #include "mc_walker.cuh"
 
 namespace mcg {
@@ -27,9 +31,8 @@ namespace mcg {
 template <typename R, int TM>
 __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned char* smraw) {
     const int nt = P.nw * P.np;
-    const int nsdShared = (size_t)P.nsd * sizeof(SdomD<R>) <= SD_SHARED_MAX ? P.nsd : 0;
-    SmemLayout L;
-    L.init<R>(P.nw, P.np, nsdShared, P.rows, P.cols, TM == TM_SHARED);
+    const int nsdShared = P.nsd;
+    const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED);
     R* vel = reinterpret_cast<R*>(smraw + L.vel);
     R* vt = reinterpret_cast<R*>(smraw + L.vt);
     unsigned long long* wthr = reinterpret_cast<unsigned long long*>(smraw + L.wthr);
@@ -116,7 +119,7 @@ __device__ __forceinline__ void flushSharedField(const InstD<R>& I, double* dst)
     for (int r = 0; r < 4; ++r) {
         long long x = part[r];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xFFFFFFFFu, x, o);
-        if (lane == 0 && x != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g_blk.csum[r]), (unsigned long long)x);
+        if (lane == 0 && x != 0) sharedAdd64(&g_blk.csum[r], x);
     }
 }
 
@@ -143,6 +146,9 @@ __global__ void __launch_bounds__(256) k_emit(Params<R> P) {
     __syncthreads();
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= P.nemit) return;
+    // static schedule: the phonons of each block region start at its front
+    if (P.regIn != nullptr && n % P.regCap == 0)
+        P.regIn[2 * (n / P.regCap)] = (unsigned)min(P.regCap, P.nemit - n);
     Rng<REPLAY> g;
     g.init(P.key0, P.key1, (uint32_t)n, &P);
     Phn<R> ph;
@@ -209,68 +215,199 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 }
 
 // ----------------------------------------------------------------- advance
-// Static kernel: one phonon per thread per pass of a grid-stride loop;
-// survivors are compacted to the two ends of the other half of the
-// ping-pong state (front: next event inside the next window).
+// Static kernel: a persistent, warp-specialised stream over the block's
+// region of the state.
+//
+// Block b owns slots [b C, (b + 1) C) of both halves of the state (C =
+// regCap). Its live phonons sit at the two ends of its region in the input
+// half: regIn[2b] at the front (their next event falls inside this
+// window), regIn[2b + 1] at the back (no event in it). The block's last
+// warp is the producer: one lane walks the front range, then the back
+// range, in tiles of T = blockDim.x - 32 slots and issues cp.async.bulk
+// copies of each tile (48 B per phonon in FP32: three 16-byte words, one
+// copy per word array) into one of STATIC_STAGES shared-memory stages,
+// completing on the stage's mbarrier. The other T threads (the consumers)
+// each take one phonon of a tile out of the stage, release the stage at
+// once (so the next copy overlaps their work), advance the phonon through
+// the window, and write the survivors to the block's region of the output
+// half: phonons whose next event falls inside the next window from the
+// front, the others from the back, positions taken from two shared-memory
+// counters per warp ballot. Stopped phonons are dropped. The warps of a
+// block never wait for one another, warps see phonons of one kind (events
+// first, then plain flights), and no global atomic is involved. Step and
+// event counts are summed per thread and added to the block's counters
+// once, at the end.
+constexpr int STATIC_STAGES = 2;
+constexpr int STATIC_PRODUCER_THREADS = 32;
+constexpr int STATIC_MAX_THREADS = 256 + STATIC_PRODUCER_THREADS;
+constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
+// bounded waits: a bulk copy lands within microseconds; the producer may
+// wait for consumers in the middle of a long window much longer
+constexpr uint64_t STATIC_COPY_WAIT_NS = 2000000000ull;
+constexpr uint64_t STATIC_STAGE_WAIT_NS = 60000000000ull;
+
+template <typename R>
+__host__ __device__ inline size_t staticStageBytes(int tile) {
+    return (size_t)tile * (2 * sizeof(typename Vec4<R>::T) + sizeof(uint4));
+}
+// offset of the first stage after the single-instance layout
+__host__ __device__ inline size_t staticStageOffset(size_t layoutTotal) {
+    return (layoutTotal + 127) & ~(size_t)127;
+}
+
 template <typename R, bool REPLAY, bool LOG, int TM>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2) k_advance(Params<R> P) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ unsigned sWarp[2][8];
-    __shared__ unsigned long long sBase[2];
+__global__ void __launch_bounds__(STATIC_MAX_THREADS, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
+k_advance(Params<R> P) {
+    using V4 = typename Vec4<R>::T;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    __shared__ uint64_t barFull[STATIC_STAGES], barEmpty[STATIC_STAGES];
+    __shared__ unsigned sCnt[STATIC_STAGES];
+    __shared__ unsigned sOut[2];
+    __shared__ int sStop;
+    const int T = (int)blockDim.x - STATIC_PRODUCER_THREADS;
+    const int nCw = T >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     InstD<R>* I = stageTables<R, TM>(P, smraw);
+    ParamView<R, TM> V;
+    V.init(P, smraw);
+    unsigned char* stage0;
+    {
+        const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED);
+        stage0 = smraw + staticStageOffset(L.total);
+    }
+    const size_t sbytes = staticStageBytes<R>(T);
+    const long long C = P.regCap;
+    const long long rbase = (long long)blockIdx.x * C;
     blkZero();
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STATIC_STAGES; ++s) {
+            mbarInit(&barFull[s], 1);
+            mbarInit(&barEmpty[s], (uint32_t)nCw);
+        }
+        sStop = 0;
+        sOut[0] = sOut[1] = 0u;
+        mbarInitFence();
+    }
     __syncthreads();
 
-    const unsigned long long nf = P.live_in[0], nb = P.live_in[1];
-    const unsigned long long n = nf + nb;
-    Window<R> W;
-    W.init(P);
-    const int lane = threadIdx.x & 31;
-
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n;
-         base += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long i = base + threadIdx.x;
-        bool alive = false, soon = false;
-        typename Vec4<R>::T A0, A1;
-        uint4 A2;
-        if (i < n) {
-            const unsigned long long slot = i < nf ? i : P.cap - nb + (i - nf);
-            ld4(P.P0in + slot, A0);
-            ld4(P.P1in + slot, A1);
-            A2 = __ldcs(P.P2in + slot);
-            Walker<R, REPLAY, LOG, TM> wk;
-            wk.load(P, I, W, A0, A1, A2);
-            while (!wk.iterate(P, W)) {}
-            alive = wk.finish(P, W);
-            soon = wk.tnext < W.next;
-            if (alive) wk.pack(A0, A1, A2);
-        }
-        // fused compaction into two ends: warp counts scanned in shared
-        // memory, one atomic per block pass and end
-        const unsigned mf = __ballot_sync(0xFFFFFFFFu, alive && soon);
-        const unsigned mb = __ballot_sync(0xFFFFFFFFu, alive && !soon);
-        const int warp = threadIdx.x >> 5;
-        if (lane == 0) { sWarp[0][warp] = (unsigned)__popc(mf); sWarp[1][warp] = (unsigned)__popc(mb); }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned tf = 0, tb = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-                const unsigned f = sWarp[0][w], b = sWarp[1][w];
-                sWarp[0][w] = tf; sWarp[1][w] = tb;
-                tf += f; tb += b;
+    if (warp == nCw) {
+        // ---------------------------------------------------- producer
+        if (lane == 0) {
+            // the input counts, clamped to the region
+            const unsigned long long nF = min((unsigned long long)P.regIn[2 * blockIdx.x], (unsigned long long)C);
+            const unsigned long long nB =
+                min((unsigned long long)P.regIn[2 * blockIdx.x + 1], (unsigned long long)C - nF);
+            const long long tF = ((long long)nF + T - 1) / T, tB = ((long long)nB + T - 1) / T;
+            const uint32_t perPhonon = (uint32_t)(2 * sizeof(V4) + sizeof(uint4));
+            int j = 0;
+            for (;; ++j) {
+                const int s = j % STATIC_STAGES;
+                const uint32_t use = (uint32_t)(j / STATIC_STAGES);
+                if (use > 0 && !mbarWait(&barEmpty[s], (use - 1) & 1u, STATIC_STAGE_WAIT_NS, &sStop)) {
+                    atomicOr(P.status, (unsigned)S_TIMEOUT);
+                    sStop = 1;
+                    break;
+                }
+                if (j >= tF + tB) {
+                    sCnt[s] = STATIC_END;
+                    mbarArrive(&barFull[s]);
+                    ++j;
+                    break;
+                }
+                long long src;
+                unsigned cnt;
+                if (j < tF) {
+                    src = rbase + (long long)j * T;
+                    cnt = (unsigned)min((long long)T, (long long)nF - (long long)j * T);
+                } else {
+                    const long long k = j - tF;
+                    src = rbase + C - (long long)nB + k * T;
+                    cnt = (unsigned)min((long long)T, (long long)nB - k * T);
+                }
+                sCnt[s] = cnt;
+                unsigned char* st = stage0 + (size_t)s * sbytes;
+                mbarArriveExpectTx(&barFull[s], cnt * perPhonon);
+                bulkLoad(st, P.P0in + src, cnt * (uint32_t)sizeof(V4), &barFull[s]);
+                bulkLoad(st + (size_t)T * sizeof(V4), P.P1in + src, cnt * (uint32_t)sizeof(V4), &barFull[s]);
+                bulkLoad(st + (size_t)T * 2 * sizeof(V4), P.P2in + src, cnt * (uint32_t)sizeof(uint4), &barFull[s]);
             }
-            sBase[0] = tf ? atomicAdd(&P.live_out[0], (unsigned long long)tf) : 0ull;
-            sBase[1] = tb ? atomicAdd(&P.live_out[1], (unsigned long long)tb) : 0ull;
+            // every copy this block issued has landed before it exits
+            const int issued = j;
+            for (int s = 0; s < STATIC_STAGES && s < issued; ++s) {
+                const int last = issued - 1 - ((issued - 1 - s) % STATIC_STAGES);
+                if (!mbarWait(&barFull[s], (uint32_t)(last / STATIC_STAGES) & 1u, STATIC_COPY_WAIT_NS))
+                    atomicOr(P.status, (unsigned)S_TIMEOUT);
+            }
         }
-        __syncthreads();
-        const unsigned long long bf = sBase[0] + sWarp[0][warp], bb = sBase[1] + sWarp[1][warp];
-        if (alive) {
-            const unsigned lt = (1u << lane) - 1u;
-            const unsigned long long o = soon ? bf + __popc(mf & lt) : P.cap - 1 - (bb + __popc(mb & lt));
-            st4(P.P0out + o, A0);
-            st4(P.P1out + o, A1);
-            __stcs(P.P2out + o, A2);
+    } else {
+        // ---------------------------------------------------- consumers
+        Window<R> W;
+        W.init(P);
+        const unsigned lt = (1u << lane) - 1u;
+        unsigned long long nSteps = 0, nEvents = 0;
+        for (int j = 0;; ++j) {
+            const int s = j % STATIC_STAGES;
+            const uint32_t use = (uint32_t)(j / STATIC_STAGES);
+            if (!mbarWait(&barFull[s], use & 1u, STATIC_COPY_WAIT_NS, &sStop)) {
+                if (lane == 0) { atomicOr(P.status, (unsigned)S_TIMEOUT); sStop = 1; }
+                break;
+            }
+            const unsigned cnt = sCnt[s];
+            if (cnt == STATIC_END) break;
+            const int i = threadIdx.x;
+            V4 A0, A1;
+            uint4 A2;
+            const bool have = i < (int)cnt;
+            if (have) {
+                const unsigned char* st = stage0 + (size_t)s * sbytes;
+                A0 = reinterpret_cast<const V4*>(st)[i];
+                A1 = reinterpret_cast<const V4*>(st + (size_t)T * sizeof(V4))[i];
+                A2 = reinterpret_cast<const uint4*>(st + (size_t)T * 2 * sizeof(V4))[i];
+            }
+            __syncwarp();
+            if (lane == 0) mbarArrive(&barEmpty[s]);
+            if (__ballot_sync(0xFFFFFFFFu, have) == 0) continue;
+            bool alive = false, soon = false;
+            if (have) {
+                Walker<R, REPLAY, LOG, TM, ParamView<R, TM>> wk;
+                wk.load(P, V, W, A0, A1, A2);
+                while (!wk.iterate(P, W)) {}
+                alive = wk.finishInto(P, W, nSteps, nEvents);
+                soon = wk.tnext < W.next;
+                if (alive) wk.pack(A0, A1, A2);
+            }
+            const unsigned mf = __ballot_sync(0xFFFFFFFFu, alive && soon);
+            const unsigned mb = __ballot_sync(0xFFFFFFFFu, alive && !soon);
+            unsigned bf = 0, bb = 0;
+            if (lane == 0) {
+                if (mf) bf = atomicAdd(&sOut[0], (unsigned)__popc(mf));
+                if (mb) bb = atomicAdd(&sOut[1], (unsigned)__popc(mb));
+            }
+            bf = __shfl_sync(0xFFFFFFFFu, bf, 0);
+            bb = __shfl_sync(0xFFFFFFFFu, bb, 0);
+            if (alive) {
+                const long long o = soon ? rbase + bf + __popc(mf & lt) : rbase + C - 1 - (bb + __popc(mb & lt));
+                st4(P.P0out + o, A0);
+                st4(P.P1out + o, A1);
+                __stcs(P.P2out + o, A2);
+            }
         }
+        // per-thread sums -> block counters
+        for (int o = 16; o > 0; o >>= 1) {
+            nSteps += __shfl_down_sync(0xFFFFFFFFu, nSteps, o);
+            nEvents += __shfl_down_sync(0xFFFFFFFFu, nEvents, o);
+        }
+        if (lane == 0) {
+            if (nSteps) sharedAdd64(&g_blk.cnt[C_PHONON_STEPS], nSteps);
+            if (nEvents) sharedAdd64(&g_blk.cnt[C_EVENTS], nEvents);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // a block that gave up leaves nothing for later launches
+        const bool ok = *reinterpret_cast<volatile int*>(&sStop) == 0;
+        P.regOut[2 * blockIdx.x] = ok ? sOut[0] : 0u;
+        P.regOut[2 * blockIdx.x + 1] = ok ? sOut[1] : 0u;
     }
     closeBlock<R, TM>(P, *I);
 }
@@ -284,13 +421,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32
 // host compacts).
 constexpr int REFILL = 8;
 
-template <typename R, bool REPLAY, bool LOG, int TM>
+template <typename R, bool REPLAY, bool LOG, int TM, typename IA>
 __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
                                             unsigned long long qbeg, unsigned long long qend,
-                                            const InstD<R>* I, const Window<R>& W) {
+                                            const IA& I, const Window<R>& W) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    Walker<R, REPLAY, LOG, TM> wk;
+    Walker<R, REPLAY, LOG, TM, IA> wk;
     bool have = false;
     unsigned long long slot = 0;
     bool drained = qbeg >= qend;
@@ -359,7 +496,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
     const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
     const unsigned long long qend = min(qbeg + chunk, n);
-    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, I, W);
+    ParamView<R, TM> V;
+    V.init(P, smraw);
+    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, V, W);
     closeBlock<R, TM>(P, *I);
 }
 
@@ -460,7 +599,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
         }
         __syncthreads();
         dynamicLoop<R, false, false, TM_AUTO>(P, P.segNext + sg, (unsigned long long)S.beg,
-                                              (unsigned long long)S.end, I, W);
+                                              (unsigned long long)S.end, InstView<R>{I}, W);
         __syncthreads();
         flushBinding<R>(*I, S.group);
         __syncthreads();

@@ -17,7 +17,8 @@ static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t sm
     auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
-    fn<<<grid, block, smem, s>>>(p);
+    // the static kernel adds its producer warp to the `block` consumers
+    fn<<<grid, DYN ? block : block + STATIC_PRODUCER_THREADS, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -26,7 +27,9 @@ static int occOne(int block, size_t smem) {
     auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
     if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, DYN ? block : block + STATIC_PRODUCER_THREADS, smem) !=
+        cudaSuccess)
+        return 0;
     return nb;
 }
 

@@ -35,6 +35,7 @@ enum Status {
     S_REPLAY_EXHAUSTED = 1,
     S_NONFINITE = 2,
     S_BAD_CELL = 4,
+    S_TIMEOUT = 8,  // a bounded device-side wait gave up (results discarded)
 };
 
 // One face of a Parallelepiped subdomain in reduced coordinates: face f

@@ -28,7 +28,18 @@ struct SmemLayout {
     }
 };
 
-// Subdomain images staged in shared memory up to this many bytes.
+// Shared layout of a single-instance advance launch (tables, every
+// subdomain image, descriptor, fixed-point field when the tally is shared);
+// the host sizes the launch with the same function.
+template <typename R>
+__host__ __device__ inline SmemLayout singleLayout(int nw, int np, int nsd, int rows, int cols, bool sharedTally) {
+    SmemLayout L;
+    L.init<R>(nw, np, nsd, rows, cols, sharedTally);
+    return L;
+}
+
+// Subdomain images a batched block stages in shared memory up to this many
+// bytes.
 constexpr size_t SD_SHARED_MAX = 32 * 1024;
 
 // Shared memory of a batched block: the current instance's descriptor and
@@ -78,10 +89,10 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 #ifndef MC_MIN_BLOCKS_F32
 #define MC_MIN_BLOCKS_F32 3
 #endif
-// The one-phonon-per-thread static kernel waits on its state loads and is
-// compiled for four resident blocks.
+// Resident blocks of the static kernel (256 consumer threads and one
+// producer warp) per SM: three, which its shared-memory stages also fit.
 #ifndef MC_MIN_BLOCKS_STATIC_F32
-#define MC_MIN_BLOCKS_STATIC_F32 4
+#define MC_MIN_BLOCKS_STATIC_F32 3
 #endif
 
 template <typename R>
@@ -115,6 +126,24 @@ __device__ __forceinline__ double toDouble(float v) {
 }
 __device__ __forceinline__ double toDouble(double v) { return v; }
 
+// Exact 64-bit add into a word of shared memory with native 32-bit atomics
+// (a 64-bit add on a shared address compiles to a compare-and-swap loop):
+// the low half takes the low 32 bits of v, and the high half the sign
+// extension of v plus the carry out of the low half, skipped when they
+// cancel (always, for the |v| < 2^31 of an FP32 flight, unless the low half
+// wraps). The two halves are consistent again once every add has landed,
+// which the callers' barriers ensure before any read.
+__device__ __forceinline__ void sharedAdd64(long long* p, long long v) {
+    unsigned* w = reinterpret_cast<unsigned*>(p);
+    const unsigned lo = (unsigned)(unsigned long long)v;
+    const unsigned old = atomicAdd(w, lo);
+    const int hi = (int)(v >> 32) + ((old + lo) < old ? 1 : 0);
+    if (hi != 0) atomicAdd(reinterpret_cast<int*>(w + 1), hi);
+}
+__device__ __forceinline__ void sharedAdd64(unsigned long long* p, unsigned long long v) {
+    sharedAdd64(reinterpret_cast<long long*>(p), (long long)v);
+}
+
 // Per-block accumulators in shared memory: the launch counters and the
 // rows' fixed-point checksums of the flights whose field amount does not go
 // into the block's shared field (those are summed from it at the end).
@@ -130,7 +159,7 @@ __device__ __forceinline__ void blkCount(int c, unsigned n) {
     const unsigned act = __activemask();
     const unsigned peers = __match_any_sync(act, c);
     const unsigned tot = __reduce_add_sync(peers, n);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && tot) atomicAdd(&g_blk.cnt[c], (unsigned long long)tot);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && tot) sharedAdd64(&g_blk.cnt[c], (unsigned long long)tot);
 }
 
 // Add v to the block checksum of row r, summed first over the lanes that
@@ -144,7 +173,7 @@ __device__ __forceinline__ void blkCsum(int r, long long v) {
     const int s2 = __reduce_add_sync(act, (int)(v >> 44));
     if ((int)(threadIdx.x & 31) == __ffs(act) - 1) {
         const long long t = (long long)s0 + (long long)s1 * (1LL << 22) + (long long)s2 * (1LL << 44);
-        if (t != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&g_blk.csum[r]), (unsigned long long)t);
+        if (t != 0) sharedAdd64(&g_blk.csum[r], t);
     }
 }
 
@@ -154,44 +183,122 @@ __device__ __forceinline__ void blkZero() {
     for (int i = threadIdx.x; i < (int)(sizeof(BlockAcc) / 8); i += blockDim.x) z[i] = 0ull;
 }
 
-// Field accumulation for one flight of one instance.
-template <typename R, int TM>
-struct Tally {
+// Instance data of the advance loop, read through a view. A batched launch
+// reads the descriptor of the phonon's instance that its block staged in
+// shared memory (InstView). A single-instance launch (ParamView) takes the
+// launch constants from the kernel parameters and its tables, subdomain
+// images and fixed-point field from its own shared-memory layout, at
+// addresses the compiler knows to be shared: no pointer is loaded from
+// memory on the way, so nothing has to be reloaded after a tally atomic.
+template <typename R>
+struct InstView {
     const InstD<R>* I;
+    __device__ __forceinline__ int rows() const { return I->rows; }
+    __device__ __forceinline__ int cols() const { return I->cols; }
+    __device__ __forceinline__ int problem() const { return I->problem; }
+    __device__ __forceinline__ int nw() const { return I->nw; }
+    __device__ __forceinline__ int np() const { return I->np; }
+    __device__ __forceinline__ long long* tal() const { return I->tal; }
+    __device__ __forceinline__ long long* dif() const { return I->dif; }
+    __device__ __forceinline__ double* tally() const { return I->tally; }
+    __device__ __forceinline__ double* gdif() const { return I->gdif; }
+    __device__ __forceinline__ int groups() const { return I->groups; }
+    __device__ __forceinline__ long long gstride() const { return I->gstride; }
+    __device__ __forceinline__ int flags() const { return I->flags; }
+    __device__ __forceinline__ R tqinv(int r) const { return I->tqinv[r]; }
+    __device__ __forceinline__ const SdomD<R>* sd() const { return I->sd; }
+    __device__ __forceinline__ const R* vel() const { return I->vel; }
+    __device__ __forceinline__ const R* vt() const { return I->vt; }
+    __device__ __forceinline__ const unsigned long long* wthr() const { return I->wthr; }
+    __device__ __forceinline__ const uint16_t* wguide() const { return I->wguide; }
+    __device__ __forceinline__ const unsigned long long* pthr() const { return I->pthr; }
+    __device__ __forceinline__ uint32_t key0() const { return I->key0; }
+    __device__ __forceinline__ uint32_t key1() const { return I->key1; }
+    __device__ __forceinline__ long long maxscat() const { return I->maxscat; }
+    __device__ __forceinline__ long long maxloop() const { return I->maxloop; }
+};
+
+// Single-instance view over singleLayout().
+template <typename R, int TM>
+struct ParamView {
+    const Params<R>* P;
+    unsigned char* sm;
+    int oVt, oWthr, oGuide, oSd, oTal;  // the vel table sits at offset 0
+    __device__ __forceinline__ void init(const Params<R>& p, unsigned char* smraw) {
+        P = &p;
+        sm = smraw;
+        const SmemLayout L = singleLayout<R>(p.nw, p.np, p.nsd, p.rows, p.cols, TM == TM_SHARED);
+        oVt = (int)L.vt; oWthr = (int)L.wthr; oGuide = (int)L.guide; oSd = (int)L.sd; oTal = (int)L.tal;
+    }
+    __device__ __forceinline__ int rows() const { return P->rows; }
+    __device__ __forceinline__ int cols() const { return P->cols; }
+    __device__ __forceinline__ int problem() const { return P->problem; }
+    __device__ __forceinline__ int nw() const { return P->nw; }
+    __device__ __forceinline__ int np() const { return P->np; }
+    __device__ __forceinline__ long long* tal() const {
+        return TM == TM_SHARED ? reinterpret_cast<long long*>(sm + oTal) : nullptr;
+    }
+    __device__ __forceinline__ long long* dif() const {
+        return reinterpret_cast<long long*>(sm + oTal) + (size_t)P->rows * P->cols;
+    }
+    __device__ __forceinline__ double* tally() const { return P->tally; }
+    __device__ __forceinline__ double* gdif() const { return nullptr; }
+    __device__ __forceinline__ int groups() const { return 1; }
+    __device__ __forceinline__ long long gstride() const { return 0; }
+    __device__ __forceinline__ int flags() const { return 0; }
+    __device__ __forceinline__ R tqinv(int r) const { return P->tqinv[r]; }
+    __device__ __forceinline__ const SdomD<R>* sd() const { return reinterpret_cast<const SdomD<R>*>(sm + oSd); }
+    __device__ __forceinline__ const R* vel() const { return reinterpret_cast<const R*>(sm); }
+    __device__ __forceinline__ const R* vt() const { return reinterpret_cast<const R*>(sm + oVt); }
+    __device__ __forceinline__ const unsigned long long* wthr() const {
+        return reinterpret_cast<const unsigned long long*>(sm + oWthr);
+    }
+    __device__ __forceinline__ const uint16_t* wguide() const { return reinterpret_cast<const uint16_t*>(sm + oGuide); }
+    __device__ __forceinline__ const unsigned long long* pthr() const { return P->pthr; }
+    __device__ __forceinline__ uint32_t key0() const { return P->key0; }
+    __device__ __forceinline__ uint32_t key1() const { return P->key1; }
+    __device__ __forceinline__ long long maxscat() const { return P->maxscat; }
+    __device__ __forceinline__ long long maxloop() const { return P->maxloop; }
+};
+
+// Field accumulation for one flight of one instance.
+template <typename R, int TM, typename IA>
+struct Tally {
+    IA V;
     long long goff;  // offset of the phonon's field copy (global layouts)
     // amount per metre of flight, rows entries: Temp sign/v; Flux sign*d
     R rho[4];
 
-    __device__ __forceinline__ int rows() const { return I->rows; }
+    __device__ __forceinline__ int rows() const { return V.rows(); }
     __device__ __forceinline__ bool shared() const {
-        return TM == TM_SHARED || (TM == TM_AUTO && I->tal != nullptr);
+        return TM == TM_SHARED || (TM == TM_AUTO && V.tal() != nullptr);
     }
     // fixed-point amount of row r for path length t
-    __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * I->tqinv[r])); }
+    __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * V.tqinv(r))); }
     // a flight's amount that does not enter the shared field
     __device__ __forceinline__ void csumAdd(int r, long long v) const { blkCsum(r, v); }
     __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&I->tal[r * I->cols + col]), (unsigned long long)v);
+        sharedAdd64(&V.tal()[r * V.cols() + col], v);
     }
     __device__ __forceinline__ void atomRange(int r, int c0, int c1, long long v) const {
-        unsigned long long* d = reinterpret_cast<unsigned long long*>(I->dif + r * (I->cols + 1));
-        atomicAdd(d + c0, (unsigned long long)v);
-        atomicAdd(d + c1, (unsigned long long)(-v));
+        long long* d = V.dif() + r * (V.cols() + 1);
+        sharedAdd64(d + c0, v);
+        sharedAdd64(d + c1, -v);
     }
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < I->rows) atomicAdd(&I->tally[goff + (size_t)col * I->rows + r], toDouble(rho[r] * t));
+            if (r < V.rows()) atomicAdd(&V.tally()[goff + (size_t)col * V.rows() + r], toDouble(rho[r] * t));
     }
     // interior cells [c0, c1) of a 1-D walk (stride 1) each with path t
     __device__ __forceinline__ void addGlobalRange(int c0, int c1, R t) const {
-        if (I->gdif) {
+        if (V.gdif()) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                if (r < I->rows) {
+                if (r < V.rows()) {
                     const double v = toDouble(rho[r] * t);
-                    atomicAdd(&I->gdif[goff + (size_t)r * (I->cols + 1) + c0], v);
-                    atomicAdd(&I->gdif[goff + (size_t)r * (I->cols + 1) + c1], -v);
+                    atomicAdd(&V.gdif()[goff + (size_t)r * (V.cols() + 1) + c0], v);
+                    atomicAdd(&V.gdif()[goff + (size_t)r * (V.cols() + 1) + c1], -v);
                 }
             }
         } else {
@@ -230,9 +337,9 @@ __device__ __forceinline__ void moveAxis(Phn<R>& ph, const SdomD<R>& S, int k, R
 // interior cells through the difference array. In the shared layout the
 // flight's whole fixed-point amount V is computed once and the last cell
 // takes the integer remainder, so the cells add up to V exactly.
-template <typename R, int TM, int K>
+template <typename R, int TM, int K, typename IA>
 __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                      Tally<R, TM>& T) {
+                                      Tally<R, TM, IA>& T) {
     const int cb = S.colbeg;
     const int b = ph.idx[K];
     const int n = S.shape[K];
@@ -284,10 +391,10 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
 // Flight of path length s from the current cell, tallied cell by cell
 // (Field::accumulate, montecarlo/field.cpp:160-288, as a cell walk); adds
 // the flight's fixed-point amount to the checksums.
-template <typename R, int TM>
+template <typename R, int TM, typename IA>
 __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                   Tally<R, TM>& T) {
-    const int acc = (TM == TM_AUTO && (T.I->flags & IF_NO_FIELD)) ? -2 : S.accum;
+                                   Tally<R, TM, IA>& T) {
+    const int acc = (TM == TM_AUTO && (T.V.flags() & IF_NO_FIELD)) ? -2 : S.accum;
     const int cb = S.colbeg;
     if (acc < 0) {
         // a single field column (or none): move only
@@ -303,9 +410,9 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
         return;
     }
-    if (acc == 0) { fly1d<R, TM, 0>(ph, S, a, ia, s, T); return; }
-    if (acc == 1) { fly1d<R, TM, 1>(ph, S, a, ia, s, T); return; }
-    if (acc == 2) { fly1d<R, TM, 2>(ph, S, a, ia, s, T); return; }
+    if (acc == 0) { fly1d<R, TM, 0, IA>(ph, S, a, ia, s, T); return; }
+    if (acc == 1) { fly1d<R, TM, 1, IA>(ph, S, a, ia, s, T); return; }
+    if (acc == 2) { fly1d<R, TM, 2, IA>(ph, S, a, ia, s, T); return; }
     // 2-D / 3-D: walk the cells (Amanatides-Woo); a shared field gives the
     // checksum as the sum of its cells, a global one the flight's amount
     if (!T.shared()) {
@@ -482,10 +589,10 @@ constexpr uint32_t PROP_DEAD = 1u << 25;
 // from it. iterate() runs one loop iteration of montecarlo/problem.cpp:401-435
 // (flight to the next event or to the end of the window, its tally, the
 // event); finish() closes the phonon's window.
-template <typename R, bool REPLAY, bool LOG, int TM>
+template <typename R, bool REPLAY, bool LOG, int TM, typename IA>
 struct Walker {
     Phn<R> ph;
-    const InstD<R>* I;
+    IA I;
     const SdomD<R>* S;
     R a[3], ia[3];
     R v, iv;
@@ -497,7 +604,7 @@ struct Walker {
     // is set up afresh at each event from (key, phonon id, event index)
     typename ReplayState<REPLAY>::T rg;
 
-    __device__ __forceinline__ void load(const Params<R>& P, const InstD<R>* inst, const Window<R>& W,
+    __device__ __forceinline__ void load(const Params<R>& P, const IA& inst, const Window<R>& W,
                                          const typename Vec4<R>::T& A0, const typename Vec4<R>::T& A1,
                                          const uint4& A2) {
         I = inst;
@@ -510,11 +617,11 @@ struct Walker {
         ph.neg = (A2.y >> 24) & 1u;
         ph.nscat = A2.z;
         ph.nloop = A2.w;
-        if constexpr (REPLAY) rg.init(I->key0, I->key1, ph.id, &P);
+        if constexpr (REPLAY) rg.init(I.key0(), I.key1(), ph.id, &P);
         budget = W.len;
-        S = &I->sd[ph.s];
+        S = &I.sd()[ph.s];
         reducedVel(*S, ph.d, a, ia);
-        v = I->vel[ph.w * I->np + ph.p];
+        v = I.vel()[ph.w * I.np() + ph.p];
         iv = R(1) / v;
         stop = 0;
         nev = 0;
@@ -547,17 +654,17 @@ struct Walker {
         const bool event = tev <= budget;
         const R s = event ? sev : budget * v;
         // tally amounts per metre (montecarlo/problem.cpp:473-544)
-        Tally<R, TM> T;
-        T.I = I;
+        Tally<R, TM, IA> T;
+        T.V = I;
         // field copy of this phonon (batch means), global fields only
-        T.goff = (TM != TM_SHARED && I->groups > 1) ? (long long)(ph.id % (uint32_t)I->groups) * I->gstride : 0;
+        T.goff = (TM != TM_SHARED && I.groups() > 1) ? (long long)(ph.id % (uint32_t)I.groups()) * I.gstride() : 0;
         const R sg = ph.neg ? R(-1) : R(1);
-        if (I->problem == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
-        else if (I->problem == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
+        if (I.problem() == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
+        else if (I.problem() == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
         else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
         const int sBefore = ph.s;
         int cellEnd = 0;
-        fly<R, TM>(ph, *S, a, ia, s, T);
+        fly<R, TM, IA>(ph, *S, a, ia, s, T);
         if (LOG) cellEnd = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
         ph.scatNext -= s;
         if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
@@ -581,7 +688,7 @@ struct Walker {
         if (LOG) physPos(*S, ph, xe);
         Rng<REPLAY> g;
         if constexpr (REPLAY) g = rg;
-        else g.init(I->key0, I->key1, ph.id, &P);
+        else g.init(I.key0(), I.key1(), ph.id, &P);
         g.setEvent(ph.nloop + 1);
         if (face >= 0) {
             const FaceD<R>& F = S->f[face];
@@ -617,7 +724,7 @@ struct Walker {
                     // coordinates, move onto the paired face (selects on
                     // every axis: no indexed writes into the phonon state)
                     ph.s = F.to;
-                    S = &I->sd[ph.s];
+                    S = &I.sd()[ph.s];
                     const int tf = F.toface;
                     const int tax = tf >= 3 ? tf - 3 : tf;
                     const bool up = tf >= 3;
@@ -633,7 +740,7 @@ struct Walker {
                     rotate(F.A, u, u2);
                     for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
                     ph.s = F.to;
-                    S = &I->sd[ph.s];
+                    S = &I.sd()[ph.s];
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         if (F.toface == j) u2[j] = R(0);
@@ -658,13 +765,13 @@ struct Walker {
         } else {
             // Material::scatter (montecarlo/material.cpp:298-303)
             uint32_t x1 = g.next(), x2 = g.next();
-            ph.w = searchGuided(I->wthr, I->wguide, I->nw, x1);
-            ph.p = searchBranch(I->pthr + ph.w * I->np, I->np, x2);
+            ph.w = searchGuided(I.wthr(), I.wguide(), I.nw(), x1);
+            ph.p = searchBranch(I.pthr() + ph.w * I.np(), I.np(), x2);
             drawIso<R>(g, ph.d);
             normalize(ph.d);
             ph.nscat++;
-            ph.scatNext = drawScatNext<R>(g, I->vt[ph.w * I->np + ph.p]);
-            v = I->vel[ph.w * I->np + ph.p];
+            ph.scatNext = drawScatNext<R>(g, I.vt()[ph.w * I.np() + ph.p]);
+            v = I.vel()[ph.w * I.np() + ph.p];
             iv = R(1) / v;
             blkCount(C_SCATTERS, 1);
         }
@@ -677,8 +784,8 @@ struct Walker {
             if (g.exhausted()) { stop = C_REPLAY_EXHAUSTED; return true; }
         }
         if (stop) return true;
-        if ((long long)ph.nscat >= I->maxscat) { stop = C_MAXSCAT; return true; }
-        if ((long long)ph.nloop >= I->maxloop) { stop = C_MAXLOOP; return true; }
+        if ((long long)ph.nscat >= I.maxscat()) { stop = C_MAXSCAT; return true; }
+        if ((long long)ph.nloop >= I.maxloop()) { stop = C_MAXLOOP; return true; }
         if (nev >= MAX_EVENTS_PER_LAUNCH) { stop = C_BAD; return true; }
         reducedVel(*S, ph.d, a, ia);
         return false;
@@ -687,6 +794,27 @@ struct Walker {
     // the phonon's window is over: count its steps, events and stop
     // reason; returns true if it stays alive
     __device__ __forceinline__ bool finish(const Params<R>& P, const Window<R>& W) {
+        int st;
+        const bool alive = close(P, W, st);
+        blkCount(C_PHONON_STEPS, (unsigned)st);
+        blkCount(C_EVENTS, (unsigned)nev);
+        return alive;
+    }
+
+    // as finish(), with the dt-steps and events of the window added to the
+    // caller's per-thread sums instead of the block counters
+    __device__ __forceinline__ bool finishInto(const Params<R>& P, const Window<R>& W, unsigned long long& steps,
+                                               unsigned long long& events) {
+        int st;
+        const bool alive = close(P, W, st);
+        steps += (unsigned)st;
+        events += (unsigned)nev;
+        return alive;
+    }
+
+    // close the window: `st` = the dt-steps the phonon was alive at the
+    // start of, stop reason counted and flagged; true if it stays alive
+    __device__ __forceinline__ bool close(const Params<R>& P, const Window<R>& W, int& stOut) {
         if constexpr (REPLAY) rg.save();
         int st = W.keff;
         if (stop == 0) {
@@ -703,8 +831,7 @@ struct Walker {
             st = (int)ceil(el * W.invdt);
             st = st < 1 ? 1 : (st > W.keff ? W.keff : st);
         }
-        blkCount(C_PHONON_STEPS, (unsigned)st);
-        blkCount(C_EVENTS, (unsigned)nev);
+        stOut = st;
         if (stop == C_REPLAY_EXHAUSTED) atomicOr(P.status, (unsigned)S_REPLAY_EXHAUSTED);
         else if (stop == C_BAD) atomicOr(P.status, (unsigned)S_NONFINITE);
         if (stop != 0 && stop != C_REPLAY_EXHAUSTED) blkCount(stop, 1);
