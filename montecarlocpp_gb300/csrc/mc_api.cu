@@ -669,6 +669,7 @@ int setupSession(mc_session_s* S) {
         const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
                                              S->tm == TM_SHARED);
         S->smem = L.total;
+        setSingleLayout(P, L);
         // static schedule: the state stages after the tables
         if (!S->dyn) S->smem = staticStageOffset(L.total) + STATIC_STAGES * staticStageBytes<R>(S->block);
     }
@@ -782,6 +783,7 @@ int advanceT(mc_session_s* S, int nl, int* done) {
             std::swap(P.P0in, P.P0out); std::swap(P.P1in, P.P1out); std::swap(P.P2in, P.P2out);
         }
         P.step0 = S->step;
+        setWindow(P);
         setQuanta(S, P);
         unsigned long long* cur = S->cnt_d + C_NCOUNTERS + 2 * S->parity;
         unsigned long long* oth = S->cnt_d + C_NCOUNTERS + 2 * (S->parity ^ 1);
@@ -973,7 +975,7 @@ int batchCaps(std::vector<InstD<R>>& inst, Params<R>& P) {
     for (auto& I : inst) {
         bNt = std::max(bNt, I.nw * I.np);
         bNw = std::max(bNw, I.nw);
-        const size_t talE = (size_t)I.rows * (2 * (size_t)I.cols + 1);
+        const size_t talE = talEntries(I.rows, (int)I.cols);
         I.flags = 0;
         if (talE * sizeof(long long) <= TAL_BATCH_MAX) {
             I.flags |= IF_TAL_SHARED;
@@ -1150,6 +1152,7 @@ int enqueueBatch(mc_batch_s* B) {
     int launches = 1;
     for (int step = 0; step < (int)B->bd.nsteps; step += P.ksteps) {
         P.step0 = step;
+        setWindow(P);
         CK(cudaMemsetAsync(B->cnt + C_NCOUNTERS + 1, 0, sizeof(unsigned long long), B->stream));
         CK(cudaMemsetAsync(B->segNext, 0, sizeof(unsigned long long) * std::max(B->nseg, 1), B->stream));
         CK(launchAdvanceBatch<R>(P, B->grid, B->block, B->stream));
@@ -1470,6 +1473,7 @@ struct ServerT : ServerBase {
         P.cap = (unsigned long long)islot[n];
         P.ninst = n;
         P.step0 = 0;
+        setWindow(P);
         CK(launchEmitBatch<R>(P, stream));
         CK(launchAdvanceBatch<R>(P, grid, block, stream));
         CK(launchDifPrefix<R>(P, stream));
@@ -1798,6 +1802,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
         const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
                                              S->tm == TM_SHARED);
         S->smem = L.total;
+        setSingleLayout(P, L);
     }
     if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
     S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;

@@ -81,6 +81,14 @@ struct Params {
     long long nemit, maxscat, maxloop;
     R dt;
     int step0, ksteps, nsteps;
+    // the window of this launch, derived from step0 on the host (setWindow)
+    int wKeff, wLast;
+    R wLen, wInvdt, wNext;
+    // single-instance launches: byte offsets in shared memory of the
+    // vel*tau table, scatter thresholds, guide table, subdomain images and
+    // fixed-point field (the vel table at 0), and of the static kernel's
+    // state stages (setSingleLayout)
+    int smVt, smWthr, smGuide, smSd, smTal, smStage;
     uint32_t key0, key1;
     // state (ping-pong halves chosen by the host)
     typename Vec4<R>::T* P0in; typename Vec4<R>::T* P1in; uint4* P2in;
@@ -183,6 +191,15 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
     o0 = c0; o1 = c1; o2 = c2; o3 = c3;
 }
 
+// One Philox block out of line: the event code draws from several call
+// sites, and one shared copy of the ten rounds keeps the advance loop small
+// enough for the instruction cache.
+static __device__ __noinline__ uint4 philoxBlock(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1) {
+    uint4 o;
+    philox4x32_10(c0, c1, c2, 0u, k0, k1, o.x, o.y, o.z, o.w);
+    return o;
+}
+
 template <bool REPLAY> struct Rng;
 
 template <> struct Rng<false> {
@@ -195,7 +212,8 @@ template <> struct Rng<false> {
     __device__ __forceinline__ void setEvent(uint32_t e) { event = e; block = 0; lane = 0; }
     __device__ __forceinline__ uint32_t next() {
         if (lane == 0) {
-            philox4x32_10(id, event, block, 0u, k0, k1, b0, b1, b2, b3);
+            const uint4 o = philoxBlock(id, event, block, k0, k1);
+            b0 = o.x; b1 = o.y; b2 = o.z; b3 = o.w;
             ++block;
             lane = 4;
         }

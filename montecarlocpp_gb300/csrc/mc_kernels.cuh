@@ -54,7 +54,7 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         sd = reinterpret_cast<const SdomD<R>*>(smraw + L.sd);
     }
     if (TM == TM_SHARED) {
-        const int nz = P.rows * (2 * P.cols + 1);
+        const int nz = (int)talEntries(P.rows, P.cols);
         for (int i = threadIdx.x; i < nz; i += blockDim.x) tal[i] = 0;
     }
     if (threadIdx.x == 0) {
@@ -67,7 +67,7 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         I->slot0 = 0; I->nemit = P.nemit;
         I->key0 = P.key0; I->key1 = P.key1;
         I->tal = TM == TM_SHARED ? tal : nullptr;
-        I->dif = TM == TM_SHARED ? tal + (size_t)P.rows * P.cols : nullptr;
+        I->dif = TM == TM_SHARED ? tal + (size_t)talStride(P.rows) * P.cols : nullptr;
         I->tally = P.tally; I->gdif = nullptr; I->csum = P.csum;
         I->groups = 1; I->gstride = 0; I->flags = 0;
         for (int r = 0; r < 4; ++r) { I->tqinv[r] = P.tqinv[r]; I->tq[r] = P.tq[r]; }
@@ -75,44 +75,46 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
     return I;
 }
 
-// Sum row r of the block's shared fixed-point field (cells) into the
-// block checksums: the field holds every flight amount that did not go to
-// g_blk.csum directly. Then flush the cells as FP64 atomics into `dst`
-// (rows x cols column-major) and clear them. All threads, after a barrier.
+// Flush the block's shared fixed-point field into `dst` (rows x cols,
+// column-major) as FP64 atomics and clear it: first the difference array
+// is prefix-summed into the cells, then every non-zero cell is added and
+// summed per row into the block checksums (the field holds every flight
+// amount that did not go to g_blk.csum directly). Both shared arrays are
+// cell-major with talStride(rows) words per cell; dst is rows x cols
+// column-major. All threads, after a barrier.
 template <typename R>
 __device__ __forceinline__ void flushSharedField(const InstD<R>& I, double* dst) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    // difference rows -> cells
-    for (int r = warp; r < I.rows; r += nwarps) {
+    const int rows = I.rows, st = talStride(rows);
+    for (int r = warp; r < rows; r += nwarps) {
         long long carry = 0;
-        long long* dr = I.dif + r * (I.cols + 1);
         for (int c0 = 0; c0 < I.cols; c0 += 32) {
             const int c = c0 + lane;
-            long long x = c < I.cols ? dr[c] : 0;
-            if (c < I.cols) dr[c] = 0;
+            long long x = c < I.cols ? I.dif[c * st + r] : 0;
+            if (c < I.cols) I.dif[c * st + r] = 0;
             for (int o = 1; o < 32; o <<= 1) {
                 long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
                 if (lane >= o) x += y;
             }
             x += carry;
-            if (c < I.cols) I.tal[r * I.cols + c] += x;
+            if (c < I.cols) I.tal[c * st + r] += x;
             carry = __shfl_sync(0xFFFFFFFFu, x, 31);
         }
-        if (lane == 0) dr[I.cols] = 0;
+        if (lane == 0) I.dif[I.cols * st + r] = 0;
     }
     __syncthreads();
     long long part[4] = {0, 0, 0, 0};
-    const int tot = I.rows * I.cols;
+    const int tot = rows * I.cols;
     for (int q = threadIdx.x; q < tot; q += blockDim.x) {
-        const long long x = I.tal[q];
+        const int c = q / rows, r = q - c * rows;
+        const long long x = I.tal[c * st + r];
         if (x != 0) {
-            const int r = q / I.cols, c = q - r * I.cols;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 if (k == r) part[k] += x;
-            atomicAdd(&dst[(size_t)c * I.rows + r], (double)x * I.tq[r]);
-            I.tal[q] = 0;
+            atomicAdd(&dst[q], (double)x * I.tq[r]);
+            I.tal[c * st + r] = 0;
         }
     }
 #pragma unroll
@@ -255,6 +257,17 @@ __host__ __device__ inline size_t staticStageOffset(size_t layoutTotal) {
     return (layoutTotal + 127) & ~(size_t)127;
 }
 
+// The shared-memory offsets of a single-instance launch into P (host).
+template <typename R>
+inline void setSingleLayout(Params<R>& P, const SmemLayout& L) {
+    P.smVt = (int)L.vt;
+    P.smWthr = (int)L.wthr;
+    P.smGuide = (int)L.guide;
+    P.smSd = (int)L.sd;
+    P.smTal = (int)L.tal;
+    P.smStage = (int)staticStageOffset(L.total);
+}
+
 template <typename R, bool REPLAY, bool LOG, int TM>
 __global__ void __launch_bounds__(STATIC_MAX_THREADS, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
 k_advance(Params<R> P) {
@@ -270,11 +283,7 @@ k_advance(Params<R> P) {
     InstD<R>* I = stageTables<R, TM>(P, smraw);
     ParamView<R, TM> V;
     V.init(P, smraw);
-    unsigned char* stage0;
-    {
-        const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED);
-        stage0 = smraw + staticStageOffset(L.total);
-    }
+    unsigned char* stage0 = smraw + P.smStage;
     const size_t sbytes = staticStageBytes<R>(T);
     const long long C = P.regCap;
     const long long rbase = (long long)blockIdx.x * C;
@@ -484,7 +493,7 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
 // Block b owns the live slots [b C, (b + 1) C) of the launch.
 template <typename R, bool REPLAY, bool LOG, int TM>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
-    extern __shared__ __align__(16) unsigned char smraw[];
+    extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ unsigned long long qnext;
     InstD<R>* I = stageTables<R, TM>(P, smraw);
     blkZero();
@@ -531,7 +540,7 @@ __device__ __forceinline__ void stageInstance(const Params<R>& P, int inst, unsi
     }
     const bool talS = (G.flags & IF_TAL_SHARED) != 0;
     if (talS) {
-        const int nz = G.rows * (2 * G.cols + 1);
+        const int nz = (int)talEntries(G.rows, G.cols);
         for (int i = threadIdx.x; i < nz; i += blockDim.x) tal[i] = 0;
     }
     if (threadIdx.x == 0) {
@@ -539,7 +548,7 @@ __device__ __forceinline__ void stageInstance(const Params<R>& P, int inst, unsi
         I->vel = vel; I->vt = vt; I->wthr = wthr; I->wguide = wguide;
         if (sdS) I->sd = reinterpret_cast<const SdomD<R>*>(smraw + L.sd);
         I->tal = talS ? tal : nullptr;
-        I->dif = talS ? tal + (size_t)G.rows * G.cols : nullptr;
+        I->dif = talS ? tal + (size_t)talStride(G.rows) * G.cols : nullptr;
     }
 }
 
@@ -566,7 +575,7 @@ __device__ __forceinline__ void flushBinding(const InstD<R>& I, int group) {
 // segment home[block] (the host spreads blocks over segments by size).
 template <typename R>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_batch(Params<R> P) {
-    extern __shared__ __align__(16) unsigned char smraw[];
+    extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ int sSeg;
     BatchSmem L;
     L.init<R>(P.bNt, P.bNw, P.bSdBytes, P.bTal);

@@ -7,6 +7,15 @@
 
 namespace mcg {
 
+// Shared fixed-point fields are cell-major with an odd stride of 64-bit
+// words per cell (rows rounded up to odd), so the rows of a cell sit at
+// fixed offsets and lanes that add to different cells spread over the
+// banks; the difference array that follows has cols + 1 such cells.
+__host__ __device__ inline int talStride(int rows) { return rows | 1; }
+__host__ __device__ inline size_t talEntries(int rows, int cols) {
+    return (size_t)talStride(rows) * (2 * (size_t)cols + 1);
+}
+
 // ---------------------------------------------------------------- tables
 // Shared layout of a single-instance launch: vel and vel*tau tables, the
 // scatter bin thresholds and guide table, the subdomains (when staged), the
@@ -24,7 +33,7 @@ struct SmemLayout {
         sd = al(guide + sizeof(uint16_t) * GUIDE);
         inst = al(sd + sizeof(SdomD<R>) * (size_t)nsdShared);
         tal = al(inst + sizeof(InstD<R>));
-        total = tal + (sharedTally ? sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1) : 0);
+        total = tal + (sharedTally ? sizeof(long long) * talEntries(rows, cols) : 0);
     }
 };
 
@@ -69,7 +78,7 @@ constexpr size_t TAL_BATCH_MAX = 32 * 1024;
 constexpr size_t BATCH_SMEM_F32 = 56 * 1024;
 
 __host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
-    return sizeof(long long) * (size_t)rows * (2 * (size_t)cols + 1);
+    return sizeof(long long) * talEntries(rows, cols);
 }
 
 // Tally modes: per-block shared histogram (64-bit fixed point, exact and
@@ -111,8 +120,12 @@ struct Phn {
 // largest single flight 2^30 units, so one 32-bit round-to-nearest
 // conversion suffices (|v| < 2^31); sums are kept in 64 bits. FP64 flight:
 // 64-bit conversion against a quantum sized for a block's total.
-__device__ __forceinline__ long long toFixed(float v) { return (long long)__float2int_rn(v); }
+__device__ __forceinline__ int toFixed(float v) { return __float2int_rn(v); }
 __device__ __forceinline__ long long toFixed(double v) { return __double2ll_rn(v); }
+// fixed-point amount of one flight in each flight precision
+template <typename R> struct FixT;
+template <> struct FixT<float> { using T = int; };
+template <> struct FixT<double> { using T = long long; };
 
 // float -> double by moving the bits (the conversion instruction runs on
 // GB300's narrow FP64 pipe); zero and subnormal inputs give zero.
@@ -138,6 +151,14 @@ __device__ __forceinline__ void sharedAdd64(long long* p, long long v) {
     const unsigned lo = (unsigned)(unsigned long long)v;
     const unsigned old = atomicAdd(w, lo);
     const int hi = (int)(v >> 32) + ((old + lo) < old ? 1 : 0);
+    if (hi != 0) atomicAdd(reinterpret_cast<int*>(w + 1), hi);
+}
+// the same for a 32-bit amount (sign extension from bit 31)
+__device__ __forceinline__ void sharedAdd64(long long* p, int v) {
+    unsigned* w = reinterpret_cast<unsigned*>(p);
+    const unsigned lo = (unsigned)v;
+    const unsigned old = atomicAdd(w, lo);
+    const int hi = (v >> 31) + ((old + lo) < old ? 1 : 0);
     if (hi != 0) atomicAdd(reinterpret_cast<int*>(w + 1), hi);
 }
 __device__ __forceinline__ void sharedAdd64(unsigned long long* p, unsigned long long v) {
@@ -218,17 +239,15 @@ struct InstView {
     __device__ __forceinline__ long long maxloop() const { return I->maxloop; }
 };
 
-// Single-instance view over singleLayout().
+// Single-instance view over singleLayout(), whose offsets the host puts in
+// the launch parameters (setSingleLayout).
 template <typename R, int TM>
 struct ParamView {
     const Params<R>* P;
     unsigned char* sm;
-    int oVt, oWthr, oGuide, oSd, oTal;  // the vel table sits at offset 0
     __device__ __forceinline__ void init(const Params<R>& p, unsigned char* smraw) {
         P = &p;
         sm = smraw;
-        const SmemLayout L = singleLayout<R>(p.nw, p.np, p.nsd, p.rows, p.cols, TM == TM_SHARED);
-        oVt = (int)L.vt; oWthr = (int)L.wthr; oGuide = (int)L.guide; oSd = (int)L.sd; oTal = (int)L.tal;
     }
     __device__ __forceinline__ int rows() const { return P->rows; }
     __device__ __forceinline__ int cols() const { return P->cols; }
@@ -236,10 +255,10 @@ struct ParamView {
     __device__ __forceinline__ int nw() const { return P->nw; }
     __device__ __forceinline__ int np() const { return P->np; }
     __device__ __forceinline__ long long* tal() const {
-        return TM == TM_SHARED ? reinterpret_cast<long long*>(sm + oTal) : nullptr;
+        return TM == TM_SHARED ? reinterpret_cast<long long*>(sm + P->smTal) : nullptr;
     }
     __device__ __forceinline__ long long* dif() const {
-        return reinterpret_cast<long long*>(sm + oTal) + (size_t)P->rows * P->cols;
+        return reinterpret_cast<long long*>(sm + P->smTal) + (size_t)talStride(P->rows) * P->cols;
     }
     __device__ __forceinline__ double* tally() const { return P->tally; }
     __device__ __forceinline__ double* gdif() const { return nullptr; }
@@ -247,13 +266,13 @@ struct ParamView {
     __device__ __forceinline__ long long gstride() const { return 0; }
     __device__ __forceinline__ int flags() const { return 0; }
     __device__ __forceinline__ R tqinv(int r) const { return P->tqinv[r]; }
-    __device__ __forceinline__ const SdomD<R>* sd() const { return reinterpret_cast<const SdomD<R>*>(sm + oSd); }
+    __device__ __forceinline__ const SdomD<R>* sd() const { return reinterpret_cast<const SdomD<R>*>(sm + P->smSd); }
     __device__ __forceinline__ const R* vel() const { return reinterpret_cast<const R*>(sm); }
-    __device__ __forceinline__ const R* vt() const { return reinterpret_cast<const R*>(sm + oVt); }
+    __device__ __forceinline__ const R* vt() const { return reinterpret_cast<const R*>(sm + P->smVt); }
     __device__ __forceinline__ const unsigned long long* wthr() const {
-        return reinterpret_cast<const unsigned long long*>(sm + oWthr);
+        return reinterpret_cast<const unsigned long long*>(sm + P->smWthr);
     }
-    __device__ __forceinline__ const uint16_t* wguide() const { return reinterpret_cast<const uint16_t*>(sm + oGuide); }
+    __device__ __forceinline__ const uint16_t* wguide() const { return reinterpret_cast<const uint16_t*>(sm + P->smGuide); }
     __device__ __forceinline__ const unsigned long long* pthr() const { return P->pthr; }
     __device__ __forceinline__ uint32_t key0() const { return P->key0; }
     __device__ __forceinline__ uint32_t key1() const { return P->key1; }
@@ -273,17 +292,21 @@ struct Tally {
     __device__ __forceinline__ bool shared() const {
         return TM == TM_SHARED || (TM == TM_AUTO && V.tal() != nullptr);
     }
+    using Fix = typename FixT<R>::T;
     // fixed-point amount of row r for path length t
-    __device__ __forceinline__ long long fixedOf(int r, R t) const { return toFixed(rho[r] * (t * V.tqinv(r))); }
+    __device__ __forceinline__ Fix fixedOf(int r, R t) const { return toFixed(rho[r] * (t * V.tqinv(r))); }
     // a flight's amount that does not enter the shared field
     __device__ __forceinline__ void csumAdd(int r, long long v) const { blkCsum(r, v); }
-    __device__ __forceinline__ void atomShared(int r, int col, long long v) const {
-        sharedAdd64(&V.tal()[r * V.cols() + col], v);
+    // shared field and difference array, cell-major: row r of column c at
+    // [c * talStride(rows) + r]
+    __device__ __forceinline__ void atomShared(int r, int col, Fix v) const {
+        sharedAdd64(&V.tal()[col * talStride(V.rows()) + r], v);
     }
-    __device__ __forceinline__ void atomRange(int r, int c0, int c1, long long v) const {
-        long long* d = V.dif() + r * (V.cols() + 1);
-        sharedAdd64(d + c0, v);
-        sharedAdd64(d + c1, -v);
+    __device__ __forceinline__ void atomRange(int r, int c0, int c1, Fix v) const {
+        long long* d = V.dif();
+        const int st = talStride(V.rows());
+        sharedAdd64(d + c0 * st + r, v);
+        sharedAdd64(d + c1 * st + r, -v);
     }
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
@@ -350,25 +373,34 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
     const int stride = S.tstride[K];
     const R inva = fabs(ia[K]);
     const int lo = min(b, e), hi = max(b, e);
+    const int nin = hi - lo - 1;  // interior cells; -1 when the flight stays in its cell
     const R tfirst = (e > b ? (R(1) - ph.off[K]) : ph.off[K]) * inva;
+    using Fix = typename FixT<R>::T;
+    if (T.shared()) {
+        // the first cell's add is common to every lane (all of V when the
+        // flight stays in its cell), the others only add to it: no lane
+        // waits for another's branch
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        if (r >= T.rows()) break;
-        const long long V = T.fixedOf(r, s);
-        if (T.shared()) {
-            if (e == b) {
-                T.atomShared(r, cb + b * stride, V);
-            } else {
-                const long long F = T.fixedOf(r, tfirst);
-                const long long I = T.fixedOf(r, inva);
-                T.atomShared(r, cb + b * stride, F);
-                T.atomShared(r, cb + e * stride, V - F - (long long)(hi - lo - 1) * I);
-                if (stride == 1) { if (hi - lo > 1) T.atomRange(r, cb + lo + 1, cb + hi, I); }
-                else for (int c = lo + 1; c < hi; ++c) T.atomShared(r, cb + c * stride, I);
+        for (int r = 0; r < 4; ++r) {
+            if (r < T.rows()) {
+                const Fix V = T.fixedOf(r, s);
+                const Fix F = T.fixedOf(r, tfirst);
+                const Fix I = T.fixedOf(r, inva);
+                T.atomShared(r, cb + b * stride, e == b ? V : F);
+                if (e != b) T.atomShared(r, cb + e * stride, V - F - (Fix)nin * I);
+                if (nin > 0) {
+                    if (stride == 1) {
+                        T.atomRange(r, cb + lo + 1, cb + hi, I);
+                    } else {
+                        for (int c = lo + 1; c < hi; ++c) T.atomShared(r, cb + c * stride, I);
+                    }
+                }
             }
-        } else {
-            T.csumAdd(r, V);
         }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (r < T.rows()) T.csumAdd(r, T.fixedOf(r, s));
     }
     if (!T.shared()) {
         if (e == b) {
@@ -400,10 +432,11 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         // a single field column (or none): move only
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            if (r >= T.rows()) break;
-            const long long V = T.fixedOf(r, s);
-            if (acc == -1 && T.shared()) T.atomShared(r, cb, V);
-            else T.csumAdd(r, V);
+            if (r < T.rows()) {
+                const typename FixT<R>::T V = T.fixedOf(r, s);
+                if (acc == -1 && T.shared()) T.atomShared(r, cb, V);
+                else T.csumAdd(r, V);
+            }
         }
         if (acc == -1 && !T.shared()) T.addGlobal(cb, s);
 #pragma unroll
@@ -569,13 +602,27 @@ struct Window {
     bool last;       // the horizon ends with this launch
     R next;          // length of the following window (0 if none)
     __device__ __forceinline__ void init(const Params<R>& P) {
-        keff = min(P.ksteps, P.nsteps - P.step0);
-        len = (R)keff * P.dt;
-        invdt = R(1) / P.dt;
-        last = (P.step0 + keff >= P.nsteps);
-        next = (R)min(P.ksteps, max(P.nsteps - P.step0 - keff, 0)) * P.dt;
+        keff = P.wKeff;
+        len = P.wLen;
+        invdt = P.wInvdt;
+        last = P.wLast != 0;
+        next = P.wNext;
     }
 };
+
+// The window fields of P for its step0: keff dt-steps of length dt from
+// step0, whether the horizon ends with them, and the next window's length
+// (the arithmetic in the flight precision, as the kernels used to form it).
+template <typename R>
+__host__ __device__ inline void setWindow(Params<R>& P) {
+    const int rest = P.nsteps - P.step0;
+    P.wKeff = P.ksteps < rest ? P.ksteps : rest;
+    P.wLen = (R)P.wKeff * P.dt;
+    P.wInvdt = R(1) / P.dt;
+    P.wLast = (P.step0 + P.wKeff >= P.nsteps) ? 1 : 0;
+    const int after = rest - P.wKeff > 0 ? rest - P.wKeff : 0;
+    P.wNext = (R)(P.ksteps < after ? P.ksteps : after) * P.dt;
+}
 
 // Walker state that only the replay kernels carry.
 struct NoReplay {};
