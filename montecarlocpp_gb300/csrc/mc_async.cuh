@@ -46,19 +46,23 @@ __device__ __forceinline__ void mbarArriveExpectTx(uint64_t* bar, uint32_t bytes
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, uint32_t parity) {
+// One try: the thread may be suspended (not spinning on issue slots) until
+// the phase completes or about `hintNs` nanoseconds have passed.
+__device__ __forceinline__ bool mbarTryWait(uint64_t* bar, uint32_t parity, uint32_t hintNs = 100000u) {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smemAddr(bar)), "r"(parity)
+        : "r"(smemAddr(bar)), "r"(parity), "r"(hintNs)
         : "memory");
     return ok != 0;
 }
 
 // Wait for the phase of parity `parity` to complete; false once `limitNs`
 // nanoseconds have passed (the phase may still complete later) or when
-// *stop becomes non-zero (another role of the block gave up).
+// *stop becomes non-zero (another role of the block gave up). Each try
+// suspends the thread for up to 100 us, so a waiting warp leaves the issue
+// slots to the warps that are working.
 __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity, uint64_t limitNs,
                                          const volatile int* stop = nullptr) {
     if (mbarTryWait(bar, parity)) return true;

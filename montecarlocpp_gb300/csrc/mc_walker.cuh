@@ -159,7 +159,7 @@ __device__ __forceinline__ void sharedAdd64(long long* p, int v) {
     const unsigned lo = (unsigned)v;
     const unsigned old = atomicAdd(w, lo);
     const int hi = (v >> 31) + ((old + lo) < old ? 1 : 0);
-    if (hi != 0) atomicAdd(reinterpret_cast<int*>(w + 1), hi);
+    atomicAdd(reinterpret_cast<int*>(w + 1), hi);  // unconditional: no branch
 }
 __device__ __forceinline__ void sharedAdd64(unsigned long long* p, unsigned long long v) {
     sharedAdd64(reinterpret_cast<long long*>(p), (long long)v);
