@@ -328,15 +328,10 @@ def main():
     if not args.no_plain:
         line["plain_kernel"] = plain_kernel(prob, W, stream, peak, peak_kind)
     if not args.no_batched:
-        line["batched"] = bench_batched(stream)
+        line["batched"] = bench_batched(stream, plain=not args.no_plain)
     if not args.no_served:
         sv = bench_served(rate=args.serve_rate, duration=args.serve_duration, drain=args.serve_drain)
-        sv["below_capacity"] = bench_served(rate=10.0, duration=10.0, drain=60.0)
-        if "plain_kernel" in line and sv["completed"]:
-            # the per-dt-step kernel at its film rate over the same solves
-            plain_sps = line["plain_kernel"]["phonon_steps_per_s"] / sv["phonon_steps_per_solve"]
-            sv["plain_solves_per_s_est"] = plain_sps
-            sv["served_vs_plain_est"] = sv["solves_per_s"] / plain_sps
+        sv["below_capacity"] = bench_served(rate=10.0, duration=10.0, drain=60.0, plain_sample=False)
         line["served"] = sv
     if rank == 0 and not args.no_cpu:
         try:
@@ -423,7 +418,45 @@ def bench_batched(stream, reps=2, plain=True):
     return out
 
 
-def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budget_gb=8.0):
+def plain_on_requests(reqs, doms, mats, done, done_idx, nsteps, sample=8, cap=10_000_000, warm=20, timed=200):
+    """The plain single-instance kernel (one dt-step per launch, full FP64
+    field) on a sample of the completed requests: its phonon-steps/s on each
+    request's own geometry and temperature, and the time it would take for
+    the phonon-steps the served solve used. Returns plain solves/s over the
+    sample and the served engine's solves/s is compared with it."""
+    import torch
+
+    import montecarlocpp_gb300 as M
+    rng = np.random.default_rng(1)
+    pick = sorted(rng.choice(len(done), size=min(sample, len(done)), replace=False).tolist()) if done else []
+    stream = torch.cuda.Stream()
+    t_plain, rates = 0.0, []
+    for k in pick:
+        r, (d, _) = reqs[done_idx[k]], doms[done_idx[k]]
+        nemit = int(min(max(done[k]["phonons"], 10_000), cap))  # the solve's own phonon count
+        prob = M.MultiProblem(mats[round(r.T, 3)], d, nemit, 1_000_000)
+        s = prob.session(dt=0.5e-12, nsteps=warm + timed, precision=32, steps_per_launch=1, seed=5,
+                         stream=stream.cuda_stream)
+        s.emit()
+        s.advance(warm)
+        _, st0 = s.result(field=False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.advance(timed)
+        e1.record(stream)
+        _, st1 = s.result(field=False)
+        s.close()
+        rate = (st1["phonon_steps"] - st0["phonon_steps"]) / (e0.elapsed_time(e1) * 1e-3)
+        rates.append({"geometry": r.geometry, "size_m": r.size, "T": r.T, "phonons": nemit, "phonon_steps_per_s": rate})
+        t_plain += done[k]["phonon_steps"] / rate
+    return {"sample": len(pick), "plain_solves_per_s": (len(pick) / t_plain) if t_plain > 0 else None,
+            "rates": rates,
+            "how": f"the per-dt-step kernel (FP32 flight, FP64 field) on each sampled request's geometry and "
+                   f"temperature with the phonons its served solve used (at most {cap}), {timed} timed launches "
+                   f"after {warm}; a request's plain time = the phonon-steps its served solve used / that rate"}
+
+
+def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budget_gb=8.0, plain_sample=True):
     """Config 4: Poisson requests (film or pore cell, size log-U(20 nm, 2 um),
     T U(100, 400 K), first-round phonons log-U(1e4, 1e7)) submitted at their
     arrival times to the serving loop; each solve runs until kappa has a 1%
@@ -454,13 +487,15 @@ def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budg
             time.sleep(0.0005)
         tickets.append(srv.submit(mats[round(r.T, 3)], d, r.nemit, seed=len(tickets), volume=vol, field=False))
     deadline = time.perf_counter() + drain
-    done = []
-    for t in tickets:
+    done, done_idx = [], []
+    for i, t in enumerate(tickets):
         res = srv.wait(t, max(0.0, deadline - time.perf_counter()))
         if res is not None:
             done.append(res)
+            done_idx.append(i)
     st = srv.stats()
     srv.close()
+    plain = plain_on_requests(reqs, doms, mats, done, done_idx, nsteps) if plain_sample else None
     lat = sorted(r["t_done"] - r["t_submit"] for r in done)
     span = (max(r["t_done"] for r in done) - c0) if done else float("nan")
     pct = (lambda q: float(np.percentile(lat, q))) if lat else (lambda q: None)
@@ -477,6 +512,8 @@ def bench_served(rate=200.0, duration=5.0, drain=20.0, nsteps=4000, seed=0, budg
             "converged": sum(1 for r in done if r["status"] == 0),
             "max_rel_se": max((r["kappa_se"] / abs(r["kappa"]) for r in done if r["kappa"]), default=None),
             "saturated": solves_per_s < 0.9 * len(reqs) / duration,
+            "plain_on_requests": plain,
+            "served_vs_plain": (solves_per_s / plain["plain_solves_per_s"]) if plain and plain["plain_solves_per_s"] else None,
             "note": ("latency counts from submission to completion; when the offered rate exceeds the "
                      "GPU's solve rate (saturated) the queue grows for the whole arrival window, so p50/p99 "
                      "grow with its length")}

@@ -995,6 +995,7 @@ int batchCaps(std::vector<InstD<R>>& inst, Params<R>& P) {
         }
     }
     P.bNt = bNt; P.bNw = bNw; P.bTal = bTal; P.bSdBytes = bSd;
+    setBatchLayout(P);
     if (batchSmemBytes<R>(P) > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "batched shared-memory tables exceed 227 KB");
     return MC_OK;
 }

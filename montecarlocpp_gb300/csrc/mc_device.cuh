@@ -84,11 +84,13 @@ struct Params {
     // the window of this launch, derived from step0 on the host (setWindow)
     int wKeff, wLast;
     R wLen, wInvdt, wNext;
-    // single-instance launches: byte offsets in shared memory of the
-    // vel*tau table, scatter thresholds, guide table, subdomain images and
-    // fixed-point field (the vel table at 0), and of the static kernel's
-    // state stages (setSingleLayout)
+    // byte offsets in shared memory of the vel*tau table, scatter
+    // thresholds, guide table, subdomain images and fixed-point field, and
+    // of the static kernel's state stages: the single-instance layout
+    // (setSingleLayout, vel at 0) or, in batched launches, the batched one
+    // (setBatchLayout)
     int smVt, smWthr, smGuide, smSd, smTal, smStage;
+    int smVel;  // batched launches: their layout's vel table (0 otherwise)
     uint32_t key0, key1;
     // state (ping-pong halves chosen by the host)
     typename Vec4<R>::T* P0in; typename Vec4<R>::T* P1in; uint4* P2in;

@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
         }
         __syncthreads();
         dynamicLoop<R, false, false, TM_AUTO>(P, P.segNext + sg, (unsigned long long)S.beg,
-                                              (unsigned long long)S.end, InstView<R>{I}, W);
+                                              (unsigned long long)S.end, BatchView<R>{&P, smraw, I}, W);
         __syncthreads();
         flushBinding<R>(*I, S.group);
         __syncthreads();
@@ -622,6 +622,20 @@ __host__ __device__ inline size_t batchSmemBytes(const Params<R>& P) {
     BatchSmem L;
     L.init<R>(P.bNt, P.bNw, P.bSdBytes, P.bTal);
     return L.total;
+}
+
+// The batched layout's offsets into P (host, after the capacities).
+template <typename R>
+inline void setBatchLayout(Params<R>& P) {
+    BatchSmem L;
+    L.init<R>(P.bNt, P.bNw, P.bSdBytes, P.bTal);
+    P.smVel = (int)L.vel;
+    P.smVt = (int)L.vt;
+    P.smWthr = (int)L.wthr;
+    P.smGuide = (int)L.guide;
+    P.smSd = (int)L.sd;
+    P.smTal = (int)L.tal;
+    P.smStage = 0;
 }
 
 // Global difference arrays -> field: block (i, y) prefix-sums row y % 4 of

@@ -219,6 +219,7 @@ struct InstView {
     __device__ __forceinline__ int problem() const { return I->problem; }
     __device__ __forceinline__ int nw() const { return I->nw; }
     __device__ __forceinline__ int np() const { return I->np; }
+    __device__ __forceinline__ bool talShared() const { return I->tal != nullptr; }
     __device__ __forceinline__ long long* tal() const { return I->tal; }
     __device__ __forceinline__ long long* dif() const { return I->dif; }
     __device__ __forceinline__ double* tally() const { return I->tally; }
@@ -254,6 +255,7 @@ struct ParamView {
     __device__ __forceinline__ int problem() const { return P->problem; }
     __device__ __forceinline__ int nw() const { return P->nw; }
     __device__ __forceinline__ int np() const { return P->np; }
+    __device__ __forceinline__ bool talShared() const { return TM == TM_SHARED; }
     __device__ __forceinline__ long long* tal() const {
         return TM == TM_SHARED ? reinterpret_cast<long long*>(sm + P->smTal) : nullptr;
     }
@@ -280,6 +282,48 @@ struct ParamView {
     __device__ __forceinline__ long long maxloop() const { return P->maxloop; }
 };
 
+// Batched view: the instance a block is bound to, as it staged it. The
+// descriptor's scalars come from the staged copy; the tables (always
+// staged) and the fixed-point field (when the instance stages one) sit at
+// the batched layout's offsets, which the host puts in the launch
+// parameters (setBatchLayout), so they are shared-memory accesses with
+// known addresses; the subdomain images stay behind the descriptor's
+// pointer (shared or global, per instance).
+template <typename R>
+struct BatchView {
+    const Params<R>* P;
+    unsigned char* sm;
+    const InstD<R>* I;
+    __device__ __forceinline__ int rows() const { return I->rows; }
+    __device__ __forceinline__ int cols() const { return I->cols; }
+    __device__ __forceinline__ int problem() const { return I->problem; }
+    __device__ __forceinline__ int nw() const { return I->nw; }
+    __device__ __forceinline__ int np() const { return I->np; }
+    __device__ __forceinline__ bool talShared() const { return (I->flags & IF_TAL_SHARED) != 0; }
+    __device__ __forceinline__ long long* tal() const { return reinterpret_cast<long long*>(sm + P->smTal); }
+    __device__ __forceinline__ long long* dif() const {
+        return reinterpret_cast<long long*>(sm + P->smTal) + (size_t)talStride(I->rows) * I->cols;
+    }
+    __device__ __forceinline__ double* tally() const { return I->tally; }
+    __device__ __forceinline__ double* gdif() const { return I->gdif; }
+    __device__ __forceinline__ int groups() const { return I->groups; }
+    __device__ __forceinline__ long long gstride() const { return I->gstride; }
+    __device__ __forceinline__ int flags() const { return I->flags; }
+    __device__ __forceinline__ R tqinv(int r) const { return I->tqinv[r]; }
+    __device__ __forceinline__ const SdomD<R>* sd() const { return I->sd; }
+    __device__ __forceinline__ const R* vel() const { return reinterpret_cast<const R*>(sm + P->smVel); }
+    __device__ __forceinline__ const R* vt() const { return reinterpret_cast<const R*>(sm + P->smVt); }
+    __device__ __forceinline__ const unsigned long long* wthr() const {
+        return reinterpret_cast<const unsigned long long*>(sm + P->smWthr);
+    }
+    __device__ __forceinline__ const uint16_t* wguide() const { return reinterpret_cast<const uint16_t*>(sm + P->smGuide); }
+    __device__ __forceinline__ const unsigned long long* pthr() const { return I->pthr; }
+    __device__ __forceinline__ uint32_t key0() const { return I->key0; }
+    __device__ __forceinline__ uint32_t key1() const { return I->key1; }
+    __device__ __forceinline__ long long maxscat() const { return I->maxscat; }
+    __device__ __forceinline__ long long maxloop() const { return I->maxloop; }
+};
+
 // Field accumulation for one flight of one instance.
 template <typename R, int TM, typename IA>
 struct Tally {
@@ -290,7 +334,7 @@ struct Tally {
 
     __device__ __forceinline__ int rows() const { return V.rows(); }
     __device__ __forceinline__ bool shared() const {
-        return TM == TM_SHARED || (TM == TM_AUTO && V.tal() != nullptr);
+        return TM == TM_SHARED || (TM == TM_AUTO && V.talShared());
     }
     using Fix = typename FixT<R>::T;
     // fixed-point amount of row r for path length t
