@@ -193,6 +193,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-pore", action="store_true")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-duration", type=float, default=3.0)
     ap.add_argument("--serve-drain", type=float, default=90.0)
@@ -325,6 +327,10 @@ def main():
             "clocks": clk.summary(),
             "kappa_W_per_mK": kappa}
 
+    if not args.no_precision:
+        line["precision"] = precision_errors(prob, dom, W, K, seed, out)
+    if not args.no_pore:
+        line["pore_cell"] = bench_pore(K)
     if not args.no_plain:
         line["plain_kernel"] = plain_kernel(prob, W, stream, peak, peak_kind)
     if not args.no_batched:
@@ -343,6 +349,65 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def field_errors(f32, f64, f64b, dom, flux_row0=1):
+    """kappa and the flux profile (every flux row, per cell) of an FP32
+    solve against the FP64 solve of the same phonons; the statistical scale
+    is the seed-to-seed difference of two FP64 solves over sqrt(2)."""
+    import montecarlocpp_gb300 as M
+    k32 = M.kappa_from_flux(f32, dom, 0, flux_row0=flux_row0)
+    k64 = M.kappa_from_flux(f64, dom, 0, flux_row0=flux_row0)
+    k64b = M.kappa_from_flux(f64b, dom, 0, flux_row0=flux_row0)
+    q32, q64, q64b = (f[flux_row0:flux_row0 + 3] for f in (f32, f64, f64b))
+    scale = np.abs(q64).max()
+    return {"kappa_fp32": k32, "kappa_fp64": k64, "kappa_rel_err": abs(k32 - k64) / abs(k64),
+            "kappa_stat_rel": abs(k64b - k64) / abs(k64) / math.sqrt(2.0),
+            "flux_profile_max_err_of_max": float(np.abs(q32 - q64).max() / scale),
+            "flux_profile_rms_err_of_max": float(np.sqrt(np.mean((q32 - q64) ** 2)) / scale),
+            "flux_profile_stat_rms_of_max": float(np.sqrt(np.mean((q64b - q64) ** 2)) / scale / math.sqrt(2.0))}
+
+
+def precision_errors(prob, dom, W, K, seed, f32):
+    """The headline film: the FP32 field of the e2e solve against FP64
+    solves (the same seed, and one more for the statistical scale)."""
+    kw = dict(dt=W["dt"], nsteps=W["nsteps"], precision=64, steps_per_launch=K)
+    t0 = time.perf_counter()
+    f64 = prob.solve(seed=seed, **kw)
+    t64 = time.perf_counter() - t0
+    f64b = prob.solve(seed=seed + 7777, **kw)
+    out = field_errors(f32, f64, f64b, dom)
+    out["fp64_solve_s"] = t64
+    out["fp64_phonon_steps_per_s"] = prob.stats["phonon_steps"] / t64
+    return out
+
+
+def bench_pore(K, nemit=50_000_000, nemit_fp64=5_000_000, nsteps=4000, dt=0.5e-12, seed=3):
+    """The 3-D periodic porous cell: 500 nm cube with a centred 250 nm
+    cubic void, diffuse pore walls, 1 K/um along x, 50^3 cells (12/26/12 per
+    block), Si-like 300 K, dt 0.5 ps x 4000, FP32 flight / FP64 tally (the
+    107424 cells' field in global FP64 atomics). One timed solve of 5e7
+    phonons; FP32 against FP64 kappa and flux field on 5e6 phonons."""
+    import montecarlocpp_gb300 as M
+    mat = M.Material.silicon(300.0)
+    dom = M.PoreCellDomain(5e-7, 2.5e-7)
+    prob = M.MultiProblem(mat, dom, nemit, 1_000_000)
+    prob.solve(dt=dt, nsteps=50, precision=32, steps_per_launch=50, seed=seed)  # warm-up
+    t0 = time.perf_counter()
+    f32 = prob.solve(dt=dt, nsteps=nsteps, precision=32, steps_per_launch=K, seed=seed)
+    el = time.perf_counter() - t0
+    st = prob.stats
+    out = {"workload": "pore cell 500 nm, void 250 nm, 50^3 cells, 5e7 phonons, dt 0.5 ps x 4000, FP32 flight",
+           "phonons": st["nemit"], "phonon_steps": st["phonon_steps"], "events": st["events"],
+           "e2e_s": el, "e2e_phonon_steps_per_s": st["phonon_steps"] / el,
+           "kappa_W_per_mK": M.kappa_from_flux(f32, dom, 0, flux_row0=1), "cols": int(f32.shape[1])}
+    small = M.MultiProblem(mat, dom, nemit_fp64, 1_000_000)
+    kw = dict(dt=dt, nsteps=nsteps, steps_per_launch=K)
+    a = small.solve(precision=32, seed=seed, **kw)
+    b = small.solve(precision=64, seed=seed, **kw)
+    c = small.solve(precision=64, seed=seed + 7777, **kw)
+    out["fp32_vs_fp64"] = dict(field_errors(a, b, c, dom), phonons=int(small.stats["nemit"]))
+    return out
 
 
 def bench_batched(stream, reps=2, plain=True):
