@@ -521,6 +521,7 @@ struct mc_session_s {
     uint32_t* rcur_d = nullptr;
     double* log_d = nullptr;
     int* logcnt_d = nullptr;
+    int lean = -1;                // static schedule: axis of the lean flight, or -1
     unsigned* reg_d = nullptr;    // static schedule: front / back live counts
                                   // per block region, one array per half
     int parity = 0;               // which half holds the live phonons
@@ -677,7 +678,17 @@ int setupSession(mc_session_s* S) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    int occ = advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->block, S->smem);
+    // static schedule with a shared 1-D field along one axis in every
+    // subdomain (and no replay or log): the kernel with the lean flight
+    S->lean = -1;
+    if (!S->dyn && !S->replay && !S->logging && S->tm == TM_SHARED) {
+        const int k = D.sd[0].accum;
+        bool same = k >= 0 && k <= 2;
+        for (const auto& x : D.sd) same = same && x.accum == k;
+        if (same) S->lean = k;
+    }
+    int occ = S->lean >= 0 ? advanceLeanOccupancy<R>(S->lean, S->block, S->smem)
+                           : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
     // state: two halves of (P0, P1, P2). The static schedule cuts each half
@@ -815,7 +826,8 @@ int advanceT(mc_session_s* S, int nl, int* done) {
             // block regions of the current half -> the other half
             P.regIn = S->reg_d + 2 * (size_t)S->grid * S->parity;
             P.regOut = S->reg_d + 2 * (size_t)S->grid * (S->parity ^ 1);
-            CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+            if (S->lean >= 0) CK(launchAdvanceLean<R>(P, S->lean, S->grid, S->block, S->smem, S->stream));
+            else CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
             S->parity ^= 1;
             S->step += S->desc.steps_per_launch;
             S->launches++;

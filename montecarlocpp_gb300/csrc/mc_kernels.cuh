@@ -243,6 +243,7 @@ constexpr int STATIC_STAGES = 2;
 constexpr int STATIC_PRODUCER_THREADS = 32;
 constexpr int STATIC_MAX_THREADS = 256 + STATIC_PRODUCER_THREADS;
 constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
+constexpr unsigned STATIC_BACK = 1u << 30;    // stage tag: a tile of the back range
 // bounded waits: a bulk copy lands within microseconds; the producer may
 // wait for consumers in the middle of a long window much longer
 constexpr uint64_t STATIC_COPY_WAIT_NS = 2000000000ull;
@@ -268,9 +269,15 @@ inline void setSingleLayout(Params<R>& P, const SmemLayout& L) {
     P.smStage = (int)staticStageOffset(L.total);
 }
 
-template <typename R, bool REPLAY, bool LOG, int TM>
+// LEAN = K >= 0 (single-instance, shared field, every subdomain tallying
+// along axis K, no replay, no log): the phonons of the back range, whose
+// next event lies beyond this window, take leanFlight; the walker runs for
+// the front range, for a back-range phonon that does meet an event, and in
+// the window that ends the horizon.
+template <typename R, bool REPLAY, bool LOG, int TM, int LEAN>
 __global__ void __launch_bounds__(STATIC_MAX_THREADS, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
 k_advance(Params<R> P) {
+    static_assert(LEAN < 0 || (!REPLAY && !LOG && TM == TM_SHARED), "the lean flight needs a plain shared-field launch");
     using V4 = typename Vec4<R>::T;
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ uint64_t barFull[STATIC_STAGES], barEmpty[STATIC_STAGES];
@@ -333,7 +340,7 @@ k_advance(Params<R> P) {
                     src = rbase + C - (long long)nB + k * T;
                     cnt = (unsigned)min((long long)T, (long long)nB - k * T);
                 }
-                sCnt[s] = cnt;
+                sCnt[s] = cnt | (j >= tF ? STATIC_BACK : 0u);
                 unsigned char* st = stage0 + (size_t)s * sbytes;
                 mbarArriveExpectTx(&barFull[s], cnt * perPhonon);
                 bulkLoad(st, P.P0in + src, cnt * (uint32_t)sizeof(V4), &barFull[s]);
@@ -361,8 +368,10 @@ k_advance(Params<R> P) {
                 if (lane == 0) { atomicOr(P.status, (unsigned)S_TIMEOUT); sStop = 1; }
                 break;
             }
-            const unsigned cnt = sCnt[s];
-            if (cnt == STATIC_END) break;
+            const unsigned tag = sCnt[s];
+            if (tag == STATIC_END) break;
+            const unsigned cnt = tag & ~STATIC_BACK;
+            const bool back = (tag & STATIC_BACK) != 0;
             const int i = threadIdx.x;
             V4 A0, A1;
             uint4 A2;
@@ -377,7 +386,23 @@ k_advance(Params<R> P) {
             if (lane == 0) mbarArrive(&barEmpty[s]);
             if (__ballot_sync(0xFFFFFFFFu, have) == 0) continue;
             bool alive = false, soon = false;
-            if (have) {
+            int lean = LEAN_EVENT;
+            if constexpr (LEAN >= 0) {
+                if (have && back && !W.last) {
+                    R tnext;
+                    lean = leanFlight<R, (LEAN >= 0 ? LEAN : 0), ParamView<R, TM>>(V, W, A0, A1, A2, tnext);
+                    if (lean != LEAN_EVENT) {
+                        nSteps += (unsigned)W.keff;
+                        alive = lean == LEAN_ALIVE;
+                        soon = tnext < W.next;
+                        if (!alive) {  // as Walker::close for a non-finite state
+                            blkCount(C_BAD, 1);
+                            atomicOr(P.status, (unsigned)S_NONFINITE);
+                        }
+                    }
+                }
+            }
+            if (have && lean == LEAN_EVENT) {
                 Walker<R, REPLAY, LOG, TM, ParamView<R, TM>> wk;
                 wk.load(P, V, W, A0, A1, A2);
                 while (!wk.iterate(P, W)) {}

@@ -19,6 +19,12 @@ cudaError_t launchAdvance(const Params<R>& p, bool dyn, bool replay, bool log, i
 template <typename R>
 cudaError_t launchCompact(const Params<R>& p, int grid, cudaStream_t s);
 
+// static kernel with the lean flight of a 1-D shared field along axis lean
+template <typename R>
+cudaError_t launchAdvanceLean(const Params<R>& p, int lean, int grid, int block, size_t smem, cudaStream_t s);
+template <typename R>
+int advanceLeanOccupancy(int lean, int block, size_t smem);
+
 // batched launches (all instances in one kernel)
 template <typename R>
 cudaError_t launchEmitBatch(const Params<R>& p, cudaStream_t s);

@@ -14,7 +14,7 @@ static cudaError_t prepare(K fn, size_t smem) {
 
 template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
 static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t smem, cudaStream_t s) {
-    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM, -1>;
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
     // the static kernel adds its producer warp to the `block` consumers
@@ -24,11 +24,36 @@ static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t sm
 
 template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
 static int occOne(int block, size_t smem) {
-    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM>;
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM, -1>;
     if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, DYN ? block : block + STATIC_PRODUCER_THREADS, smem) !=
         cudaSuccess)
+        return 0;
+    return nb;
+}
+
+// The static kernel with the lean flight along axis `lean` (0..2).
+template <>
+cudaError_t launchAdvanceLean<MC_REAL>(const Params<MC_REAL>& p, int lean, int grid, int block, size_t smem,
+                                       cudaStream_t s) {
+    auto fn = lean == 0 ? k_advance<MC_REAL, false, false, TM_SHARED, 0>
+            : lean == 1 ? k_advance<MC_REAL, false, false, TM_SHARED, 1>
+                        : k_advance<MC_REAL, false, false, TM_SHARED, 2>;
+    cudaError_t e = prepare(fn, smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, block + STATIC_PRODUCER_THREADS, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <>
+int advanceLeanOccupancy<MC_REAL>(int lean, int block, size_t smem) {
+    auto fn = lean == 0 ? k_advance<MC_REAL, false, false, TM_SHARED, 0>
+            : lean == 1 ? k_advance<MC_REAL, false, false, TM_SHARED, 1>
+                        : k_advance<MC_REAL, false, false, TM_SHARED, 2>;
+    if (prepare(fn, smem) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block + STATIC_PRODUCER_THREADS, smem) != cudaSuccess)
         return 0;
     return nb;
 }

@@ -930,6 +930,67 @@ struct Walker {
     }
 };
 
+// Outcome of leanFlight.
+enum { LEAN_EVENT = 0, LEAN_ALIVE = 1, LEAN_BAD = 2 };
+
+// One window of a phonon whose next event lies beyond the window end, in a
+// single-instance launch with a shared field whose subdomains all tally
+// along axis K (a 1-D field). It is Walker::load, the first
+// Walker::iterate and Walker::close of such a phonon, operation for
+// operation (the same arithmetic in the same order, so the same results),
+// without the walker's event handling, loop and bookkeeping. Returns
+// LEAN_EVENT, having changed nothing, if the phonon does meet an event in
+// the window (the caller then runs the walker); otherwise the flight is
+// tallied, the state packed back into A0..A2, *tnext set to the time from
+// the window end to the next event, and LEAN_ALIVE returned (LEAN_BAD for a
+// non-finite free path, which the caller counts as the walker would).
+template <typename R, int K, typename IA>
+__device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typename Vec4<R>::T& A0,
+                                          typename Vec4<R>::T& A1, uint4& A2, R& tnext) {
+    Phn<R> ph;
+    unpackCell(A2.x, ph.s, ph.idx);
+    ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
+    ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
+    ph.id = realToId<R>(A1.w);
+    ph.w = (int)(A2.y & 0xFFFFu);
+    ph.p = (int)((A2.y >> 16) & 0xFFu);
+    ph.neg = (A2.y >> 24) & 1u;
+    ph.nscat = A2.z;
+    ph.nloop = A2.w;
+    const SdomD<R>& S = I.sd()[ph.s];
+    R a[3], ia[3];
+    reducedVel(S, ph.d, a, ia);
+    const R v = I.vel()[ph.w * I.np() + ph.p];
+    const R iv = R(1) / v;
+    R sev = ph.scatNext;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const R dist = (-(R)ph.idx[k] - ph.off[k]) * ia[k];
+        if (a[k] < R(0) && dist < sev) sev = dist;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const R dist = (((R)(S.shape[k] - ph.idx[k])) - ph.off[k]) * ia[k];
+        if (a[k] > R(0) && dist < sev) sev = dist;
+    }
+    if (sev * iv <= W.len) return LEAN_EVENT;
+    const R s = W.len * v;
+    Tally<R, TM_SHARED, IA> T;
+    T.V = I;
+    T.goff = 0;
+    const R sg = ph.neg ? R(-1) : R(1);
+    if (I.problem() == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
+    else if (I.problem() == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
+    else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
+    fly1d<R, TM_SHARED, K, IA>(ph, S, a, ia, s, T);
+    ph.scatNext -= s;
+    if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
+    tnext = (sev - s) * iv;
+    if (!(ph.scatNext == ph.scatNext)) return LEAN_BAD;
+    packPhonon(ph, A0, A1, A2);
+    return LEAN_ALIVE;
+}
+
 // Add the block's counters to the launch counters (after a barrier).
 __device__ __forceinline__ void flushCounts(unsigned long long* counters) {
     for (int q = threadIdx.x; q < C_NCOUNTERS; q += blockDim.x)

@@ -270,3 +270,42 @@ def test_determinism(gmat):
     b = P.solve(dt=0.5e-12, nsteps=300, precision=32, steps_per_launch=30, seed=9)
     assert P.stats["events"] == ea
     assert field_err(a, b) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["film", "cross", "bulk"])
+@pytest.mark.parametrize("prec", [32, 64])
+def test_lean_flight_matches_the_walker(name, prec, gmat):
+    """The per-step static kernel takes a lean straight-line flight for the
+    phonons with no event in the window when the field is 1-D along one
+    axis and no event log is kept; with a log it runs the walker for every
+    phonon. The two must agree: the lean flight repeats the walker's
+    arithmetic and each block's fixed-point field is exact, so counters are
+    equal and fields differ only by the order of the FP64 atomics that add
+    the blocks' fields (1e-13 of each row's scale)."""
+    dom = domains()[name]
+    kind, nemit, dt, nsteps = CASES[name]
+    P = PROBLEM[kind](gmat, dom, 4 * nemit, 10**6)
+    kw = dict(dt=dt, nsteps=min(nsteps, 300), precision=prec, steps_per_launch=1, schedule=1, seed=31)
+    lean = P.solve(**kw)
+    sl = dict(P.stats)
+    walker = P.solve(log_cap=4, log_phonons=1, **kw)
+    sw = dict(P.stats)
+    for k in ("events", "scatters", "absorbed", "horizon_stops", "phonon_steps", "nonfinite", "escapes"):
+        assert sl[k] == sw[k], k
+    assert field_err(walker, lean) < 1e-13
+    assert np.allclose(sl["checksum"], sw["checksum"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("name", ["film", "cross"])
+def test_fp64_plain_kernel_against_oracle_without_log(name, gmat, omat):
+    """The per-step kernel with the lean flight in FP64 against the oracle:
+    event counts exact, field within 1e-9 of each row's scale."""
+    dom = domains()[name]
+    kind, nemit, dt, nsteps = CASES[name]
+    o, ost, _ = O.solve(omat, O.ODomain(dom), kind, nemit=nemit, maxscat=10**6, dt=dt, horizon=dt * nsteps,
+                        rng=O.RNG_PHILOX, seed=7)
+    P = PROBLEM[kind](gmat, dom, nemit, 10**6)
+    g = P.solve(dt=dt, nsteps=nsteps, precision=64, steps_per_launch=1, schedule=1, seed=7)
+    assert P.stats["events"] == ost["events"]
+    assert P.stats["phonon_steps"] == ost["phonon_steps"]
+    assert field_err(o, g) < 1e-9
