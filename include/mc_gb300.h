@@ -99,11 +99,18 @@ int mc_domain_cell_volumes(mc_domain_h d, double* out);
 void mc_domain_destroy(mc_domain_h d);
 
 /* -------------------------------------------------------------- problem */
-enum { MC_TEMP = 0, MC_FLUX = 1, MC_MULTI = 2 };
+/* MC_CUMTEMP / MC_CUMFLUX: CumTempProblem / CumFluxProblem
+ * (montecarlo/problem.h:205-239): Temp / Flux binned by the scatter count
+ * before each flight, cum_size + 1 bins of ceil((maxscat - 1) / cum_size)
+ * scatters (bin 0: not yet scattered), returned as cumulative sums over
+ * the bins (rows cum_size + 1, or 3 (cum_size + 1) with x, y, z per bin). */
+enum { MC_TEMP = 0, MC_FLUX = 1, MC_MULTI = 2, MC_CUMTEMP = 3, MC_CUMFLUX = 4 };
 enum { MC_TALLY_AUTO = -1, MC_TALLY_SHARED = 0, MC_TALLY_GLOBAL = 1 };
 
 typedef struct {
-    int problem;            /* MC_TEMP (1 row), MC_FLUX (3), MC_MULTI (4)   */
+    int problem;            /* MC_TEMP (1 row), MC_FLUX (3), MC_MULTI (4),
+                               MC_CUMTEMP (cum_size + 1), MC_CUMFLUX
+                               (3 (cum_size + 1))                          */
     long nemit;             /* requested phonons (montecarlo/problem.cpp:329-337 rounding) */
     long maxscat;
     long maxloop;           /* 0 -> 100 * maxscat (montecarlo/problem.cpp:339) */
@@ -134,6 +141,8 @@ typedef struct {
                                lane refill with in-place state             */
     int compact_interval;   /* dynamic schedule: compact dead slots every
                                this many launches (0: never)               */
+    long cum_size;          /* MC_CUMTEMP / MC_CUMFLUX: bins after the first
+                               (the reference's `size`, >= 1; maxscat >= 2) */
 } mc_problem_desc;
 
 enum { MC_SCHED_AUTO = 0, MC_SCHED_STATIC = 1, MC_SCHED_DYNAMIC = 2 };
@@ -158,6 +167,17 @@ typedef struct {
  * (montecarlo/main.cpp:162-165): out is rows x cols column-major and holds
  * power * postProc(tally) / cellVol. Host buffers; synchronous. */
 int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st);
+
+/* Repeated solves and their statistics: solveField(prob, nsim) followed by
+ * calcStats (montecarlo/main.cpp:181-210) with Statistics' Welford update
+ * (montecarlo/field.cpp:226-262). Replica i runs the problem with Philox key
+ * p->seed + i (the reference seeds each run from random_device). mean and
+ * sd (may be NULL) receive the cell-by-cell mean and sample standard
+ * deviation (n - 1; zero for one replica), rows x cols column-major; st
+ * (may be NULL) sums the replicas' counters and checksums. Replay streams
+ * and logs are refused (MC_ERR_UNSUPPORTED). Host buffers; synchronous. */
+int mc_solve_replicas(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, long nsim, double* mean, double* sd,
+                      mc_stats* st);
 
 /* Size of the fixed device scratch array behind mc_solve_noalloc: 32 MiB,
  * held on every device that loads this library until the process exits. */

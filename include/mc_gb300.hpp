@@ -6,6 +6,8 @@
 //   FilmDomain(dim, div, dT), BulkDomain(...)  montecarlo/domain.h:93-137
 //   TempProblem / FluxProblem / MultiProblem
 //       (mat, dom, nemit, maxscat, maxloop)   montecarlo/problem.h:157-203
+//   CumTempProblem / CumFluxProblem (mat, dom, nemit, size, maxscat, maxloop)
+//                                         montecarlo/problem.h:205-239
 // FieldProblem::solve() returns the rows x cols field in the column-major
 // layout of Eigen::ArrayXXd (montecarlo/problem.cpp:370-445); errors that the
 // reference turns into BOOST_ASSERT_MSG aborts are thrown as mcgb::Error.
@@ -144,12 +146,23 @@ struct RunOptions {
 
 class FieldProblem {
 public:
-    FieldProblem(const Material& mat, const Domain& dom, long nemit, long maxscat, long maxloop, int kind)
-        : mat_(mat), dom_(dom), nemit_(nemit), maxscat_(maxscat), maxloop_(maxloop), kind_(kind) {
+    FieldProblem(const Material& mat, const Domain& dom, long nemit, long maxscat, long maxloop, int kind,
+                 long size = 0)
+        : mat_(mat), dom_(dom), nemit_(nemit), maxscat_(maxscat), maxloop_(maxloop), kind_(kind), size_(size) {
         if (nemit <= 0 || maxscat <= 0 || maxloop < 0) throw Error(MC_ERR_ARG, "Invalid problem arguments");
+        if ((kind == MC_CUMTEMP || kind == MC_CUMFLUX) && (size < 1 || maxscat < 2))
+            throw Error(MC_ERR_ARG, "Invalid problem arguments");
     }
     virtual ~FieldProblem() = default;
-    long rows() const { return kind_ == MC_TEMP ? 1 : (kind_ == MC_FLUX ? 3 : 4); }
+    long rows() const {
+        switch (kind_) {
+        case MC_TEMP: return 1;
+        case MC_FLUX: return 3;
+        case MC_MULTI: return 4;
+        case MC_CUMTEMP: return size_ + 1;
+        default: return 3 * (size_ + 1);
+        }
+    }
 
     // all phonons on the GPU; column-major rows x cols
     std::vector<double> solve(const RunOptions& o = RunOptions(), mc_stats* stats = nullptr) const {
@@ -165,6 +178,7 @@ public:
         d.seed = o.seed;
         d.steps_per_launch = o.stepsPerLaunch > 0 ? o.stepsPerLaunch : (int)o.nsteps;
         d.tally_mode = MC_TALLY_AUTO;
+        d.cum_size = size_;
         std::vector<double> out((size_t)(rows() * dom_.cols()));
         mc_stats st;
         check(mc_solve(mat_.handle(), dom_.handle(), &d, out.data(), &st));
@@ -177,6 +191,7 @@ private:
     const Domain& dom_;
     long nemit_, maxscat_, maxloop_;
     int kind_;
+    long size_;
 };
 
 struct TempProblem : FieldProblem {
@@ -190,6 +205,15 @@ struct FluxProblem : FieldProblem {
 struct MultiProblem : FieldProblem {
     MultiProblem(const Material& m, const Domain& d, long nemit, long maxscat, long maxloop = 0)
         : FieldProblem(m, d, nemit, maxscat, maxloop, MC_MULTI) {}
+};
+// montecarlo/problem.h:205-239 (argument order of the reference's constructors)
+struct CumTempProblem : FieldProblem {
+    CumTempProblem(const Material& m, const Domain& d, long nemit, long size, long maxscat, long maxloop = 0)
+        : FieldProblem(m, d, nemit, maxscat, maxloop, MC_CUMTEMP, size) {}
+};
+struct CumFluxProblem : FieldProblem {
+    CumFluxProblem(const Material& m, const Domain& d, long nemit, long size, long maxscat, long maxloop = 0)
+        : FieldProblem(m, d, nemit, maxscat, maxloop, MC_CUMFLUX, size) {}
 };
 
 }  // namespace mcgb

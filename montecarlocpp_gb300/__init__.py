@@ -3,7 +3,7 @@ montecarlocpp deviational phonon Monte Carlo solver.
 
 The compute path is libmc_gb300.so (hand-written CUDA kernels behind the C
 ABI in include/mc_gb300.h). This package mirrors the reference's host API
-(Material, *Domain, Temp/Flux/MultiProblem) over that ABI.
+(Material, *Domain, Temp/Flux/Multi/CumTemp/CumFluxProblem) over that ABI.
 """
 
 from .batch import Batch
@@ -11,13 +11,14 @@ from .serve import Server
 from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PERI, RIG, SPEC, TOP, BulkDomain,
                       CrossPlaneFilmDomain, Domain, FilmDomain, Pair, Parallelepiped, PoreCellDomain)
 from .materials import SiliconModel, silicon_tables, write_material_files
-from .problem import (FLUX, MULTI, TEMP, FluxProblem, Material, MultiProblem, Session,
-                      TempProblem, kappa_from_flux)
+from .problem import (CUMFLUX, CUMTEMP, FLUX, MULTI, TEMP, CumFluxProblem, CumTempProblem, FluxProblem,
+                      Material, MultiProblem, Session, TempProblem, kappa_from_flux)
 
 __all__ = [
     "BAC", "LEF", "BOT", "FRO", "RIG", "TOP", "SPEC", "DIFF", "ISOT", "PERI", "INTER",
     "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "Pair",
     "Parallelepiped", "SiliconModel", "silicon_tables", "write_material_files", "Material",
-    "TempProblem", "FluxProblem", "MultiProblem", "Session", "TEMP", "FLUX", "MULTI",
+    "TempProblem", "FluxProblem", "MultiProblem", "CumTempProblem", "CumFluxProblem", "Session", "TEMP",
+    "FLUX", "MULTI", "CUMTEMP", "CUMFLUX",
     "kappa_from_flux", "Batch", "Server",
 ]

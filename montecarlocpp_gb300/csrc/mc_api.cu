@@ -459,6 +459,55 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
     return MC_OK;
 }
 
+// Field rows of a problem (montecarlo/problem.cpp:470-471,502-503,535-536,
+// 578-581,615-618): Temp 1, Flux 3, Multi 4, CumTemp size + 1, CumFlux
+// 3 (size + 1).
+long problemRows(int problem, long size) {
+    switch (problem) {
+    case MC_TEMP: return 1;
+    case MC_FLUX: return 3;
+    case MC_MULTI: return 4;
+    case MC_CUMTEMP: return size + 1;
+    default: return 3 * (size + 1);
+    }
+}
+// CumTemp / CumFlux scatters per bin, ceil((maxscat - 1) / size)
+// (montecarlo/problem.cpp:558-564); 1 for the other problems.
+int cumStepOf(int problem, long maxscat, long size) {
+    if (problem != MC_CUMTEMP && problem != MC_CUMFLUX) return 1;
+    return (int)((maxscat - 1 + size - 1) / size);
+}
+// Whether row class k (see rowClass) holds times rather than displacements.
+bool timeClass(int problem, int k) {
+    return problem == MC_CUMTEMP || ((problem == MC_TEMP || problem == MC_MULTI) && k == 0);
+}
+// Problem arguments the kernels need (the reference asserts or divides by
+// zero otherwise).
+int checkProblem(const mc_problem_desc& p) {
+    if (p.problem < MC_TEMP || p.problem > MC_CUMFLUX) return fail(MC_ERR_ARG, "Invalid problem");
+    if (p.problem == MC_CUMTEMP || p.problem == MC_CUMFLUX) {
+        if (p.cum_size < 1) return fail(MC_ERR_ARG, "cum_size must be >= 1");
+        if (p.maxscat < 2) return fail(MC_ERR_ARG, "CumTemp / CumFlux need maxscat >= 2");
+        if (p.cum_size > (1L << 20)) return fail(MC_ERR_ARG, "cum_size too large");
+    }
+    return MC_OK;
+}
+// postProc of the summed raw field, rows x cols column-major, in place
+// (montecarlo/problem.cpp:478-481,511-514,546-551,598-606,636-645): the
+// cumulative sums over the scatter-count bins, then the division of the
+// time rows by the material's energy sum.
+void postProcess(int problem, long rows, long cols, double energySum, double* v) {
+    if (problem == MC_CUMTEMP || problem == MC_CUMFLUX) {
+        const long per = problem == MC_CUMTEMP ? 1 : 3;
+        for (long c = 0; c < cols; ++c)
+            for (long r = per; r < rows; ++r) v[c * rows + r] += v[c * rows + r - per];
+    }
+    for (long c = 0; c < cols; ++c)
+        for (long r = 0; r < rows; ++r)
+            if (problem == MC_TEMP || problem == MC_CUMTEMP || (problem == MC_MULTI && r == 0))
+                v[c * rows + r] /= energySum;
+}
+
 template <typename R>
 void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
     std::memset(&b, 0, sizeof(b));
@@ -623,9 +672,10 @@ int setupSession(mc_session_s* S) {
     // counters: C_NCOUNTERS + two (front, back) live-count pairs
     CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
     CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
-    S->rows = S->desc.problem == MC_TEMP ? 1 : (S->desc.problem == MC_FLUX ? 3 : 4);
+    S->rows = (int)problemRows(S->desc.problem, S->desc.cum_size);
     CK(cudaMalloc(&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L)));
     P.problem = S->desc.problem; P.rows = S->rows; P.cols = (int)D.cols;
+    P.cumStep = cumStepOf(S->desc.problem, S->desc.maxscat, S->desc.cum_size);
     P.nemit = S->nemit;
     P.maxscat = S->desc.maxscat;
     P.maxloop = S->maxloop;
@@ -777,8 +827,7 @@ void setQuanta(const mc_session_s* S, Params<R>& P) {
     const double window = (double)keff * S->desc.dt;
     const double perBlock = std::ceil((double)S->nemit / ((double)S->grid * S->block)) * S->block;
     for (int r = 0; r < 4; ++r) {
-        const bool timeRow = (S->desc.problem == MC_TEMP && r == 0) || (S->desc.problem == MC_MULTI && r == 0);
-        const double q = tallyQuantum(sizeof(R) == 4, window * (timeRow ? 1.0 : S->vmax), perBlock);
+        const double q = tallyQuantum(sizeof(R) == 4, window * (timeClass(S->desc.problem, r) ? 1.0 : S->vmax), perBlock);
         P.tq[r] = q;
         P.tqinv[r] = (R)(1.0 / q);
     }
@@ -849,13 +898,11 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
     if (out) {
         std::vector<double> t(nval);
         if (nval) CK(cudaMemcpy(t.data(), S->tally_d, sizeof(double) * nval, cudaMemcpyDeviceToHost));
-        // postProc and / cellVol (montecarlo/problem.cpp:439-444,478-551)
+        // postProc and / cellVol (montecarlo/problem.cpp:439-444,478-648)
+        postProcess(S->desc.problem, S->rows, D.cols, m.energySum, t.data());
         for (long col = 0; col < D.cols; ++col)
-            for (int r = 0; r < S->rows; ++r) {
-                double v = t[(size_t)col * S->rows + r];
-                if (S->desc.problem == MC_TEMP || (S->desc.problem == MC_MULTI && r == 0)) v = v / m.energySum;
-                out[(size_t)col * S->rows + r] = S->power * (v / D.cellVol[col]);
-            }
+            for (int r = 0; r < S->rows; ++r)
+                out[(size_t)col * S->rows + r] = S->power * (t[(size_t)col * S->rows + r] / D.cellVol[col]);
     }
     if (S->logging && S->desc.log && S->desc.log_counts) {
         long long ln = std::min<long long>(S->desc.log_phonons, S->nemit);
@@ -1044,7 +1091,7 @@ int setupBatch(mc_batch_s* B) {
     size_t off = 0;
     for (int i = 0; i < n; ++i) {
         const mc_problem_desc& p = B->probs[i];
-        B->rows[i] = p.problem == MC_TEMP ? 1 : (p.problem == MC_FLUX ? 3 : 4);
+        B->rows[i] = (int)problemRows(p.problem, p.cum_size);
         B->cols[i] = (int)B->doms[i]->cols;
         B->fieldOff[i] = off;
         off += (size_t)B->rows[i] * B->cols[i] + (size_t)B->rows[i] * (B->cols[i] + 1) + 4;
@@ -1069,6 +1116,7 @@ int setupBatch(mc_batch_s* B) {
         I.sd = P.sd; I.em = P.em; I.emitCdf = P.emitCdf;
         I.nw = P.nw; I.np = P.np; I.nem = P.nem; I.nsd = P.nsd;
         I.problem = pd.problem; I.rows = B->rows[i]; I.cols = B->cols[i]; I.inst = i;
+        I.cumStep = cumStepOf(pd.problem, pd.maxscat, pd.cum_size);
         I.maxscat = pd.maxscat;
         I.maxloop = pd.maxloop != 0 ? pd.maxloop : 100 * pd.maxscat;
         I.slot0 = islot[i]; I.nemit = B->nemit[i];
@@ -1083,13 +1131,12 @@ int setupBatch(mc_batch_s* B) {
         I.gstride = 0;
         // a block's shared field takes at most the instance's phonons
         for (int r = 0; r < 4; ++r) {
-            const bool timeRow = (pd.problem == MC_TEMP || pd.problem == MC_MULTI) && r == 0;
-            const double q = tallyQuantum(sizeof(R) == 4, window * (timeRow ? 1.0 : vmax), (double)B->nemit[i]);
+            const double q = tallyQuantum(sizeof(R) == 4, window * (timeClass(pd.problem, r) ? 1.0 : vmax), (double)B->nemit[i]);
             I.tq[r] = q;
             I.tqinv[r] = (R)(1.0 / q);
         }
         if (pd.maxscat <= 0 || pd.maxloop < 0 || pd.nemit <= 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
-        if (pd.problem < MC_TEMP || pd.problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+        if (int rcp = checkProblem(pd)) return rcp;
     }
     B->cap = islot[n];
     Params<R>& P = batchParams<R>(B);
@@ -1128,6 +1175,8 @@ int setupBatch(mc_batch_s* B) {
     P.islot = B->islot;
     P.ninst = n;
     P.maxGroups = 1;
+    P.maxRows = 1;
+    for (int i = 0; i < n; ++i) P.maxRows = std::max(P.maxRows, B->rows[i]);
     B->block = B->bd.block_size > 0 ? B->bd.block_size : 256;
     if (B->block % 32 || B->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
     int dev = 0, nsm = 0;
@@ -1348,6 +1397,7 @@ struct ServerT : ServerBase {
         base.insts = insts_d;
         base.islot = islot_d;
         base.maxGroups = d.groups;
+        base.maxRows = 4;
         block = d.block_size > 0 ? d.block_size : 256;
         if (block % 32 || block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1706,7 +1756,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     }
     S->nemit = (long)tot;
     S->power = wsum / (double)tot * m.fluxSum / 4.;
-    S->rows = S->desc.problem == MC_TEMP ? 1 : (S->desc.problem == MC_FLUX ? 3 : 4);
+    S->rows = (int)problemRows(S->desc.problem, S->desc.cum_size);
     const size_t nt = (size_t)m.nw * m.np, n = (size_t)S->nemit;
     const size_t nval = (size_t)S->rows * std::max(D.cols, 1L);
     size_t off = 0;
@@ -1794,6 +1844,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     S->tally_d = (double*)(base + oTally);
     S->csum_d = (double*)(base + oCsum);
     P.problem = S->desc.problem; P.rows = S->rows; P.cols = (int)D.cols;
+    P.cumStep = cumStepOf(S->desc.problem, S->desc.maxscat, S->desc.cum_size);
     P.nemit = S->nemit;
     P.maxscat = S->desc.maxscat;
     P.maxloop = S->maxloop;
@@ -1889,7 +1940,7 @@ void mc_domain_destroy(mc_domain_h d) { delete d; }
 
 int mc_session_create(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, mc_session_h* out) {
     if (!m || !d || !p || !out) return fail(MC_ERR_ARG, "null argument");
-    if (p->problem < MC_TEMP || p->problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+    if (int rcp = checkProblem(*p)) return rcp;
     if (p->nemit <= 0 || p->maxscat <= 0 || p->maxloop < 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
     if (!(p->dt > 0.) || p->nsteps <= 0 || p->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
     if (p->steps_per_launch <= 0) return fail(MC_ERR_ARG, "steps_per_launch must be >= 1");
@@ -1963,13 +2014,68 @@ int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* o
     return rc;
 }
 
+// Replicas (montecarlo/main.cpp:181-210): nsim solves of one session whose
+// Philox key is seed + i for replica i, folded into Statistics' Welford
+// mean and sum of squared deviations (montecarlo/field.cpp:226-262).
+int mc_solve_replicas(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, long nsim, double* mean, double* sd,
+                      mc_stats* st) {
+    if (!m || !d || !p || !mean || nsim < 1) return fail(MC_ERR_ARG, "mc_solve_replicas: null argument or nsim < 1");
+    if (p->replay_words || p->replay_offsets || p->log)
+        return fail(MC_ERR_UNSUPPORTED, "mc_solve_replicas: replicas take neither replay streams nor logs");
+    mc_session_h s = nullptr;
+    int rc = mc_session_create(m, d, p, &s);
+    if (rc) return rc;
+    const size_t nval = (size_t)s->rows * (size_t)s->dom->cols;
+    std::vector<double> x(nval), mu(nval, 0.), m2(nval, 0.);
+    mc_stats tot;
+    std::memset(&tot, 0, sizeof(tot));
+    for (long i = 0; i < nsim && !rc; ++i) {
+        const uint64_t seed = p->seed + (uint64_t)i;
+        s->desc.seed = seed;
+        s->p32.key0 = s->p64.key0 = (uint32_t)seed;
+        s->p32.key1 = s->p64.key1 = (uint32_t)(seed >> 32);
+        rc = mc_session_emit(s);
+        int done = 0;
+        while (!rc && !done) rc = mc_session_advance(s, 64, &done);
+        mc_stats one;
+        if (!rc) rc = mc_session_result(s, x.data(), &one);
+        if (rc) break;
+        // Statistics::add
+        const double n = (double)(i + 1);
+        for (size_t k = 0; k < nval; ++k) {
+            const double dl = x[k] - mu[k];
+            mu[k] += dl / n;
+            m2[k] += dl * (x[k] - mu[k]);
+        }
+        if (i == 0) tot = one;
+        else {
+            tot.phonon_steps += one.phonon_steps; tot.events += one.events; tot.scatters += one.scatters;
+            tot.escapes += one.escapes; tot.horizon_stops += one.horizon_stops; tot.maxscat_stops += one.maxscat_stops;
+            tot.maxloop_stops += one.maxloop_stops; tot.absorbed += one.absorbed; tot.nonfinite += one.nonfinite;
+            tot.status |= one.status; tot.launches += one.launches;
+            for (int r = 0; r < 4; ++r) tot.checksum[r] += one.checksum[r];
+        }
+    }
+    if (!rc) {
+        std::memcpy(mean, mu.data(), sizeof(double) * nval);
+        // Statistics::variance: s / (n - 1), zero below two replicas
+        if (sd)
+            for (size_t k = 0; k < nval; ++k) sd[k] = nsim < 2 ? 0. : std::sqrt(m2[k] / (double)(nsim - 1));
+        if (st) *st = tot;
+    }
+    std::string msg = g_err;
+    mc_session_destroy(s);
+    g_err = msg;
+    return rc;
+}
+
 // The solve of mc_solve with every device buffer inside g_noallocScratch:
 // a session object on the host stack whose pointers lead into the array,
 // driven through the same emission, advance and result steps. Nothing is
 // allocated on the device and nothing is freed.
 int mc_solve_noalloc(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* out, mc_stats* st) {
     if (!m || !d || !p) return fail(MC_ERR_ARG, "null argument");
-    if (p->problem < MC_TEMP || p->problem > MC_MULTI) return fail(MC_ERR_ARG, "Invalid problem");
+    if (int rcp = checkProblem(*p)) return rcp;
     if (p->nemit <= 0 || p->maxscat <= 0 || p->maxloop < 0) return fail(MC_ERR_ARG, "Invalid problem arguments");
     if (!(p->dt > 0.) || p->nsteps <= 0 || p->nsteps > (1L << 30)) return fail(MC_ERR_ARG, "dt and nsteps must be positive");
     if (p->steps_per_launch <= 0) return fail(MC_ERR_ARG, "steps_per_launch must be >= 1");
@@ -2048,12 +2154,11 @@ int mc_batch_result(mc_batch_h b, int i, double* out, mc_stats* st) {
     const mc_domain_s& D = *b->doms[i];
     const int problem = b->probs[i].problem;
     if (out) {
+        std::vector<double> v(f.begin(), f.begin() + (size_t)rows * cols);
+        postProcess(problem, rows, cols, m.energySum, v.data());
         for (int c = 0; c < cols; ++c)
-            for (int r = 0; r < rows; ++r) {
-                double v = f[(size_t)c * rows + r];
-                if (problem == MC_TEMP || (problem == MC_MULTI && r == 0)) v = v / m.energySum;
-                out[(size_t)c * rows + r] = b->power[i] * (v / D.cellVol[c]);
-            }
+            for (int r = 0; r < rows; ++r)
+                out[(size_t)c * rows + r] = b->power[i] * (v[(size_t)c * rows + r] / D.cellVol[c]);
     }
     if (st) {
         int rc = batchCounters(b, st);

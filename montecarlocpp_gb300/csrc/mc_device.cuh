@@ -78,6 +78,7 @@ struct Params {
     const unsigned long long* fpthr;
     // problem
     int problem, rows, cols;
+    int cumStep;  // CumTemp / CumFlux: scatters per bin, ceil((maxscat - 1) / size)
     long long nemit, maxscat, maxloop;
     R dt;
     int step0, ksteps, nsteps;
@@ -133,6 +134,7 @@ struct Params {
     const long long* islot;
     int ninst;
     int maxGroups;  // largest field-copy count of the instances
+    int maxRows;    // largest row count of the instances
     // work segments of a batched advance: each block starts on segment
     // home[block] and moves on to any segment with slots left; segNext[s]
     // counts the slots of segment s already claimed
@@ -163,6 +165,7 @@ struct InstD {
     const long long* emitCdf;         // cumulative phonons per emitter
     int nw, np, nem, nsd;
     int problem, rows, cols, inst;
+    int cumStep;                      // CumTemp / CumFlux scatters per bin
     long long maxscat, maxloop;
     long long slot0, nemit;           // the instance's state slots
     uint32_t key0, key1;

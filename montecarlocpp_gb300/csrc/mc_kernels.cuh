@@ -62,7 +62,7 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         I->fwthr = P.fwthr; I->fpthr = P.fpthr;
         I->sd = sd; I->em = P.em; I->emitCdf = P.emitCdf;
         I->nw = P.nw; I->np = P.np; I->nem = P.nem; I->nsd = P.nsd;
-        I->problem = P.problem; I->rows = P.rows; I->cols = P.cols; I->inst = 0;
+        I->problem = P.problem; I->rows = P.rows; I->cols = P.cols; I->inst = 0; I->cumStep = P.cumStep;
         I->maxscat = P.maxscat; I->maxloop = P.maxloop;
         I->slot0 = 0; I->nemit = P.nemit;
         I->key0 = P.key0; I->key1 = P.key1;
@@ -110,10 +110,11 @@ __device__ __forceinline__ void flushSharedField(const InstD<R>& I, double* dst)
         const int c = q / rows, r = q - c * rows;
         const long long x = I.tal[c * st + r];
         if (x != 0) {
+            const int k0 = rowClass(I.problem, r);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (k == r) part[k] += x;
-            atomicAdd(&dst[q], (double)x * I.tq[r]);
+                if (k == k0) part[k] += x;
+            atomicAdd(&dst[q], (double)x * I.tq[k0]);
             I.tal[c * st + r] = 0;
         }
     }
@@ -132,7 +133,7 @@ __device__ __forceinline__ void closeBlock(const Params<R>& P, const InstD<R>& I
     __syncthreads();
     if (TM == TM_SHARED) flushSharedField<R>(I, P.tally);
     __syncthreads();
-    if (threadIdx.x < I.rows && g_blk.csum[threadIdx.x] != 0)
+    if ((int)threadIdx.x < rowClasses(I.problem, I.rows) && g_blk.csum[threadIdx.x] != 0)
         atomicAdd(&P.csum[threadIdx.x], (double)g_blk.csum[threadIdx.x] * I.tq[threadIdx.x]);
     flushCounts(P.counters);
 }
@@ -586,7 +587,8 @@ __device__ __forceinline__ void flushBinding(const InstD<R>& I, int group) {
     __syncthreads();
     if (threadIdx.x < 4) {
         const long long x = g_blk.csum[threadIdx.x];
-        if (threadIdx.x < I.rows && x != 0) atomicAdd(&I.csum[4 * group + threadIdx.x], (double)x * I.tq[threadIdx.x]);
+        if ((int)threadIdx.x < rowClasses(I.problem, I.rows) && x != 0)
+            atomicAdd(&I.csum[4 * group + threadIdx.x], (double)x * I.tq[threadIdx.x]);
         g_blk.csum[threadIdx.x] = 0;
     }
 }
@@ -663,12 +665,13 @@ inline void setBatchLayout(Params<R>& P) {
     P.smStage = 0;
 }
 
-// Global difference arrays -> field: block (i, y) prefix-sums row y % 4 of
-// field copy y / 4 of instance i and adds it to that copy.
+// Global difference arrays -> field: block (i, y) prefix-sums row
+// y % maxRows of field copy y / maxRows of instance i and adds it to that
+// copy.
 template <typename R>
 __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
     const InstD<R>& I = P.insts[blockIdx.x];
-    const int r = blockIdx.y & 3, grp = blockIdx.y >> 2;
+    const int r = (int)(blockIdx.y % (unsigned)P.maxRows), grp = (int)(blockIdx.y / (unsigned)P.maxRows);
     if (r >= I.rows || grp >= I.groups || I.gdif == nullptr) return;
     const long long go = (long long)grp * I.gstride;
     const int lane = threadIdx.x;

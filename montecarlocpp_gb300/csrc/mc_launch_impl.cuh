@@ -93,7 +93,7 @@ cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int grid, int 
 
 template <>
 cudaError_t launchDifPrefix<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
-    k_difprefix<MC_REAL><<<dim3((unsigned)p.ninst, 4u * (unsigned)p.maxGroups), 32, 0, s>>>(p);
+    k_difprefix<MC_REAL><<<dim3((unsigned)p.ninst, (unsigned)p.maxRows * (unsigned)p.maxGroups), 32, 0, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -10,8 +10,20 @@ namespace mcg {
 // Face kinds, in the order of montecarlo/boundary.h:137-281.
 enum FaceKind { F_SPEC = 0, F_DIFF = 1, F_ISOT = 2, F_PERI = 3, F_INTER = 4 };
 
-// Tally problems (montecarlo/problem.h:157-203): rows 1, 3, 4.
-enum Problem { P_TEMP = 0, P_FLUX = 1, P_MULTI = 2 };
+// Tally problems (montecarlo/problem.h:157-239): rows 1, 3, 4, and for the
+// scatter-count binned CumTemp / CumFlux size + 1 and 3 (size + 1).
+enum Problem { P_TEMP = 0, P_FLUX = 1, P_MULTI = 2, P_CUMTEMP = 3, P_CUMFLUX = 4 };
+
+// Row class of field row r: the fixed-point quantum and the checksum it
+// uses (time rows of CumTemp all share class 0, the three flux components
+// of every CumFlux bin classes 0..2).
+__host__ __device__ inline int rowClass(int problem, int r) {
+    return problem == P_CUMTEMP ? 0 : (problem == P_CUMFLUX ? r % 3 : r);
+}
+// number of row classes (checksums) of a problem with `rows` rows
+__host__ __device__ inline int rowClasses(int problem, int rows) {
+    return problem == P_CUMTEMP ? 1 : (problem == P_CUMFLUX ? 3 : rows);
+}
 
 // Reason a phonon stopped (device counters).
 enum Counter {

@@ -217,6 +217,7 @@ struct InstView {
     __device__ __forceinline__ int rows() const { return I->rows; }
     __device__ __forceinline__ int cols() const { return I->cols; }
     __device__ __forceinline__ int problem() const { return I->problem; }
+    __device__ __forceinline__ int cumStep() const { return I->cumStep; }
     __device__ __forceinline__ int nw() const { return I->nw; }
     __device__ __forceinline__ int np() const { return I->np; }
     __device__ __forceinline__ bool talShared() const { return I->tal != nullptr; }
@@ -253,6 +254,7 @@ struct ParamView {
     __device__ __forceinline__ int rows() const { return P->rows; }
     __device__ __forceinline__ int cols() const { return P->cols; }
     __device__ __forceinline__ int problem() const { return P->problem; }
+    __device__ __forceinline__ int cumStep() const { return P->cumStep; }
     __device__ __forceinline__ int nw() const { return P->nw; }
     __device__ __forceinline__ int np() const { return P->np; }
     __device__ __forceinline__ bool talShared() const { return TM == TM_SHARED; }
@@ -297,6 +299,7 @@ struct BatchView {
     __device__ __forceinline__ int rows() const { return I->rows; }
     __device__ __forceinline__ int cols() const { return I->cols; }
     __device__ __forceinline__ int problem() const { return I->problem; }
+    __device__ __forceinline__ int cumStep() const { return I->cumStep; }
     __device__ __forceinline__ int nw() const { return I->nw; }
     __device__ __forceinline__ int np() const { return I->np; }
     __device__ __forceinline__ bool talShared() const { return (I->flags & IF_TAL_SHARED) != 0; }
@@ -329,8 +332,11 @@ template <typename R, int TM, typename IA>
 struct Tally {
     IA V;
     long long goff;  // offset of the phonon's field copy (global layouts)
-    // amount per metre of flight, rows entries: Temp sign/v; Flux sign*d
+    // amount per metre of flight of the flight's nAct rows, which are field
+    // rows rowBase .. rowBase + nAct - 1: Temp sign/v; Flux sign*d; Multi
+    // both; CumTemp / CumFlux those of the flight's scatter-count bin
     R rho[4];
+    int nAct, rowBase;
 
     __device__ __forceinline__ int rows() const { return V.rows(); }
     __device__ __forceinline__ bool shared() const {
@@ -344,28 +350,30 @@ struct Tally {
     // shared field and difference array, cell-major: row r of column c at
     // [c * talStride(rows) + r]
     __device__ __forceinline__ void atomShared(int r, int col, Fix v) const {
-        sharedAdd64(&V.tal()[col * talStride(V.rows()) + r], v);
+        sharedAdd64(&V.tal()[col * talStride(V.rows()) + rowBase + r], v);
     }
     __device__ __forceinline__ void atomRange(int r, int c0, int c1, Fix v) const {
-        long long* d = V.dif();
+        long long* d = V.dif() + rowBase + r;
         const int st = talStride(V.rows());
-        sharedAdd64(d + c0 * st + r, v);
-        sharedAdd64(d + c1 * st + r, -v);
+        sharedAdd64(d + c0 * st, v);
+        sharedAdd64(d + c1 * st, -v);
     }
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < V.rows()) atomicAdd(&V.tally()[goff + (size_t)col * V.rows() + r], toDouble(rho[r] * t));
+            if (r < nAct)
+                atomicAdd(&V.tally()[goff + (size_t)col * V.rows() + rowBase + r], toDouble(rho[r] * t));
     }
     // interior cells [c0, c1) of a 1-D walk (stride 1) each with path t
     __device__ __forceinline__ void addGlobalRange(int c0, int c1, R t) const {
         if (V.gdif()) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                if (r < V.rows()) {
+                if (r < nAct) {
                     const double v = toDouble(rho[r] * t);
-                    atomicAdd(&V.gdif()[goff + (size_t)r * (V.cols() + 1) + c0], v);
-                    atomicAdd(&V.gdif()[goff + (size_t)r * (V.cols() + 1) + c1], -v);
+                    const size_t row = (size_t)(rowBase + r) * (V.cols() + 1);
+                    atomicAdd(&V.gdif()[goff + row + c0], v);
+                    atomicAdd(&V.gdif()[goff + row + c1], -v);
                 }
             }
         } else {
@@ -373,6 +381,30 @@ struct Tally {
         }
     }
 };
+
+// The rows a flight adds to (montecarlo/problem.cpp:473-544,589-633, each
+// amount times the phonon's sign): the per-metre amounts rho and the rows'
+// place in the field, from the phonon's sign, 1/v, direction and scatter
+// count before the flight.
+template <typename R, int TM, typename IA>
+__device__ __forceinline__ void setFlightRows(Tally<R, TM, IA>& T, int problem, bool neg, R iv, const R d[3],
+                                              uint32_t nscat, int cumStep) {
+    const R sg = neg ? R(-1) : R(1);
+    T.rowBase = 0;
+    if (problem == P_TEMP) { T.nAct = 1; T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
+    else if (problem == P_FLUX) { T.nAct = 3; T.rho[0] = sg * d[0]; T.rho[1] = sg * d[1]; T.rho[2] = sg * d[2]; T.rho[3] = R(0); }
+    else if (problem == P_MULTI) { T.nAct = 4; T.rho[0] = sg * iv; T.rho[1] = sg * d[0]; T.rho[2] = sg * d[1]; T.rho[3] = sg * d[2]; }
+    else {
+        const int bin = (int)(((unsigned long long)nscat + (unsigned long long)cumStep - 1ull) / (unsigned long long)cumStep);
+        if (problem == P_CUMTEMP) {
+            T.nAct = 1; T.rowBase = bin;
+            T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0);
+        } else {
+            T.nAct = 3; T.rowBase = 3 * bin;
+            T.rho[0] = sg * d[0]; T.rho[1] = sg * d[1]; T.rho[2] = sg * d[2]; T.rho[3] = R(0);
+        }
+    }
+}
 
 // Reduced velocity a = S (M^-1 d) and its reciprocal.
 template <typename R>
@@ -426,7 +458,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
         // waits for another's branch
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            if (r < T.rows()) {
+            if (r < T.nAct) {
                 const Fix V = T.fixedOf(r, s);
                 const Fix F = T.fixedOf(r, tfirst);
                 const Fix I = T.fixedOf(r, inva);
@@ -444,7 +476,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
     } else {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < T.rows()) T.csumAdd(r, T.fixedOf(r, s));
+            if (r < T.nAct) T.csumAdd(r, T.fixedOf(r, s));
     }
     if (!T.shared()) {
         if (e == b) {
@@ -476,7 +508,7 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         // a single field column (or none): move only
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            if (r < T.rows()) {
+            if (r < T.nAct) {
                 const typename FixT<R>::T V = T.fixedOf(r, s);
                 if (acc == -1 && T.shared()) T.atomShared(r, cb, V);
                 else T.csumAdd(r, V);
@@ -495,7 +527,7 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
     if (!T.shared()) {
 #pragma unroll
         for (int r = 0; r < 4; ++r)
-            if (r < T.rows()) T.csumAdd(r, T.fixedOf(r, s));
+            if (r < T.nAct) T.csumAdd(r, T.fixedOf(r, s));
     }
     R rem = s;
     const int s0 = S.tstride[1], s01 = S.tstride[2];
@@ -514,7 +546,7 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         if (T.shared()) {
 #pragma unroll
             for (int r = 0; r < 4; ++r)
-                if (r < T.rows()) T.atomShared(r, col, T.fixedOf(r, tmin));
+                if (r < T.nAct) T.atomShared(r, col, T.fixedOf(r, tmin));
         } else {
             T.addGlobal(col, tmin);
         }
@@ -749,10 +781,7 @@ struct Walker {
         T.V = I;
         // field copy of this phonon (batch means), global fields only
         T.goff = (TM != TM_SHARED && I.groups() > 1) ? (long long)(ph.id % (uint32_t)I.groups()) * I.gstride() : 0;
-        const R sg = ph.neg ? R(-1) : R(1);
-        if (I.problem() == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
-        else if (I.problem() == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
-        else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
+        setFlightRows(T, I.problem(), ph.neg, iv, ph.d, ph.nscat, I.cumStep());
         const int sBefore = ph.s;
         int cellEnd = 0;
         fly<R, TM, IA>(ph, *S, a, ia, s, T);
@@ -978,10 +1007,7 @@ __device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typen
     Tally<R, TM_SHARED, IA> T;
     T.V = I;
     T.goff = 0;
-    const R sg = ph.neg ? R(-1) : R(1);
-    if (I.problem() == P_TEMP) { T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0); }
-    else if (I.problem() == P_FLUX) { T.rho[0] = sg * ph.d[0]; T.rho[1] = sg * ph.d[1]; T.rho[2] = sg * ph.d[2]; T.rho[3] = R(0); }
-    else { T.rho[0] = sg * iv; T.rho[1] = sg * ph.d[0]; T.rho[2] = sg * ph.d[1]; T.rho[3] = sg * ph.d[2]; }
+    setFlightRows(T, I.problem(), ph.neg, iv, ph.d, ph.nscat, I.cumStep());
     fly1d<R, TM_SHARED, K, IA>(ph, S, a, ia, s, T);
     ph.scatNext -= s;
     if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);

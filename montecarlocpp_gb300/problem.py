@@ -20,7 +20,7 @@ from . import _lib
 from .domains import Domain
 from .materials import silicon_tables
 
-TEMP, FLUX, MULTI = 0, 1, 2
+TEMP, FLUX, MULTI, CUMTEMP, CUMFLUX = 0, 1, 2, 3, 4
 TALLY_AUTO, TALLY_SHARED, TALLY_GLOBAL = -1, 0, 1
 
 
@@ -135,10 +135,11 @@ def _handle(dom):
 
 
 class FieldProblem:
-    """Common part of Temp/Flux/Multi problems (montecarlo/problem.h:121-147)."""
+    """Common part of the field problems (montecarlo/problem.h:121-147)."""
 
     kind = MULTI
     loopFactor = 100  # montecarlo/problem.h:124
+    size = 0          # CumTemp / CumFlux bins after the first
 
     def __init__(self, mat: Material, dom, nemit: int, maxscat: int, maxloop: int = 0):
         if nemit <= 0 or maxscat <= 0 or maxloop < 0:
@@ -150,7 +151,7 @@ class FieldProblem:
         self.stats = None
 
     def rows(self):
-        return {TEMP: 1, FLUX: 3, MULTI: 4}[self.kind]
+        return {TEMP: 1, FLUX: 3, MULTI: 4, CUMTEMP: self.size + 1, CUMFLUX: 3 * (self.size + 1)}[self.kind]
 
     def desc(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
              grid_blocks=0, tally_mode=TALLY_AUTO, replay=None, log_cap=0, log_phonons=0, stream=None,
@@ -179,6 +180,7 @@ class FieldProblem:
             log = (log, counts)
         d.stream = stream
         d.schedule, d.compact_interval = int(schedule), int(compact_interval)
+        d.cum_size = int(self.size)
         return d, keep, log
 
     def solve(self, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, block_size=0,
@@ -202,6 +204,22 @@ class FieldProblem:
         del keep
         return out.reshape(self.rows(), self.handle.cols, order="F")
 
+    def solve_replicas(self, nsim, *, dt, nsteps, seed=0, precision=32, steps_per_launch=0, schedule=0):
+        """solveField(prob, nsim) + calcStats (montecarlo/main.cpp:181-210):
+        nsim solves with seeds seed, seed + 1, ...; returns the cell-by-cell
+        mean and sample standard deviation (rows x cols each)."""
+        d, keep, _ = self.desc(dt=dt, nsteps=nsteps, seed=seed, precision=precision,
+                               steps_per_launch=steps_per_launch, schedule=schedule)
+        n = self.rows() * self.handle.cols
+        mean, sd = np.zeros(n), np.zeros(n)
+        st = _lib.Stats()
+        _lib.check(_lib.lib().mc_solve_replicas(self.mat.h, self.handle.h, C.byref(d), int(nsim), _dp(mean), _dp(sd),
+                                                C.byref(st)))
+        self.stats = st.as_dict()
+        del keep
+        shape = (self.rows(), self.handle.cols)
+        return mean.reshape(shape, order="F"), sd.reshape(shape, order="F")
+
     def session(self, **kw):
         return Session(self, **kw)
 
@@ -216,6 +234,31 @@ class FluxProblem(FieldProblem):
 
 class MultiProblem(FieldProblem):
     kind = MULTI
+
+
+class _CumProblem(FieldProblem):
+    """CumTempProblem / CumFluxProblem(mat, dom, nemit, size, maxscat,
+    maxloop=0) (montecarlo/problem.h:205-239): the field binned by the
+    scatter count before each flight into size + 1 bins of
+    ceil((maxscat - 1) / size) scatters, returned as cumulative sums over the
+    bins (the last bin holds the Temp / Flux field)."""
+
+    def __init__(self, mat: Material, dom, nemit: int, size: int, maxscat: int, maxloop: int = 0):
+        if size < 1 or maxscat < 2:
+            raise ValueError("Invalid problem arguments")
+        super().__init__(mat, dom, nemit, maxscat, maxloop)
+        self.size = int(size)
+
+    def step(self):
+        return -(-(self.maxscat - 1) // self.size)
+
+
+class CumTempProblem(_CumProblem):
+    kind = CUMTEMP
+
+
+class CumFluxProblem(_CumProblem):
+    kind = CUMFLUX
 
 
 class Session:

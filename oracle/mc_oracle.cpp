@@ -753,7 +753,15 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
     long maxscat = P->maxscat;
     long maxloop = P->maxloop != 0 ? P->maxloop : 100 * maxscat;
     double power = wsum / nemit * m.fluxSum / 4.;
-    long rows = P->problem == ORC_TEMP ? 1 : (P->problem == ORC_FLUX ? 3 : 4);
+    // CumTemp / CumFlux (montecarlo/problem.cpp:553-648): size + 1 bins of
+    // the scatter count before a flight, step = ceil((maxscat - 1) / size)
+    const bool cum = P->problem == ORC_CUMTEMP || P->problem == ORC_CUMFLUX;
+    if (P->problem < ORC_TEMP || P->problem > ORC_CUMFLUX) return -1;
+    if (cum && (P->cum_size < 1 || maxscat < 2)) return -1;
+    const long cumStep = cum ? (maxscat - 1 + P->cum_size - 1) / P->cum_size : 1;
+    long rows = P->problem == ORC_TEMP ? 1 : (P->problem == ORC_FLUX ? 3 : (P->problem == ORC_MULTI ? 4 : 0));
+    if (P->problem == ORC_CUMTEMP) rows = P->cum_size + 1;
+    if (P->problem == ORC_CUMFLUX) rows = 3 * (P->cum_size + 1);
     long cols = D.cols;
     double H = P->horizon;
     bool useH = H > 0.;
@@ -838,7 +846,8 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
             ph.dir = normalized(dir);
             drawScatNext(m, ph, g);
 
-            double amount[4];
+            std::vector<double> amountV((size_t)rows, 0.);
+            double* amount = amountV.data();
             for (long i = 0; i < maxloop; ++i) {
                 g.setEvent((uint32_t)(i + 1));
                 Phonon pre = ph;
@@ -887,7 +896,17 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
                 V3 dx = sub(ph.pos, pre.pos);
                 if (P->problem == ORC_TEMP) { amount[0] = ph.sign * dtm; }
                 else if (P->problem == ORC_FLUX) { for (int q = 0; q < 3; ++q) amount[q] = ph.sign * dx[q]; }
-                else { amount[0] = ph.sign * dtm; for (int q = 0; q < 3; ++q) amount[q + 1] = ph.sign * dx[q]; }
+                else if (P->problem == ORC_MULTI) {
+                    amount[0] = ph.sign * dtm;
+                    for (int q = 0; q < 3; ++q) amount[q + 1] = ph.sign * dx[q];
+                } else {
+                    // the bin of the scatter count before the flight
+                    // (montecarlo/problem.cpp:589-596,626-633)
+                    std::fill(amountV.begin(), amountV.end(), 0.);
+                    const long bin = ((long)pre.nscat + cumStep - 1) / cumStep;
+                    if (P->problem == ORC_CUMTEMP) amount[bin] = ph.sign * dtm;
+                    else for (int q = 0; q < 3; ++q) amount[3 * bin + q] = ph.sign * dx[q];
+                }
                 accumulate(D, si, pre.pos, ph.pos, amount, L.F);
                 V3 endPos = ph.pos;
                 int siBefore = si;
@@ -966,6 +985,13 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
         st.horizon_stops += L.st.horizon_stops; st.maxscat_stops += L.st.maxscat_stops;
         st.absorbed += L.st.absorbed; st.replay_exhausted += L.st.replay_exhausted;
     }
+    // CumTemp / CumFlux postProc: cumulative sums over the bins
+    // (montecarlo/problem.cpp:598-606,636-645)
+    if (cum) {
+        const long per = P->problem == ORC_CUMTEMP ? 1 : 3;
+        for (long c = 0; c < cols; ++c)
+            for (long r = per; r < rows; ++r) sum[c * rows + r] += sum[c * rows + r - per];
+    }
     // montecarlo/problem.cpp:439-444
     for (int si = 0; si < (int)D.sd.size(); ++si) {
         const Sdom& s = D.sd[si];
@@ -975,7 +1001,8 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
         for (long c = s.colbeg; c < s.colbeg + sp; ++c)
             for (long r = 0; r < rows; ++r) {
                 double v = sum[c * rows + r];
-                if (P->problem == ORC_TEMP || (P->problem == ORC_MULTI && r == 0)) v = v / m.energySum;
+                if (P->problem == ORC_TEMP || P->problem == ORC_CUMTEMP || (P->problem == ORC_MULTI && r == 0))
+                    v = v / m.energySum;
                 out[c * rows + r] = power * (v / cv);
             }
     }

@@ -62,10 +62,10 @@ enum {
     ORC_RNG_REPLAY = 2      /* per-phonon recorded 32-bit words */
 };
 
-enum { ORC_TEMP = 0, ORC_FLUX = 1, ORC_MULTI = 2 };
+enum { ORC_TEMP = 0, ORC_FLUX = 1, ORC_MULTI = 2, ORC_CUMTEMP = 3, ORC_CUMFLUX = 4 };
 
 typedef struct {
-    int problem;            /* ORC_TEMP / ORC_FLUX / ORC_MULTI */
+    int problem;            /* ORC_TEMP / ORC_FLUX / ORC_MULTI / ORC_CUMTEMP / ORC_CUMFLUX */
     long nemit;
     long maxscat;
     long maxloop;           /* 0 -> 100 * maxscat (montecarlo/problem.cpp:339) */
@@ -90,6 +90,9 @@ typedef struct {
     int64_t* log_counts;
     long log_cap;
     long log_phonons;                /* only phonons id < log_phonons log */
+    /* CumTemp / CumFlux: number of scatter-count bins after the first
+       (montecarlo/problem.cpp:553-648); rows = size + 1 or 3 (size + 1) */
+    long cum_size;
 } orc_problem;
 
 typedef struct {

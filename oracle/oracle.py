@@ -17,7 +17,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmc_oracle.so")
 
-TEMP, FLUX, MULTI = 0, 1, 2
+TEMP, FLUX, MULTI, CUMTEMP, CUMFLUX = 0, 1, 2, 3, 4
 RNG_MT, RNG_PHILOX, RNG_REPLAY = 0, 1, 2
 LOG_FIELDS = ("loop", "sdom", "face", "sdom_after", "cell", "x", "y", "z",
               "time", "nscat", "w", "p")
@@ -43,7 +43,7 @@ class Problem(C.Structure):
                 ("record_words", C.POINTER(C.c_uint32)), ("record_counts", C.POINTER(C.c_int64)),
                 ("record_cap", C.c_long),
                 ("log", C.POINTER(C.c_double)), ("log_counts", C.POINTER(C.c_int64)),
-                ("log_cap", C.c_long), ("log_phonons", C.c_long)]
+                ("log_cap", C.c_long), ("log_phonons", C.c_long), ("cum_size", C.c_long)]
 
 
 class Stats(C.Structure):
@@ -193,11 +193,13 @@ class ODomain:
 
 def solve(mat, dom, problem=MULTI, nemit=1000, maxscat=1000, maxloop=0, dt=0.0,
           horizon=0.0, rng=RNG_PHILOX, seed=0, nchunk=1, nthreads=0,
-          replay=None, record_cap=0, log_cap=0, log_phonons=0):
-    """Run the oracle. Returns (out rows x cols, stats dict, extras)."""
+          replay=None, record_cap=0, log_cap=0, log_phonons=0, size=0):
+    """Run the oracle. Returns (out rows x cols, stats dict, extras).
+    `size` is the bin count of CUMTEMP / CUMFLUX."""
     L = lib()
     P = Problem()
     P.problem, P.nemit, P.maxscat, P.maxloop = problem, nemit, maxscat, maxloop
+    P.cum_size = size
     P.dt, P.horizon, P.rng, P.seed = dt, horizon, rng, seed
     P.nchunk, P.nthreads = nchunk, nthreads
     extras = {}
@@ -224,7 +226,7 @@ def solve(mat, dom, problem=MULTI, nemit=1000, maxscat=1000, maxloop=0, dt=0.0,
         P.log = _dp(lg)
         P.log_counts = lc.ctypes.data_as(C.POINTER(C.c_int64))
         P.log_cap, P.log_phonons = log_cap, nlp
-    rows = {TEMP: 1, FLUX: 3, MULTI: 4}[problem]
+    rows = {TEMP: 1, FLUX: 3, MULTI: 4, CUMTEMP: size + 1, CUMFLUX: 3 * (size + 1)}[problem]
     out = np.zeros(rows * dom.cols)
     st = Stats()
     rc_ = L.orc_solve(mat.h, dom.h, C.byref(P), _dp(out), C.byref(st))

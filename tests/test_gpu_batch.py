@@ -23,13 +23,15 @@ def instances():
         M.TempProblem(mats[380.0], M.CrossPlaneFilmDomain(1e-7, 1e-7, 20), 2000, 10**6),
         M.MultiProblem(mats[300.0], M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4)), 1500, 10**6),
         M.FluxProblem(mats[150.0], M.BulkDomain.from_cli(1e-6, 10), 500, 1000),
+        M.CumTempProblem(mats[380.0], M.FilmDomain.from_cli(1e-7, 1e-7, 30), 1500, 5, 41),
+        M.CumFluxProblem(mats[300.0], M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4)), 800, 2, 21),
     ]
 
 
 @pytest.mark.parametrize("K", [0, 40])
 def test_batch_equals_single_fp64(K):
     probs = instances()
-    seeds = [11, 12, 13, 14, 15]
+    seeds = [11, 12, 13, 14, 15, 16, 17]
     dt, nsteps = 0.5e-12, 400
     B = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=64, steps_per_launch=K, use_graph=False)
     B.run()

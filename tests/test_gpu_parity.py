@@ -309,3 +309,90 @@ def test_fp64_plain_kernel_against_oracle_without_log(name, gmat, omat):
     assert P.stats["events"] == ost["events"]
     assert P.stats["phonon_steps"] == ost["phonon_steps"]
     assert field_err(o, g) < 1e-9
+
+
+CUM = {M.CUMTEMP: M.CumTempProblem, M.CUMFLUX: M.CumFluxProblem}
+
+
+@pytest.mark.parametrize("kind", [M.CUMTEMP, M.CUMFLUX])
+@pytest.mark.parametrize("K,schedule", [(1, 1), (40, 2), (100000, 0)])
+def test_cum_problems_fp64_against_oracle(kind, K, schedule, gmat, omat):
+    """CumTemp / CumFlux (montecarlo/problem.cpp:553-648): the field binned
+    by the scatter count before each flight, cumulative over the bins. FP64
+    flight against the oracle in the static (lean flight), dynamic and
+    whole-horizon schedules: event counts exact, field within 1e-9."""
+    dom = domains()["film"]
+    nemit, dt, nsteps, size, maxscat = 2000, 0.5e-12, 400, 4, 21
+    o, ost, _ = O.solve(omat, O.ODomain(dom), kind, nemit=nemit, maxscat=maxscat, dt=dt, horizon=dt * nsteps,
+                        rng=O.RNG_PHILOX, seed=9, size=size)
+    P = CUM[kind](gmat, dom, nemit, size, maxscat)
+    g = P.solve(dt=dt, nsteps=nsteps, precision=64, steps_per_launch=K, schedule=schedule, seed=9)
+    assert g.shape == o.shape == (P.rows(), dom_cols(dom))
+    for k in ("events", "scatters", "maxscat_stops", "phonon_steps"):
+        assert P.stats[k] == ost[k], k
+    assert field_err(o, g) < 1e-9
+
+
+def dom_cols(dom):
+    return M.problem._handle(dom).cols
+
+
+def test_cum_flux_pore_cell_fp64_and_fp32(gmat, omat):
+    """CumFlux on the 3-D pore cell (FP64 global atomics at the flight's bin
+    rows) against the oracle, and the FP32 field's error."""
+    dom = M.PoreCellDomain(5e-7, 2.5e-7, (4, 8, 4))
+    nemit, dt, nsteps, size, maxscat = 1500, 0.5e-12, 300, 3, 31
+    o, ost, _ = O.solve(omat, O.ODomain(dom), M.CUMFLUX, nemit=nemit, maxscat=maxscat, dt=dt,
+                        horizon=dt * nsteps, rng=O.RNG_PHILOX, seed=4, size=size)
+    P = M.CumFluxProblem(gmat, dom, nemit, size, maxscat)
+    g = P.solve(dt=dt, nsteps=nsteps, precision=64, steps_per_launch=50, seed=4)
+    assert P.stats["events"] == ost["events"]
+    assert field_err(o, g) < 1e-9
+    g32 = P.solve(dt=dt, nsteps=nsteps, precision=32, steps_per_launch=50, seed=4)
+    assert field_err(o, g32) < 5e-3
+
+
+def test_cum_last_bin_is_the_plain_field(gmat):
+    """The last cumulative bin of CumTemp / CumFlux is the Temp / Flux field
+    of the same phonons (FP32 flight, same Philox streams; bins few enough
+    that every field stays in the blocks' shared fixed-point layout)."""
+    dom = domains()["film"]
+    kw = dict(dt=0.5e-12, nsteps=300, precision=32, steps_per_launch=300, seed=17)
+    t = M.TempProblem(gmat, dom, 20000, 25).solve(**kw)
+    f = M.FluxProblem(gmat, dom, 20000, 25).solve(**kw)
+    ct = M.CumTempProblem(gmat, dom, 20000, 6, 25).solve(**kw)
+    cf = M.CumFluxProblem(gmat, dom, 20000, 4, 25).solve(**kw)
+    assert field_err(t, ct[-1:]) < 1e-12
+    assert field_err(f, cf[-3:]) < 1e-12
+
+
+def test_cum_problem_arguments(gmat):
+    dom = domains()["film"]
+    with pytest.raises(ValueError):
+        M.CumTempProblem(gmat, dom, 100, 0, 10)
+    with pytest.raises(ValueError):
+        M.CumFluxProblem(gmat, dom, 100, 3, 1)
+
+
+def test_replica_statistics(gmat):
+    """mc_solve_replicas: nsim solves with seeds seed + i and their
+    Welford mean and sample standard deviation (montecarlo/field.cpp:226-262,
+    montecarlo/main.cpp:181-210), against numpy over the same solves run
+    one at a time."""
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 20)
+    P = M.MultiProblem(gmat, dom, 5000, 10**6)
+    kw = dict(dt=0.5e-12, nsteps=200, precision=64, steps_per_launch=200)
+    mean, sd = P.solve_replicas(5, seed=40, **kw)
+    st = dict(P.stats)
+    runs = []
+    ev = 0
+    for i in range(5):
+        runs.append(P.solve(seed=40 + i, **kw))
+        ev += P.stats["events"]
+    runs = np.array(runs)
+    assert st["events"] == ev
+    assert field_err(runs.mean(axis=0), mean) < 1e-12
+    ref_sd = runs.std(axis=0, ddof=1)
+    assert np.allclose(sd, ref_sd, rtol=1e-9, atol=1e-12 * np.abs(ref_sd).max())
+    one, sd1 = P.solve_replicas(1, seed=40, **kw)
+    assert field_err(runs[0], one) < 1e-12 and not sd1.any()

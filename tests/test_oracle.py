@@ -215,3 +215,27 @@ def test_golden_fixtures(name, omat):
     assert got["log_counts"] == ref["log_counts"]
     for ga, ra in zip(got["log"], ref["log"]):
         assert np.allclose(np.array(ga), np.array(ra), rtol=1e-13, atol=1e-22)
+
+
+def test_cum_problems_bin_the_scatter_count(omat):
+    """CumTemp / CumFlux (montecarlo/problem.cpp:553-648): with the same
+    phonons, the last cumulative bin is the Temp / Flux field, bin 0 holds
+    the flights before any scatter, and the bins grow by the flights of each
+    scatter-count range."""
+    import montecarlocpp_gb300 as M
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 20)
+    od = O.ODomain(dom)
+    kw = dict(nemit=3000, maxscat=21, dt=0.5e-12, horizon=0.5e-12 * 400, rng=O.RNG_PHILOX, seed=5)
+    t, _, _ = O.solve(omat, od, O.TEMP, **kw)
+    f, _, _ = O.solve(omat, od, O.FLUX, **kw)
+    ct, st, _ = O.solve(omat, od, O.CUMTEMP, size=4, **kw)      # bins of 5 scatters
+    cf, _, _ = O.solve(omat, od, O.CUMFLUX, size=4, **kw)
+    assert ct.shape == (5, 20) and cf.shape == (15, 20)
+    assert np.allclose(ct[-1], t[0], rtol=1e-12, atol=1e-12 * np.abs(t).max())
+    assert np.allclose(cf[-3:], f, rtol=1e-12, atol=1e-12 * np.abs(f).max())
+    # one bin after the first: every scattered flight in bin 1
+    c1, _, _ = O.solve(omat, od, O.CUMTEMP, size=1, **kw)
+    assert np.allclose(c1[0], ct[0], rtol=1e-12, atol=1e-12 * np.abs(t).max())
+    assert np.allclose(c1[1], t[0], rtol=1e-12, atol=1e-12 * np.abs(t).max())
+    # bins differ: scattering changes the contributions
+    assert np.abs(np.diff(ct, axis=0)).max() > 0
