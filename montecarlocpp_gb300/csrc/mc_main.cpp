@@ -7,6 +7,7 @@
 //           | custom T disp relax
 //           film dim0 dim1 div1 | bulk dim0 div0
 //           temp|flux|multi nemit maxscat maxloop nsim
+//           | cumtemp|cumflux nemit size maxscat maxloop nsim
 //           [dt nsteps precision seed]
 //
 // The trailing four arguments are the GPU run loop's time horizon
@@ -38,7 +39,8 @@ void printSolution(const std::vector<double>& sol, long rows, long cols) {
 int usage() {
     std::fprintf(stderr,
                  "usage: mc_main prefix silicon|grey T | custom T disp relax  film dim0 dim1 div1 | bulk dim0 div0"
-                 "  temp|flux|multi nemit maxscat maxloop nsim  [dt nsteps precision seed]\n");
+                 "  temp|flux|multi nemit maxscat maxloop nsim | cumtemp|cumflux nemit size maxscat maxloop nsim"
+                 "  [dt nsteps precision seed]\n");
     return 2;
 }
 
@@ -78,8 +80,10 @@ int main(int argc, char** argv) {
             std::fprintf(stderr, "Invalid domain (film and bulk are served by this driver)\n");
             return 1;
         }
-        long nemit = 0, maxscat = 0, maxloop = 0, nsim = 1;
-        ss >> probStr >> nemit >> maxscat >> maxloop >> nsim;
+        long nemit = 0, maxscat = 0, maxloop = 0, nsim = 1, size = 0;
+        ss >> probStr >> nemit;
+        if (probStr == "cumtemp" || probStr == "cumflux") ss >> size;  // montecarlo/main.cpp:446-456
+        ss >> maxscat >> maxloop >> nsim;
         if (!ss) { std::fprintf(stderr, "Invalid problem arguments\n"); return 1; }
         mcgb::RunOptions o;
         double dt;
@@ -91,6 +95,8 @@ int main(int argc, char** argv) {
         if (probStr == "temp") prob.reset(new mcgb::TempProblem(mat, *dom, nemit, maxscat, maxloop));
         else if (probStr == "flux") prob.reset(new mcgb::FluxProblem(mat, *dom, nemit, maxscat, maxloop));
         else if (probStr == "multi") prob.reset(new mcgb::MultiProblem(mat, *dom, nemit, maxscat, maxloop));
+        else if (probStr == "cumtemp") prob.reset(new mcgb::CumTempProblem(mat, *dom, nemit, size, maxscat, maxloop));
+        else if (probStr == "cumflux") prob.reset(new mcgb::CumFluxProblem(mat, *dom, nemit, size, maxscat, maxloop));
         else { std::fprintf(stderr, "Invalid problem\n"); return 1; }
         const long rows = prob->rows(), cols = dom->cols();
         std::vector<double> mean((size_t)(rows * cols), 0.), m2((size_t)(rows * cols), 0.);
@@ -102,7 +108,7 @@ int main(int argc, char** argv) {
             std::printf("Solution %ld (%ld phonons, %.6g phonon-steps, %.3f ms)\n", n, st.nemit, st.phonon_steps,
                         st.kernel_ms);
             printSolution(sol, rows, cols);
-            // Welford (montecarlo/field.cpp:323-330)
+            // Welford (montecarlo/field.cpp:255-262)
             for (size_t i = 0; i < sol.size(); ++i) {
                 double d = sol[i] - mean[i];
                 mean[i] += d / (double)(n + 1);

@@ -54,3 +54,25 @@ def test_driver_matches_python_binding(tmp_path, gmat):
     ref = P.solve(dt=5e-13, nsteps=100, precision=64, seed=3)
     assert field.shape == ref.shape
     assert np.allclose(field, ref, rtol=1e-8, atol=1e-8 * np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_driver_cumflux_with_replicas(tmp_path, gmat):
+    """`cumflux nemit size maxscat maxloop nsim` (montecarlo/main.cpp:
+    446-456): the printed mean and standard deviation of the replicas match
+    mc_solve_replicas for the same seeds."""
+    M.write_material_files(str(tmp_path))
+    B.build()
+    cmd = [B.MAIN, str(tmp_path), "silicon", "300", "film", "1e-7", "1e-7", "10", "cumflux", "400", "2", "11", "0",
+           "3", "5e-13", "80", "64", "5"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    text = r.stdout.split("Mean\n")[1]
+    mean_txt, sd_txt = text.split("Standard Deviation\n")
+    parse = lambda t: np.array([[float(x) for x in ln.split()] for ln in t.splitlines() if ln.strip()])
+    mean, sd = parse(mean_txt), parse(sd_txt)
+    P = M.CumFluxProblem(gmat, M.FilmDomain.from_cli(1e-7, 1e-7, 10), 400, 2, 11)
+    rm, rs = P.solve_replicas(3, dt=5e-13, nsteps=80, precision=64, seed=5)
+    assert mean.shape == rm.shape == (9, 10)
+    assert np.allclose(mean, rm, rtol=1e-8, atol=1e-8 * np.abs(rm).max())
+    assert np.allclose(sd, rs, rtol=1e-6, atol=1e-8 * np.abs(rs).max())
