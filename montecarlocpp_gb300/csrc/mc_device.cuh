@@ -215,6 +215,16 @@ template <> struct Rng<false> {
         k0 = key0; k1 = key1; id = pid; event = 0; block = 0; lane = 0;
     }
     __device__ __forceinline__ void setEvent(uint32_t e) { event = e; block = 0; lane = 0; }
+    // make the next block now if the current one is used up (next() then
+    // finds words ready): lets the lanes that will draw make it together
+    __device__ __forceinline__ void fill() {
+        if (lane == 0) {
+            const uint4 o = philoxBlock(id, event, block, k0, k1);
+            b0 = o.x; b1 = o.y; b2 = o.z; b3 = o.w;
+            ++block;
+            lane = 4;
+        }
+    }
     __device__ __forceinline__ uint32_t next() {
         if (lane == 0) {
             const uint4 o = philoxBlock(id, event, block, k0, k1);
@@ -247,6 +257,7 @@ template <> struct Rng<true> {
         ex = false;
     }
     __device__ __forceinline__ void setEvent(uint32_t) {}
+    __device__ __forceinline__ void fill() {}
     __device__ __forceinline__ uint32_t next() {
         if (pos < end) return w[pos++];
         ex = true;

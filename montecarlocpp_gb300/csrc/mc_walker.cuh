@@ -810,42 +810,70 @@ struct Walker {
         if constexpr (REPLAY) g = rg;
         else g.init(I.key0(), I.key1(), ph.id, &P);
         g.setEvent(ph.nloop + 1);
+        // the event: a relaxation scatter (kind -1) or the face's boundary
+        const FaceD<R>* F = face >= 0 ? &S->f[face] : nullptr;
+        const int kind = face >= 0 ? F->kind : -1;
         if (face >= 0) {
-            const FaceD<R>& F = S->f[face];
             // the flight ends on the face: snap that coordinate
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 if (face == k) { ph.idx[k] = 0; ph.off[k] = R(0); }
                 if (face == k + 3) { ph.idx[k] = S->shape[k] - 1; ph.off[k] = R(1); }
             }
-            switch (F.kind) {
-            case F_SPEC: {  // montecarlo/boundary.cpp:283-287
-                R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
-                for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F.n[j];
-                normalize(ph.d);
-                break;
-            }
-            case F_DIFF: {  // montecarlo/boundary.cpp:308-312
-                R vv[3];
-                drawAniso<R>(g, false, vv);
-                rotate(F.rot, vv, ph.d);
-                normalize(ph.d);
-                ph.nscat++;
-                break;
-            }
-            case F_ISOT:  // montecarlo/boundary.cpp:455-460
-                stop = C_ABSORBED;
-                break;
-            case F_PERI:     // montecarlo/boundary.cpp:516-522
-            case F_INTER: {  // montecarlo/boundary.cpp:349-359 (single pair)
-                if (F.to < 0) { stop = C_ESCAPES; break; }
-                if (F.tang) {
+        }
+        // A scatter and a diffuse wall both draw a new direction: their
+        // lanes make the first Philox block together and share one
+        // direction draw (same words in the same order as drawIso /
+        // drawAniso, so the same results), instead of each kind running
+        // its own copy in turn.
+        const bool draws = kind < 0 || kind == F_DIFF;
+        if (draws) g.fill();
+        if (kind < 0) {
+            // Material::scatter (montecarlo/material.cpp:298-303)
+            uint32_t x1 = g.next(), x2 = g.next();
+            ph.w = searchGuided(I.wthr(), I.wguide(), I.nw(), x1);
+            ph.p = searchBranch(I.pthr() + ph.w * I.np(), I.np(), x2);
+        }
+        if (draws) {
+            // isotropic after a scatter (montecarlo/random.cpp:16-27);
+            // cosine law about the inward normal at a diffuse wall
+            // (montecarlo/boundary.cpp:308-312, montecarlo/random.cpp:29-44),
+            // where it counts as a scatter
+            R c, sn;
+            const uint32_t wp = g.next();
+            if (kind < 0) isoPolar(wp, c, sn);
+            else anisoPolar(wp, false, c, sn);
+            R sp, cp;
+            sincospi_(uone<R>(g.next()), &sp, &cp);
+            const R vv[3] = {sn * cp, sn * sp, c};
+            if (kind < 0) { ph.d[0] = vv[0]; ph.d[1] = vv[1]; ph.d[2] = vv[2]; }
+            else rotate(F->rot, vv, ph.d);
+            normalize(ph.d);
+            ph.nscat++;
+        }
+        if (kind < 0) {
+            ph.scatNext = drawScatNext<R>(g, I.vt()[ph.w * I.np() + ph.p]);
+            v = I.vel()[ph.w * I.np() + ph.p];
+            iv = R(1) / v;
+            blkCount(C_SCATTERS, 1);
+        } else if (kind == F_SPEC) {  // montecarlo/boundary.cpp:283-287
+            R nd = (F->n[0] * ph.d[0] + F->n[1] * ph.d[1]) + F->n[2] * ph.d[2];
+            for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F->n[j];
+            normalize(ph.d);
+        } else if (kind == F_ISOT) {  // montecarlo/boundary.cpp:455-460
+            stop = C_ABSORBED;
+        } else if (kind == F_PERI || kind == F_INTER) {
+            // montecarlo/boundary.cpp:516-522 (Peri), 349-359 (Inter, single pair)
+            if (F->to < 0) {
+                stop = C_ESCAPES;
+            } else {
+                if (F->tang) {
                     // same axis, tangential cells unchanged: keep the split
                     // coordinates, move onto the paired face (selects on
                     // every axis: no indexed writes into the phonon state)
-                    ph.s = F.to;
+                    ph.s = F->to;
                     S = &I.sd()[ph.s];
-                    const int tf = F.toface;
+                    const int tf = F->toface;
                     const int tax = tf >= 3 ? tf - 3 : tf;
                     const bool up = tf >= 3;
 #pragma unroll
@@ -857,14 +885,14 @@ struct Walker {
                 } else {
                     R u[3], u2[3];
                     for (int j = 0; j < 3; ++j) u[j] = (R)ph.idx[j] + ph.off[j];
-                    rotate(F.A, u, u2);
-                    for (int j = 0; j < 3; ++j) u2[j] += F.b[j];
-                    ph.s = F.to;
+                    rotate(F->A, u, u2);
+                    for (int j = 0; j < 3; ++j) u2[j] += F->b[j];
+                    ph.s = F->to;
                     S = &I.sd()[ph.s];
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
-                        if (F.toface == j) u2[j] = R(0);
-                        if (F.toface == j + 3) u2[j] = S->S[j];
+                        if (F->toface == j) u2[j] = R(0);
+                        if (F->toface == j + 3) u2[j] = S->S[j];
                     }
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
@@ -874,26 +902,12 @@ struct Walker {
                         ph.off[j] = clamp01(u2[j] - (R)ii);
                     }
                 }
-                if (F.kind == F_PERI && !F.ident) {
+                if (kind == F_PERI && !F->ident) {
                     R dd[3] = {ph.d[0], ph.d[1], ph.d[2]};
-                    rotate(F.Rd, dd, ph.d);
+                    rotate(F->Rd, dd, ph.d);
                     normalize(ph.d);
                 }
-                break;
             }
-            }
-        } else {
-            // Material::scatter (montecarlo/material.cpp:298-303)
-            uint32_t x1 = g.next(), x2 = g.next();
-            ph.w = searchGuided(I.wthr(), I.wguide(), I.nw(), x1);
-            ph.p = searchBranch(I.pthr() + ph.w * I.np(), I.np(), x2);
-            drawIso<R>(g, ph.d);
-            normalize(ph.d);
-            ph.nscat++;
-            ph.scatNext = drawScatNext<R>(g, I.vt()[ph.w * I.np() + ph.p]);
-            v = I.vel()[ph.w * I.np() + ph.p];
-            iv = R(1) / v;
-            blkCount(C_SCATTERS, 1);
         }
         ++nev;
         if (LOG) logEvent(P, ph, sBefore, face, ph.s, xe, (double)P.step0 * (double)P.dt + (double)(W.len - budget),
