@@ -487,7 +487,7 @@ int checkProblem(const mc_problem_desc& p) {
     if (p.problem < MC_TEMP || p.problem > MC_CUMFLUX) return fail(MC_ERR_ARG, "Invalid problem");
     if (p.problem == MC_CUMTEMP || p.problem == MC_CUMFLUX) {
         if (p.cum_size < 1) return fail(MC_ERR_ARG, "cum_size must be >= 1");
-        if (p.maxscat < 2) return fail(MC_ERR_ARG, "CumTemp / CumFlux need maxscat >= 2");
+        if (p.maxscat < 2 || p.maxscat >= (1L << 31)) return fail(MC_ERR_ARG, "CumTemp / CumFlux need 2 <= maxscat < 2^31");
         if (p.cum_size > (1L << 20)) return fail(MC_ERR_ARG, "cum_size too large");
     }
     return MC_OK;
@@ -978,6 +978,7 @@ struct mc_batch_s {
     unsigned int* status = nullptr;
     long long cap = 0;
     int block = 256, grid = 0;
+    int tm = 2;                     // field mode of the advance launches (batchFieldMode)
     SegD* segs = nullptr;           // work segments of the advance launches
     int* home = nullptr;            // first segment of each block
     unsigned long long* segNext = nullptr;
@@ -1028,6 +1029,21 @@ void planSegments(const std::vector<long long>& slot0, const std::vector<long>& 
 // shared-memory capacities: fixed-point fields up to TAL_BATCH_MAX bytes,
 // subdomain images while the block stays within BATCH_SMEM_F32 (twice that
 // in FP64). `inst` must hold nw, np, nsd, rows and cols.
+// The field mode every instance of a batched launch shares (so the launch
+// runs the kernel without the others' code), or TM_AUTO.
+template <typename R>
+int batchFieldMode(const std::vector<InstD<R>>& inst) {
+    bool allShared = true, allGlobal = true, allNone = true;
+    for (const auto& I : inst) {
+        const bool none = (I.flags & IF_NO_FIELD) != 0 || I.tally == nullptr;
+        const bool sh = !none && (I.flags & IF_TAL_SHARED) != 0;
+        allNone = allNone && none;
+        allShared = allShared && sh;
+        allGlobal = allGlobal && !none && !sh;
+    }
+    return allNone ? TM_NONE : (allShared ? TM_SHARED : (allGlobal ? TM_GLOBAL : TM_AUTO));
+}
+
 template <typename R>
 int batchCaps(std::vector<InstD<R>>& inst, Params<R>& P) {
     int bNt = 0, bNw = 0, bTal = 0;
@@ -1182,7 +1198,8 @@ int setupBatch(mc_batch_s* B) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int occ = advanceBatchOccupancy<R>(batchSmemBytes<R>(P), B->block);
+    B->tm = batchFieldMode<R>(inst);
+    const int occ = advanceBatchOccupancy<R>(B->tm, batchSmemBytes<R>(P), B->block);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
     B->grid = B->bd.grid_blocks > 0 ? B->bd.grid_blocks : occ * nsm;
     std::vector<SegD> segs;
@@ -1217,7 +1234,7 @@ int enqueueBatch(mc_batch_s* B) {
         setWindow(P);
         CK(cudaMemsetAsync(B->cnt + C_NCOUNTERS + 1, 0, sizeof(unsigned long long), B->stream));
         CK(cudaMemsetAsync(B->segNext, 0, sizeof(unsigned long long) * std::max(B->nseg, 1), B->stream));
-        CK(launchAdvanceBatch<R>(P, B->grid, B->block, B->stream));
+        CK(launchAdvanceBatch<R>(P, B->tm, B->grid, B->block, B->stream));
         ++launches;
     }
     CK(launchDifPrefix<R>(P, B->stream));
@@ -1511,7 +1528,8 @@ struct ServerT : ServerBase {
                 if (I.tally == nullptr) I.flags |= IF_NO_FIELD;
             }
         }
-        const int occ = advanceBatchOccupancy<R>(batchSmemBytes<R>(P), block);
+        const int tm = batchFieldMode<R>(inst);
+        const int occ = advanceBatchOccupancy<R>(tm, batchSmemBytes<R>(P), block);
         if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
         const int grid = std::min(occ, 64) * nsm;
         std::vector<SegD> segs;
@@ -1538,7 +1556,7 @@ struct ServerT : ServerBase {
         P.step0 = 0;
         setWindow(P);
         CK(launchEmitBatch<R>(P, stream));
-        CK(launchAdvanceBatch<R>(P, grid, block, stream));
+        CK(launchAdvanceBatch<R>(P, tm, grid, block, stream));
         CK(launchDifPrefix<R>(P, stream));
         CK(launchRoundReduce<R>(P, accs_d, gsum_d, stream));
         std::vector<double> gsum((size_t)n * MAX_GROUPS * 4);

@@ -600,7 +600,11 @@ __device__ __forceinline__ void flushBinding(const InstD<R>& I, int group) {
 // its field and moves on to the next segment with work, so that a few
 // expensive instances end up spread over the whole GPU. A block starts on
 // segment home[block] (the host spreads blocks over segments by size).
-template <typename R>
+// TM: the field mode of every instance of the launch when they share one
+// (TM_SHARED: all stage a shared field; TM_GLOBAL: all add to their global
+// field; TM_NONE: none keeps a field), else TM_AUTO (per instance): a launch
+// whose instances agree runs without the code of the other modes.
+template <typename R, int TM>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_batch(Params<R> P) {
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ int sSeg;
@@ -634,7 +638,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
             curInst = S.inst;
         }
         __syncthreads();
-        dynamicLoop<R, false, false, TM_AUTO>(P, P.segNext + sg, (unsigned long long)S.beg,
+        dynamicLoop<R, false, false, TM>(P, P.segNext + sg, (unsigned long long)S.beg,
                                               (unsigned long long)S.end, BatchView<R>{&P, smraw, I}, W);
         __syncthreads();
         flushBinding<R>(*I, S.group);

@@ -28,12 +28,14 @@ int advanceLeanOccupancy(int lean, int block, size_t smem);
 // batched launches (all instances in one kernel)
 template <typename R>
 cudaError_t launchEmitBatch(const Params<R>& p, cudaStream_t s);
+// tm: the launch's common field mode (TM_SHARED / TM_GLOBAL / TM_NONE) or
+// TM_AUTO (batchFieldMode)
 template <typename R>
-cudaError_t launchAdvanceBatch(const Params<R>& p, int grid, int block, cudaStream_t s);
+cudaError_t launchAdvanceBatch(const Params<R>& p, int tm, int grid, int block, cudaStream_t s);
 template <typename R>
 cudaError_t launchDifPrefix(const Params<R>& p, cudaStream_t s);
 template <typename R>
-int advanceBatchOccupancy(size_t smem, int block);
+int advanceBatchOccupancy(int tm, size_t smem, int block);
 template <typename R>
 cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
                               cudaStream_t s);

@@ -82,12 +82,21 @@ cudaError_t launchEmitBatch<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <typename R>
+static auto batchKernel(int tm) {
+    return tm == TM_SHARED ? k_advance_batch<R, TM_SHARED>
+         : tm == TM_GLOBAL ? k_advance_batch<R, TM_GLOBAL>
+         : tm == TM_NONE   ? k_advance_batch<R, TM_NONE>
+                           : k_advance_batch<R, TM_AUTO>;
+}
+
 template <>
-cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int grid, int block, cudaStream_t s) {
+cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int tm, int grid, int block, cudaStream_t s) {
     const size_t smem = batchSmemBytes<MC_REAL>(p);
-    cudaError_t e = prepare(k_advance_batch<MC_REAL>, smem);
+    auto fn = batchKernel<MC_REAL>(tm);
+    cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
-    k_advance_batch<MC_REAL><<<grid, block, smem, s>>>(p);
+    fn<<<grid, block, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -105,11 +114,11 @@ cudaError_t launchRoundReduce<MC_REAL>(const Params<MC_REAL>& p, double* const* 
 }
 
 template <>
-int advanceBatchOccupancy<MC_REAL>(size_t smem, int block) {
-    if (prepare(k_advance_batch<MC_REAL>, smem) != cudaSuccess) return 0;
+int advanceBatchOccupancy<MC_REAL>(int tm, size_t smem, int block) {
+    auto fn = batchKernel<MC_REAL>(tm);
+    if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_advance_batch<MC_REAL>, block, smem) != cudaSuccess)
-        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess) return 0;
     return nb;
 }
 

@@ -85,7 +85,9 @@ __host__ __device__ inline size_t smemTallyBytes(int rows, int cols) {
 // order-independent adds) flushed with FP64 atomics, or FP64 atomics
 // straight to the global field (fields too large for shared memory), or
 // either per instance (batched launches: shared when InstD::tal is set).
-enum { TM_SHARED = 0, TM_GLOBAL = 1, TM_AUTO = 2 };
+enum { TM_SHARED = 0, TM_GLOBAL = 1, TM_AUTO = 2, TM_NONE = 3 };
+// (TM_NONE: batched launches whose instances keep no field, only the
+// per-flight checksums -- the flight code without any field path.)
 
 // Hard cap on events one thread processes in one launch (a guard: a
 // phonon that reaches it is killed and flagged non-finite).
@@ -395,7 +397,8 @@ __device__ __forceinline__ void setFlightRows(Tally<R, TM, IA>& T, int problem, 
     else if (problem == P_FLUX) { T.nAct = 3; T.rho[0] = sg * d[0]; T.rho[1] = sg * d[1]; T.rho[2] = sg * d[2]; T.rho[3] = R(0); }
     else if (problem == P_MULTI) { T.nAct = 4; T.rho[0] = sg * iv; T.rho[1] = sg * d[0]; T.rho[2] = sg * d[1]; T.rho[3] = sg * d[2]; }
     else {
-        const int bin = (int)(((unsigned long long)nscat + (unsigned long long)cumStep - 1ull) / (unsigned long long)cumStep);
+        // nscat < maxscat < 2^31 and cumStep < 2^31 (checked on the host)
+        const int bin = (int)((nscat + (uint32_t)cumStep - 1u) / (uint32_t)cumStep);
         if (problem == P_CUMTEMP) {
             T.nAct = 1; T.rowBase = bin;
             T.rho[0] = sg * iv; T.rho[1] = T.rho[2] = T.rho[3] = R(0);
@@ -502,7 +505,7 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
 template <typename R, int TM, typename IA>
 __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
                                    Tally<R, TM, IA>& T) {
-    const int acc = (TM == TM_AUTO && (T.V.flags() & IF_NO_FIELD)) ? -2 : S.accum;
+    const int acc = (TM == TM_NONE || (TM == TM_AUTO && (T.V.flags() & IF_NO_FIELD))) ? -2 : S.accum;
     const int cb = S.colbeg;
     if (acc < 0) {
         // a single field column (or none): move only
