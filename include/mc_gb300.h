@@ -179,6 +179,15 @@ int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* o
 int mc_solve_replicas(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, long nsim, double* mean, double* sd,
                       mc_stats* st);
 
+/* No counterpart in the reference: a device self-check of the bounded
+ * waits every asynchronous kernel here relies on. One block waits on an
+ * mbarrier phase that nothing completes, with a deadline of limit_ms
+ * (0 < limit_ms <= 1000); the wait must give up on its own. *status receives
+ * the device status bits (8 = a wait gave up, which the solves report as
+ * MC_ERR_TIMEOUT) and *waited_ms how long the wait took. The device stays
+ * usable afterwards. */
+int mc_check_bounded_wait(double limit_ms, unsigned* status, double* waited_ms);
+
 /* Size of the fixed device scratch array behind mc_solve_noalloc: 32 MiB,
  * held on every device that loads this library until the process exits. */
 #define MC_NOALLOC_SCRATCH_BYTES (32u << 20)

@@ -96,7 +96,7 @@ SYMBOLS = [
     "mc_material_create", "mc_material_load", "mc_material_sums", "mc_material_tables",
     "mc_material_destroy",
     "mc_domain_create", "mc_domain_cols", "mc_domain_cell_volumes", "mc_domain_destroy",
-    "mc_solve", "mc_solve_noalloc", "mc_solve_replicas",
+    "mc_solve", "mc_solve_noalloc", "mc_solve_replicas", "mc_check_bounded_wait",
     "mc_session_create", "mc_session_emit", "mc_session_advance", "mc_session_result",
     "mc_session_state_bytes", "mc_session_destroy",
     "mc_batch_create", "mc_batch_run", "mc_batch_result", "mc_batch_stats", "mc_batch_state_bytes",
@@ -140,6 +140,7 @@ def lib(build_if_missing: bool = True):
     L.mc_domain_destroy.argtypes = [C.c_void_p]
     L.mc_solve.argtypes = [C.c_void_p, C.c_void_p, P(ProblemDesc), P(C.c_double), P(Stats)]
     L.mc_solve_noalloc.argtypes = [C.c_void_p, C.c_void_p, P(ProblemDesc), P(C.c_double), P(Stats)]
+    L.mc_check_bounded_wait.argtypes = [C.c_double, P(C.c_uint), P(C.c_double)]
     L.mc_solve_replicas.argtypes = [C.c_void_p, C.c_void_p, P(ProblemDesc), C.c_long, P(C.c_double),
                                     P(C.c_double), P(Stats)]
     L.mc_session_create.argtypes = [C.c_void_p, C.c_void_p, P(ProblemDesc), P(C.c_void_p)]

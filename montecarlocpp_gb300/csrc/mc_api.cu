@@ -2032,6 +2032,31 @@ int mc_solve(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, double* o
     return rc;
 }
 
+// Bounded-wait self-check: a wait that nothing completes must give up with
+// S_TIMEOUT after about limit_ms, and the device must stay usable.
+int mc_check_bounded_wait(double limit_ms, unsigned* status, double* waited_ms) {
+    if (!(limit_ms > 0.) || limit_ms > 1000.) return fail(MC_ERR_ARG, "limit_ms must be in (0, 1000]");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    unsigned* st_d = nullptr;
+    unsigned long long* w_d = nullptr;
+    CK(cudaMalloc(&st_d, sizeof(unsigned)));
+    CK(cudaMalloc(&w_d, sizeof(unsigned long long)));
+    CK(cudaMemset(st_d, 0, sizeof(unsigned)));
+    cudaError_t e = launchWaitCheck(st_d, (unsigned long long)(limit_ms * 1e6), w_d, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    unsigned st = 0;
+    unsigned long long w = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&st, st_d, sizeof(st), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&w, w_d, sizeof(w), cudaMemcpyDeviceToHost);
+    cudaFree(st_d);
+    cudaFree(w_d);
+    if (e != cudaSuccess) return fail(MC_ERR_CUDA, std::string("bounded-wait check: ") + cudaGetErrorString(e));
+    if (status) *status = st;
+    if (waited_ms) *waited_ms = (double)w * 1e-6;
+    return MC_OK;
+}
+
 // Replicas (montecarlo/main.cpp:181-210): nsim solves of one session whose
 // Philox key is seed + i for replica i, folded into Statistics' Welford
 // mean and sum of squared deviations (montecarlo/field.cpp:226-262).

@@ -40,6 +40,10 @@ template <typename R>
 cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
                               cudaStream_t s);
 
+// the bounded-wait self-check (mc_check_bounded_wait)
+cudaError_t launchWaitCheck(unsigned* status, unsigned long long limitNs, unsigned long long* waitedNs,
+                            cudaStream_t s);
+
 // Maximum resident blocks per SM of the advance kernel for this
 // configuration (0 if it cannot launch).
 template <typename R>

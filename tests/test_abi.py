@@ -104,3 +104,11 @@ def test_no_cpu_fallback(gmat):
     with pytest.raises(_lib.McError) as e:
         p.solve(dt=1e-12, nsteps=10)
     assert e.value.code == -3
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a CUDA device is present")
+def test_bounded_wait_check_needs_a_device():
+    import ctypes as C
+    st, w = C.c_uint(0), C.c_double(0.0)
+    assert _lib.lib().mc_check_bounded_wait(10.0, C.byref(st), C.byref(w)) == -3
+    assert _lib.lib().mc_check_bounded_wait(0.0, C.byref(st), C.byref(w)) == -1
