@@ -237,6 +237,19 @@ int mc_session_advance(mc_session_h s, int nlaunch, int* done);
 int mc_session_result(mc_session_h s, double* out, mc_stats* st);
 /* Bytes the phonon state of this session occupies on the device. */
 size_t mc_session_state_bytes(mc_session_h s);
+/* Snapshot and resume (no counterpart in the reference, whose solves run
+ * to completion in one call): mc_session_snapshot synchronises and copies
+ * everything a session needs to continue -- the live phonon state, live
+ * counts, counters, status, raw field, checksums and replay cursors -- into
+ * a host buffer of mc_session_snapshot_bytes(s) bytes; mc_session_restore
+ * loads such a buffer into a session created with the same material,
+ * domain and problem description (checked), which then continues with
+ * mc_session_advance exactly as the original would have: every phonon's
+ * random numbers depend only on its id and event index. Sessions that log
+ * trajectories are refused (MC_ERR_UNSUPPORTED). */
+size_t mc_session_snapshot_bytes(mc_session_h s);
+int mc_session_snapshot(mc_session_h s, void* buf, size_t bytes);
+int mc_session_restore(mc_session_h s, const void* buf, size_t bytes);
 void mc_session_destroy(mc_session_h s);
 
 /* ------------------------------------------------------------ batches */

@@ -98,7 +98,8 @@ SYMBOLS = [
     "mc_domain_create", "mc_domain_cols", "mc_domain_cell_volumes", "mc_domain_destroy",
     "mc_solve", "mc_solve_noalloc", "mc_solve_replicas", "mc_check_bounded_wait",
     "mc_session_create", "mc_session_emit", "mc_session_advance", "mc_session_result",
-    "mc_session_state_bytes", "mc_session_destroy",
+    "mc_session_state_bytes", "mc_session_destroy", "mc_session_snapshot_bytes", "mc_session_snapshot",
+    "mc_session_restore",
     "mc_batch_create", "mc_batch_run", "mc_batch_result", "mc_batch_stats", "mc_batch_state_bytes",
     "mc_batch_destroy",
     "mc_server_create", "mc_server_submit", "mc_server_poll", "mc_server_wait", "mc_server_stats",
@@ -147,6 +148,10 @@ def lib(build_if_missing: bool = True):
     L.mc_session_emit.argtypes = [C.c_void_p]
     L.mc_session_advance.argtypes = [C.c_void_p, C.c_int, P(C.c_int)]
     L.mc_session_result.argtypes = [C.c_void_p, P(C.c_double), P(Stats)]
+    L.mc_session_snapshot_bytes.restype = C.c_size_t
+    L.mc_session_snapshot_bytes.argtypes = [C.c_void_p]
+    L.mc_session_snapshot.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    L.mc_session_restore.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     L.mc_session_state_bytes.restype = C.c_size_t
     L.mc_session_state_bytes.argtypes = [C.c_void_p]
     L.mc_session_destroy.argtypes = [C.c_void_p]

@@ -571,6 +571,7 @@ struct mc_session_s {
     double* log_d = nullptr;
     int* logcnt_d = nullptr;
     int lean = -1;                // static schedule: axis of the lean flight, or -1
+    long long slots = 0;          // phonon slots per half of the state
     unsigned* reg_d = nullptr;    // static schedule: front / back live counts
                                   // per block region, one array per half
     int parity = 0;               // which half holds the live phonons
@@ -754,6 +755,7 @@ int setupSession(mc_session_s* S) {
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
     S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
+    S->slots = (long long)n;
     CK(cudaMalloc(&S->state, 2 * half));
     char* sb = (char*)S->state;
     V4* h0[2]; V4* h1[2]; uint4* h2[2];
@@ -2004,6 +2006,112 @@ int mc_session_result(mc_session_h s, double* out, mc_stats* st) {
 }
 
 size_t mc_session_state_bytes(mc_session_h s) { return s ? s->stateBytes : 0; }
+
+// ---------------------------------------------------------------- snapshot
+// A session's resumable state, in one host buffer: a header that must match
+// the restoring session, then the live half of the phonon state, the live
+// counts (block regions of both halves in the static schedule; the slot
+// count in the dynamic one sits among the counters), counters, status,
+// raw field, checksums and, in replay mode, the per-phonon stream cursors.
+// Philox streams are keyed by phonon id and event index, so a restored
+// session continues every trajectory exactly.
+namespace {
+struct SnapHeader {
+    uint32_t magic, version;
+    int32_t prec, dyn, grid, block, rows, replay;
+    int64_t nemit, slots, cols;
+    int32_t step, parity, launches, sinceCompact;
+};
+constexpr uint32_t SNAP_MAGIC = 0x5353434Du;  // "MCSS"
+
+struct SnapPart { void* dev; size_t bytes; };
+
+std::vector<SnapPart> snapParts(mc_session_s* S) {
+    std::vector<SnapPart> v;
+    const size_t v4 = S->prec == 32 ? sizeof(float4) : sizeof(dbl4);
+    const int half = S->parity;
+    void *a, *b, *c;
+    if (S->prec == 32) {
+        const Params<float>& P = S->p32;
+        a = half ? (void*)P.P0out : (void*)P.P0in; b = half ? (void*)P.P1out : (void*)P.P1in;
+        c = half ? (void*)P.P2out : (void*)P.P2in;
+    } else {
+        const Params<double>& P = S->p64;
+        a = half ? (void*)P.P0out : (void*)P.P0in; b = half ? (void*)P.P1out : (void*)P.P1in;
+        c = half ? (void*)P.P2out : (void*)P.P2in;
+    }
+    const size_t n = (size_t)S->slots;
+    v.push_back({a, v4 * n});
+    v.push_back({b, v4 * n});
+    v.push_back({c, sizeof(uint4) * n});
+    v.push_back({S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 4)});
+    v.push_back({S->status_d, sizeof(unsigned int)});
+    v.push_back({S->tally_d, sizeof(double) * (size_t)S->rows * (size_t)std::max(S->dom->cols, 1L)});
+    v.push_back({S->csum_d, sizeof(double) * 4});
+    if (S->reg_d) v.push_back({S->reg_d, sizeof(unsigned) * 4 * (size_t)S->grid});
+    if (S->replay) v.push_back({S->rcur_d, sizeof(uint32_t) * (size_t)S->nemit});
+    return v;
+}
+
+SnapHeader snapHeader(const mc_session_s* S) {
+    SnapHeader h;
+    std::memset(&h, 0, sizeof(h));
+    h.magic = SNAP_MAGIC; h.version = 1;
+    h.prec = S->prec; h.dyn = S->dyn ? 1 : 0; h.grid = S->grid; h.block = S->block; h.rows = S->rows;
+    h.replay = S->replay ? 1 : 0;
+    h.nemit = S->nemit; h.slots = S->slots; h.cols = S->dom->cols;
+    h.step = S->step; h.parity = S->parity; h.launches = S->launches; h.sinceCompact = S->sinceCompact;
+    return h;
+}
+}  // namespace
+
+size_t mc_session_snapshot_bytes(mc_session_h s) {
+    if (!s) return 0;
+    size_t n = sizeof(SnapHeader);
+    for (const SnapPart& p : snapParts(s)) n += (p.bytes + 7) & ~(size_t)7;
+    return n;
+}
+
+int mc_session_snapshot(mc_session_h s, void* buf, size_t bytes) {
+    if (!s || !buf) return fail(MC_ERR_ARG, "null argument");
+    if (s->logging) return fail(MC_ERR_UNSUPPORTED, "sessions that log trajectories cannot be snapshotted");
+    if (bytes < mc_session_snapshot_bytes(s)) return fail(MC_ERR_ARG, "snapshot buffer too small");
+    CK(cudaStreamSynchronize(s->stream));
+    char* p = (char*)buf;
+    const SnapHeader h = snapHeader(s);
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    for (const SnapPart& q : snapParts(s)) {
+        CK(cudaMemcpy(p, q.dev, q.bytes, cudaMemcpyDeviceToHost));
+        p += (q.bytes + 7) & ~(size_t)7;
+    }
+    return MC_OK;
+}
+
+int mc_session_restore(mc_session_h s, const void* buf, size_t bytes) {
+    if (!s || !buf) return fail(MC_ERR_ARG, "null argument");
+    if (s->logging) return fail(MC_ERR_UNSUPPORTED, "sessions that log trajectories cannot be restored");
+    if (bytes < sizeof(SnapHeader)) return fail(MC_ERR_ARG, "snapshot buffer too small");
+    SnapHeader h;
+    std::memcpy(&h, buf, sizeof(h));
+    const SnapHeader mine = snapHeader(s);
+    if (h.magic != SNAP_MAGIC || h.version != 1) return fail(MC_ERR_ARG, "not a session snapshot");
+    if (h.prec != mine.prec || h.dyn != mine.dyn || h.grid != mine.grid || h.block != mine.block ||
+        h.rows != mine.rows || h.replay != mine.replay || h.nemit != mine.nemit || h.slots != mine.slots ||
+        h.cols != mine.cols)
+        return fail(MC_ERR_ARG, "snapshot of a different problem or launch configuration");
+    if (h.step < 0 || h.step > (int)s->desc.nsteps || (h.parity != 0 && h.parity != 1))
+        return fail(MC_ERR_ARG, "corrupt snapshot header");
+    CK(cudaStreamSynchronize(s->stream));
+    s->step = h.step; s->parity = h.parity; s->launches = h.launches; s->sinceCompact = h.sinceCompact;
+    if (bytes < mc_session_snapshot_bytes(s)) return fail(MC_ERR_ARG, "snapshot buffer too small");
+    const char* p = (const char*)buf + sizeof(h);
+    for (const SnapPart& q : snapParts(s)) {
+        CK(cudaMemcpy(q.dev, p, q.bytes, cudaMemcpyHostToDevice));
+        p += (q.bytes + 7) & ~(size_t)7;
+    }
+    return MC_OK;
+}
 
 void mc_session_destroy(mc_session_h s) { freeSession(s); }
 

@@ -295,6 +295,21 @@ class Session:
     def state_bytes(self):
         return _lib.lib().mc_session_state_bytes(self.h)
 
+    def snapshot(self) -> bytearray:
+        """Everything the session needs to continue, as host bytes."""
+        n = _lib.lib().mc_session_snapshot_bytes(self.h)
+        buf = bytearray(n)
+        cbuf = (C.c_char * n).from_buffer(buf)
+        _lib.check(_lib.lib().mc_session_snapshot(self.h, cbuf, n))
+        return buf
+
+    def restore(self, buf):
+        """Load a snapshot of a session of the same problem; advance()
+        then continues it exactly."""
+        b = bytearray(buf)
+        cbuf = (C.c_char * len(b)).from_buffer(b)
+        _lib.check(_lib.lib().mc_session_restore(self.h, cbuf, len(b)))
+
     def close(self):
         if getattr(self, "h", None) and _lib._lib is not None:
             _lib._lib.mc_session_destroy(self.h)
