@@ -404,7 +404,7 @@ k_advance(Params<R> P) {
                 }
             }
             if (have && lean == LEAN_EVENT) {
-                Walker<R, REPLAY, LOG, TM, ParamView<R, TM>> wk;
+                Walker<R, REPLAY, LOG, TM, ParamView<R, TM>, true> wk;
                 wk.load(P, V, W, A0, A1, A2);
                 while (!wk.iterate(P, W)) {}
                 alive = wk.finishInto(P, W, nSteps, nEvents);

@@ -434,26 +434,36 @@ __device__ __forceinline__ void moveAxis(Phn<R>& ph, const SdomD<R>& S, int k, R
     ph.idx[k] = i;
 }
 
+// Component k of a 3-vector by selects (no indexed access, so the vector
+// stays in registers whatever k is).
+template <typename T>
+__device__ __forceinline__ T pick3(const T v[3], int k) {
+    return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]);
+}
+
 // 1-D flight along axis K (the only axis with cells): closed form of
 // montecarlo/field.cpp:187-223 -- partial first and last cells, full
 // interior cells through the difference array. In the shared layout the
 // flight's whole fixed-point amount V is computed once and the last cell
-// takes the integer remainder, so the cells add up to V exactly.
-template <typename R, int TM, int K, typename IA>
+// takes the integer remainder, so the cells add up to V exactly. Called
+// with a constant K the selects fold away (one copy per axis); with a
+// run-time K one copy serves every axis.
+template <typename R, int TM, typename IA>
 __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                      Tally<R, TM, IA>& T) {
+                                      Tally<R, TM, IA>& T, const int K) {
     const int cb = S.colbeg;
-    const int b = ph.idx[K];
+    const int b = pick3(ph.idx, K);
     const int n = S.shape[K];
+    const R offK = pick3(ph.off, K);
     // displacement in cell units relative to the current cell
-    const R du = ph.off[K] + s * a[K];
+    const R du = offK + s * pick3(a, K);
     int e = b + (int)floor(du);
     e = min(max(e, 0), n - 1);
     const int stride = S.tstride[K];
-    const R inva = fabs(ia[K]);
+    const R inva = fabs(pick3(ia, K));
     const int lo = min(b, e), hi = max(b, e);
     const int nin = hi - lo - 1;  // interior cells; -1 when the flight stays in its cell
-    const R tfirst = (e > b ? (R(1) - ph.off[K]) : ph.off[K]) * inva;
+    const R tfirst = (e > b ? (R(1) - offK) : offK) * inva;
     using Fix = typename FixT<R>::T;
     if (T.shared()) {
         // the first cell's add is common to every lane (all of V when the
@@ -492,17 +502,20 @@ __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3
             else for (int c = lo + 1; c < hi; ++c) T.addGlobal(cb + c * stride, inva);
         }
     }
-    ph.idx[K] = e;
-    ph.off[K] = clamp01(du - (R)(e - b));
+    const R offNew = clamp01(du - (R)(e - b));
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
-        if (j != K) moveAxis(ph, S, j, ph.off[j] + s * a[j]);
+    for (int j = 0; j < 3; ++j) {
+        if (j == K) { ph.idx[j] = e; ph.off[j] = offNew; }
+        else moveAxis(ph, S, j, ph.off[j] + s * a[j]);
+    }
 }
 
 // Flight of path length s from the current cell, tallied cell by cell
 // (Field::accumulate, montecarlo/field.cpp:160-288, as a cell walk); adds
 // the flight's fixed-point amount to the checksums.
-template <typename R, int TM, typename IA>
+// COMPACT: one run-time-axis copy of the 1-D flight instead of one per
+// axis (smaller code for kernels that run the walker rarely).
+template <typename R, int TM, typename IA, bool COMPACT>
 __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
                                    Tally<R, TM, IA>& T) {
     const int acc = (TM == TM_NONE || (TM == TM_AUTO && (T.V.flags() & IF_NO_FIELD))) ? -2 : S.accum;
@@ -522,9 +535,13 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         for (int k = 0; k < 3; ++k) moveAxis(ph, S, k, ph.off[k] + s * a[k]);
         return;
     }
-    if (acc == 0) { fly1d<R, TM, 0, IA>(ph, S, a, ia, s, T); return; }
-    if (acc == 1) { fly1d<R, TM, 1, IA>(ph, S, a, ia, s, T); return; }
-    if (acc == 2) { fly1d<R, TM, 2, IA>(ph, S, a, ia, s, T); return; }
+    if (COMPACT) {
+        if (acc <= 2) { fly1d<R, TM, IA>(ph, S, a, ia, s, T, acc); return; }
+    } else {
+        if (acc == 0) { fly1d<R, TM, IA>(ph, S, a, ia, s, T, 0); return; }
+        if (acc == 1) { fly1d<R, TM, IA>(ph, S, a, ia, s, T, 1); return; }
+        if (acc == 2) { fly1d<R, TM, IA>(ph, S, a, ia, s, T, 2); return; }
+    }
     // 2-D / 3-D: walk the cells (Amanatides-Woo); a shared field gives the
     // checksum as the sum of its cells, a global one the flight's amount
     if (!T.shared()) {
@@ -715,7 +732,7 @@ constexpr uint32_t PROP_DEAD = 1u << 25;
 // from it. iterate() runs one loop iteration of montecarlo/problem.cpp:401-435
 // (flight to the next event or to the end of the window, its tally, the
 // event); finish() closes the phonon's window.
-template <typename R, bool REPLAY, bool LOG, int TM, typename IA>
+template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool COMPACT = false>
 struct Walker {
     Phn<R> ph;
     IA I;
@@ -787,7 +804,7 @@ struct Walker {
         setFlightRows(T, I.problem(), ph.neg, iv, ph.d, ph.nscat, I.cumStep());
         const int sBefore = ph.s;
         int cellEnd = 0;
-        fly<R, TM, IA>(ph, *S, a, ia, s, T);
+        fly<R, TM, IA, COMPACT>(ph, *S, a, ia, s, T);
         if (LOG) cellEnd = ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2];
         ph.scatNext -= s;
         if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
@@ -1025,7 +1042,7 @@ __device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typen
     T.V = I;
     T.goff = 0;
     setFlightRows(T, I.problem(), ph.neg, iv, ph.d, ph.nscat, I.cumStep());
-    fly1d<R, TM_SHARED, K, IA>(ph, S, a, ia, s, T);
+    fly1d<R, TM_SHARED, IA>(ph, S, a, ia, s, T, K);
     ph.scatNext -= s;
     if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
     tnext = (sev - s) * iv;
