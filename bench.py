@@ -433,8 +433,10 @@ def bench_batched(stream, reps=2, plain=True):
         probs.append(M.MultiProblem(mats[T], M.FilmDomain.from_cli(1e-7, sp.thickness, sp.cells), sp.nemit,
                                     1_000_000))
     seeds = list(range(len(probs)))
+    from montecarlocpp_gb300 import autotune
+    cfg, trials = autotune.tune_batch(probs, dt=dt, nsteps=nsteps)
     B = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=32, use_graph=True,
-                stream=stream.cuda_stream)
+                stream=stream.cuda_stream, **cfg)
     B.run()
     torch.cuda.synchronize()
     times = []
@@ -449,7 +451,9 @@ def bench_batched(stream, reps=2, plain=True):
                        "dt 0.5 ps x 4000 steps",
            "phonons": int(st["nemit"]), "phonon_steps": st["phonon_steps"],
            "batched_s": tb, "batched_solves_per_s": len(probs) / tb,
-           "batched_phonon_steps_per_s": st["phonon_steps"] / tb, "launches_per_run": st["launches"]}
+           "batched_phonon_steps_per_s": st["phonon_steps"] / tb, "launches_per_run": st["launches"],
+           "autotuned": cfg,
+           "autotune_trials": [dict(c, phonon_steps_per_s=r) for c, r in trials]}
     B.close()
     def kappas64(sd):
         B64 = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=sd, precision=64, use_graph=False)

@@ -1,9 +1,13 @@
-"""Project autotuner for the advance kernel's launch parameters.
+"""Project autotuner for the advance kernels' launch parameters.
 
-Searches dt-steps per launch (the compaction / sort interval), block size and
-tally layout on a reduced copy of the workload (fewer phonons, a shortened
-horizon), timing device-resident solves with CUDA events, and returns the
-fastest. Results are cached per workload signature for the process.
+tune(): dt-steps per launch (the compaction / sort interval), block size and
+tally layout of a single solve, on a reduced copy of the workload (fewer
+phonons), timing device-resident solves with CUDA events.
+tune_batch(): block size and dt-steps per launch of a batched solve, on a
+copy of the batch with a fraction of each instance's phonons, timing the
+replayed CUDA graph.
+Both return the fastest configuration; results are cached per workload
+signature for the process.
 """
 
 from __future__ import annotations
@@ -63,3 +67,48 @@ def tune(prob, W, stream, Ks=(50, 200, 1000, 4000), blocks=(128, 256), tallies=(
 def best_steps_per_launch(prob, W, stream):
     best, _ = tune(prob, W, stream, blocks=(256,))
     return best["steps_per_launch"]
+
+
+def tune_batch(problems, *, dt, nsteps, precision=32, blocks=(128, 256), Ks=(0, 1000), scale=0.1,
+               min_nemit=1000, reps=2):
+    """Return (best {"block_size", "steps_per_launch"}, list of (config,
+    phonon-steps/s)) for a batch of the given problems (steps_per_launch 0:
+    the whole horizon in one launch)."""
+    import torch
+
+    from .batch import Batch
+    from .problem import CUMFLUX, CUMTEMP, FLUX, MULTI, TEMP, CumFluxProblem, CumTempProblem, FluxProblem, \
+        MultiProblem, TempProblem
+    key = ("batch", tuple((type(p.dom).__name__, p.nemit_requested, p.kind) for p in problems), dt, nsteps,
+           precision)
+    if key in _cache:
+        return _cache[key]
+    cls = {TEMP: TempProblem, FLUX: FluxProblem, MULTI: MultiProblem}
+    small = []
+    for p in problems:
+        n = max(min_nemit, int(p.nemit_requested * scale))
+        if p.kind in (CUMTEMP, CUMFLUX):
+            c = CumTempProblem if p.kind == CUMTEMP else CumFluxProblem
+            small.append(c(p.mat, p.dom, n, p.size, p.maxscat, p.maxloop))
+        else:
+            small.append(cls[p.kind](p.mat, p.dom, n, p.maxscat, p.maxloop))
+    results = []
+    for b, K in itertools.product(blocks, Ks):
+        if K > nsteps:
+            continue
+        B = Batch(small, dt=dt, nsteps=nsteps, precision=precision, steps_per_launch=K, block_size=b,
+                  use_graph=True)
+        B.run()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            B.run()
+            st = B.stats()  # synchronises
+            rate = st["phonon_steps"] / (time.perf_counter() - t0)
+            best = rate if best is None else max(best, rate)
+        B.close()
+        results.append(({"block_size": b, "steps_per_launch": K}, best))
+    cfg = max(results, key=lambda x: x[1])[0]
+    _cache[key] = (cfg, results)
+    return cfg, results

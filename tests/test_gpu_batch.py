@@ -71,3 +71,18 @@ def test_batched_films_workload_shape():
     th = np.array([s.thickness for s in specs])
     assert n.min() >= 10_000 and n.max() <= 1_000_000
     assert (np.diff(n[np.argsort(th)]) >= 0).all()
+
+
+def test_batch_autotuner_picks_a_tried_configuration():
+    """The batch autotuner times block sizes and dt-steps per launch on a
+    scaled-down copy of the batch and returns the fastest it tried; the
+    chosen configuration runs the full batch."""
+    from montecarlocpp_gb300 import autotune
+    probs = instances()[:3]
+    cfg, trials = autotune.tune_batch(probs, dt=0.5e-12, nsteps=200, blocks=(128, 256), Ks=(0, 50), scale=0.5)
+    assert len(trials) == 4 and all(r > 0 for _, r in trials)
+    assert cfg == max(trials, key=lambda t: t[1])[0]
+    B = M.Batch(probs, dt=0.5e-12, nsteps=200, precision=32, **cfg)
+    B.run()
+    assert B.stats()["phonon_steps"] > 0
+    B.close()
