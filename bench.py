@@ -121,6 +121,26 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+def profile_figure(name, pattern):
+    """A figure from a committed ncu summary under profiles/ (the regex's
+    first group), or None."""
+    import re
+    p = os.path.join(HERE, "profiles", name)
+    if os.path.exists(p):
+        m = re.search(pattern, open(p).read())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def warp_efficiency(name):
+    """Warp-execution efficiency of a kernel from its ncu summary: threads
+    active per warp instruction / 32."""
+    x = profile_figure(name, r"threads active per warp instruction \| ([0-9.]+) of 32")
+    return {"threads_active_per_warp_instruction": x, "efficiency": x / 32.0,
+            "source": f"profiles/{name} (ncu smsp__thread_inst_executed_per_inst_executed)"} if x else None
+
+
 def traffic_per_phonon():
     """DRAM bytes per live phonon per fused advance launch, from the
     committed ncu summary of k_advance_dyn (the line
@@ -296,6 +316,7 @@ def main():
             "launches_per_solve": nl, "phonon_steps_per_launch": steps_launch,
             "algorithmic_bytes_per_launch": bytes_launch,
             "state_bytes_per_launch": 96.0 * live, "traffic_source": tsrc,
+            "warp_execution": warp_efficiency("k_advance_dyn_film.md"),
             "note": ("algorithmic bytes are 96 B per phonon-step (state read + written once per dt-step); "
                      "this kernel keeps each phonon in registers for all K = %d dt-steps of a launch and "
                      "touches its 48 B state once each way per launch (state_bytes_per_launch), so frac > 1 "
@@ -352,16 +373,22 @@ def main():
 
 
 def field_errors(f32, f64, f64b, dom, flux_row0=1):
-    """kappa and the flux profile (every flux row, per cell) of an FP32
-    solve against the FP64 solve of the same phonons; the statistical scale
-    is the seed-to-seed difference of two FP64 solves over sqrt(2)."""
+    """kappa, the flux profile (every flux row, per cell) and the
+    temperature profile (row 0) of an FP32 solve against the FP64 solve of
+    the same phonons; the statistical scale is the seed-to-seed difference of
+    two FP64 solves over sqrt(2)."""
     import montecarlocpp_gb300 as M
     k32 = M.kappa_from_flux(f32, dom, 0, flux_row0=flux_row0)
     k64 = M.kappa_from_flux(f64, dom, 0, flux_row0=flux_row0)
     k64b = M.kappa_from_flux(f64b, dom, 0, flux_row0=flux_row0)
     q32, q64, q64b = (f[flux_row0:flux_row0 + 3] for f in (f32, f64, f64b))
     scale = np.abs(q64).max()
-    return {"kappa_fp32": k32, "kappa_fp64": k64, "kappa_rel_err": abs(k32 - k64) / abs(k64),
+    t32, t64, t64b = (f[0] for f in (f32, f64, f64b))
+    tscale = np.abs(t64).max()
+    temp = {"temperature_profile_max_err_of_max": float(np.abs(t32 - t64).max() / tscale),
+            "temperature_profile_rms_err_of_max": float(np.sqrt(np.mean((t32 - t64) ** 2)) / tscale),
+            "temperature_profile_stat_rms_of_max": float(np.sqrt(np.mean((t64b - t64) ** 2)) / tscale / math.sqrt(2.0))}
+    return {**temp, "kappa_fp32": k32, "kappa_fp64": k64, "kappa_rel_err": abs(k32 - k64) / abs(k64),
             "kappa_stat_rel": abs(k64b - k64) / abs(k64) / math.sqrt(2.0),
             "flux_profile_max_err_of_max": float(np.abs(q32 - q64).max() / scale),
             "flux_profile_rms_err_of_max": float(np.sqrt(np.mean((q32 - q64) ** 2)) / scale),
@@ -452,7 +479,7 @@ def bench_batched(stream, reps=2, plain=True):
            "phonons": int(st["nemit"]), "phonon_steps": st["phonon_steps"],
            "batched_s": tb, "batched_solves_per_s": len(probs) / tb,
            "batched_phonon_steps_per_s": st["phonon_steps"] / tb, "launches_per_run": st["launches"],
-           "autotuned": cfg,
+           "autotuned": cfg, "warp_execution": warp_efficiency("k_advance_batch_64films.md"),
            "autotune_trials": [dict(c, phonon_steps_per_s=r) for c, r in trials]}
     B.close()
     def kappas64(sd):
@@ -646,7 +673,8 @@ def plain_kernel(prob, W, stream, peak, peak_kind, nsteps=64):
     s.close()
     return {"steps_per_launch": 1, "launch_ms": ms, "phonon_steps_per_s": n / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": 96.0 * n}}
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": 96.0 * n,
+                         "warp_execution": warp_efficiency("k_advance_static_film.md")}}
 
 
 if __name__ == "__main__":

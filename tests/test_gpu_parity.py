@@ -221,22 +221,34 @@ def test_checksum_fp64(gmat):
 
 def test_kappa_statistical_parity(gmat, omat):
     """FP32 GPU (Philox) against the FP64 oracle run with the reference's
-    mt19937 scheme: kappa of the 100 nm film within 3 standard errors."""
+    mt19937 scheme on the 100 nm film, 8 independent replicas each:
+    * kappa within 3 standard errors;
+    * the per-cell temperature profile (row 0) and x-flux profile (row 1):
+      every cell's difference of means within 5 standard errors of that cell
+      (Welch, 14 degrees of freedom), and the mean squared z over the 40
+      cells below 2.5 (its expectation is about 1.2 for equal means)."""
     dom = M.FilmDomain.from_cli(1e-7, 1e-7, 20)
     od = O.ODomain(dom)
-    dt, nsteps = 0.5e-12, 1000
-    ko, kg = [], []
-    for s in range(6):
-        o, _, _ = O.solve(omat, od, O.MULTI, nemit=20000, maxscat=10**6, dt=dt, horizon=dt * nsteps,
+    dt, nsteps, n, R = 0.5e-12, 1000, 15000, 8
+    ko, kg, fo, fg = [], [], [], []
+    for s in range(R):
+        o, _, _ = O.solve(omat, od, O.MULTI, nemit=n, maxscat=10**6, dt=dt, horizon=dt * nsteps,
                           rng=O.RNG_MT, nchunk=8, seed=100 * s)
         ko.append(M.kappa_from_flux(o, dom, 0, flux_row0=1))
-    P = M.MultiProblem(gmat, dom, 20000, 10**6)
-    for s in range(6):
+        fo.append(np.asarray(o)[:2])
+    P = M.MultiProblem(gmat, dom, n, 10**6)
+    for s in range(R):
         g = P.solve(dt=dt, nsteps=nsteps, precision=32, steps_per_launch=100, seed=1000 + s)
         kg.append(M.kappa_from_flux(g, dom, 0, flux_row0=1))
+        fg.append(np.asarray(g)[:2])
     ko, kg = np.array(ko), np.array(kg)
-    se = np.sqrt(ko.var(ddof=1) / len(ko) + kg.var(ddof=1) / len(kg))
+    se = np.sqrt(ko.var(ddof=1) / R + kg.var(ddof=1) / R)
     assert abs(ko.mean() - kg.mean()) < 3 * se
+    fo, fg = np.array(fo), np.array(fg)                      # replicas x 2 rows x cells
+    se = np.sqrt(fo.var(axis=0, ddof=1) / R + fg.var(axis=0, ddof=1) / R)
+    z = (fo.mean(axis=0) - fg.mean(axis=0)) / se
+    assert np.abs(z).max() < 5, np.abs(z).max(axis=1)
+    assert (z ** 2).mean() < 2.5, (z ** 2).mean(axis=1)
 
 
 def test_edge_cases(gmat, omat):
