@@ -92,6 +92,44 @@ typedef struct {
  * per subdomain, one pair per Inter face. */
 int mc_domain_create(const mc_pped_desc* ppeds, int n, const mc_pair_desc* pairs, int npairs,
                      mc_domain_h* out);
+
+/* Subdomain shapes (montecarlo/subdomain.h:128-640). */
+enum {
+    MC_PARALLELEPIPED = 0,   /* 3 columns; faces Bac Lef Bot Fro Rig Top            */
+    MC_TRIANGULAR_PRISM = 1, /* 3 columns; faces Bac Lef Bot Dia Top               */
+    MC_TETRAHEDRON = 2,      /* 3 columns; faces Bac Lef Bot Dia                   */
+    MC_PRISM = 3,            /* N columns: axis, then the N - 1 base vertices;
+                                faces Bot Top Sid0 .. Sid(N-1)                     */
+    MC_PYRAMID = 4           /* N columns: apex, then the N - 1 base vertices;
+                                faces Bot Sid0 .. Sid(N-1)                         */
+};
+#define MC_MAX_SDOM_COLS 9
+#define MC_MAX_SDOM_FACES 11
+
+/* A subdomain of any shape: the constructor arguments (o, mat, div, gradT,
+ * T) of Parallelepiped, TriangularPrism, Tetrahedron, Prism<N> and
+ * Pyramid<N> (montecarlo/subdomain.h:145-158,224-236,303-314,386-410,
+ * 524-547) and each face's kind, in bdry<I>() order. mat is column-major:
+ * column c at mat[3c .. 3c + 2]. Prism and Pyramid take one division
+ * count, div[0]: < 0 no field, else one column for the whole subdomain.
+ * The GPU kernels take subdomains of at most 6 faces (Prism<N <= 4>,
+ * Pyramid<N <= 5>), Peri faces off the parallelepiped frame only with the
+ * identity rotation; MC_ERR_UNSUPPORTED otherwise. */
+typedef struct {
+    int shape;
+    int ncols;
+    double o[3];
+    double mat[3 * MC_MAX_SDOM_COLS];
+    long div[3];
+    double gradT[3];
+    int kind[MC_MAX_SDOM_FACES];
+    double T[MC_MAX_SDOM_FACES];
+} mc_sdom_desc;
+
+/* mc_domain_create for subdomains of any shape; pairs name faces by their
+ * bdry<I>() index in each subdomain. */
+int mc_domain_create_shapes(const mc_sdom_desc* sdoms, int n, const mc_pair_desc* pairs, int npairs,
+                            mc_domain_h* out);
 /* Number of field columns (montecarlo/field.cpp:93-113). */
 long mc_domain_cols(mc_domain_h d);
 /* Cell volumes, one per column (CellVolF, montecarlo/problem.cpp:302-306). */

@@ -24,6 +24,15 @@ class PpedDesc(C.Structure):
                 ("gradT", C.c_double * 3), ("kind", C.c_int * 6), ("T", C.c_double * 6)]
 
 
+MAX_SDOM_COLS, MAX_SDOM_FACES = 9, 11
+
+
+class SdomDesc(C.Structure):
+    _fields_ = [("shape", C.c_int), ("ncols", C.c_int), ("o", C.c_double * 3),
+                ("mat", C.c_double * (3 * MAX_SDOM_COLS)), ("div", C.c_long * 3), ("gradT", C.c_double * 3),
+                ("kind", C.c_int * MAX_SDOM_FACES), ("T", C.c_double * MAX_SDOM_FACES)]
+
+
 class PairDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("sdom1", C.c_int), ("face1", C.c_int), ("sdom2", C.c_int),
                 ("face2", C.c_int), ("transl", C.c_double * 3), ("rot", C.c_double * 9)]
@@ -95,7 +104,7 @@ SYMBOLS = [
     "mc_last_error", "mc_version",
     "mc_material_create", "mc_material_load", "mc_material_sums", "mc_material_tables",
     "mc_material_destroy",
-    "mc_domain_create", "mc_domain_cols", "mc_domain_cell_volumes", "mc_domain_destroy",
+    "mc_domain_create", "mc_domain_create_shapes", "mc_domain_cols", "mc_domain_cell_volumes", "mc_domain_destroy",
     "mc_solve", "mc_solve_noalloc", "mc_solve_replicas", "mc_check_bounded_wait",
     "mc_session_create", "mc_session_emit", "mc_session_advance", "mc_session_result",
     "mc_session_state_bytes", "mc_session_destroy", "mc_session_snapshot_bytes", "mc_session_snapshot",
@@ -135,6 +144,7 @@ def lib(build_if_missing: bool = True):
     L.mc_material_tables.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
     L.mc_material_destroy.argtypes = [C.c_void_p]
     L.mc_domain_create.argtypes = [P(PpedDesc), C.c_int, P(PairDesc), C.c_int, P(C.c_void_p)]
+    L.mc_domain_create_shapes.argtypes = [P(SdomDesc), C.c_int, P(PairDesc), C.c_int, P(C.c_void_p)]
     L.mc_domain_cols.restype = C.c_long
     L.mc_domain_cols.argtypes = [C.c_void_p]
     L.mc_domain_cell_volumes.argtypes = [C.c_void_p, P(C.c_double)]

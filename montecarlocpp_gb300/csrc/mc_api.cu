@@ -251,7 +251,10 @@ bool readAll(const char* path, std::vector<double>& v) {
 
 struct HostFace {
     int kind;
-    V3 n, o;
+    int shape = 0;            // 0 Parallelogram, 1 Triangle, 2 Polygon
+    V3 n, o, si, sj;          // inward normal, origin, shape vectors
+    std::vector<V3> verts;    // Polygon: vertices relative to o
+    std::vector<double> tri;  // Polygon: triangle areas
     double area, T;
     int pairS = -1, pairF = -1;
     M3 R = eye();
@@ -259,11 +262,215 @@ struct HostFace {
     int ninter = 0;
 };
 
+V3 addv(const V3& a, const V3& b) { return mk(a[0] + b[0], a[1] + b[1], a[2] + b[2]); }
+V3 subv(const V3& a, const V3& b) { return mk(a[0] - b[0], a[1] - b[1], a[2] - b[2]); }
+V3 sclv(double s, const V3& a) { return mk(s * a[0], s * a[1], s * a[2]); }
+
+// Boundary(o, shape) with the shape's normal and area: Parallelogram
+// (montecarlo/boundary.cpp:121-152), Triangle (154-186), Polygon<N>
+// (188-258; triangles (v_n, v_n+1) for n < N - 2).
+HostFace makeFace(int kind, double T, const V3& o, int shape, const V3& si, const V3& sj,
+                  const std::vector<V3>& verts = std::vector<V3>()) {
+    HostFace F;
+    F.kind = kind; F.T = T; F.o = o; F.shape = shape; F.si = si; F.sj = sj;
+    if (shape == 2) {
+        F.verts = verts;
+        double a = 0.;
+        for (size_t k = 0; k + 1 < verts.size(); ++k) {
+            V3 cr = cross(verts[k], verts[k + 1]);
+            F.tri.push_back(std::sqrt(dot(cr, cr)) / 2.);
+            a += F.tri.back();
+        }
+        F.area = a;
+        F.n = unit(cross(verts[0], verts[1]));
+    } else {
+        V3 cr = cross(si, sj);
+        F.n = unit(cr);
+        F.area = std::sqrt(dot(cr, cr)) / (shape == 1 ? 2. : 1.);
+    }
+    return F;
+}
+
+// A subdomain on the host: the reference's Subdomain matrix (for the
+// escape tolerance and the cell coordinates), the shape's volume and
+// faces, and the device frame (a box holding the shape) with its walk grid.
+struct HostSdom {
+    int shape = MC_PARALLELEPIPED;
+    V3 o;
+    M3 M;                 // Subdomain::matrix (matBase for Prism / Pyramid)
+    long div[3];          // Subdomain divisions
+    double vol = 0.;
+    std::vector<HostFace> f;
+    std::vector<V3> col;  // the constructor's matrix columns
+    std::vector<double> subvol;  // Prism / Pyramid: volume(mat)
+    V3 fo;                // frame origin and matrix
+    M3 FM;
+};
+
+// Faces of each shape in bdry<I>() order and its volume: Parallelepiped
+// (montecarlo/subdomain.h:145-158), TriangularPrism (224-236),
+// Tetrahedron (303-314), Prism<N> (386-410, InitSidesF 458-475, PrismImpl
+// montecarlo/subdomain.cpp:376-397) and Pyramid<N> (subdomain.h:524-547,
+// InitSidesF 595-613, PyramidImpl subdomain.cpp:409-431).
+int buildShape(const mc_sdom_desc& p, HostSdom& H) {
+    const int N = p.ncols;
+    H.shape = p.shape;
+    H.o = mk(p.o[0], p.o[1], p.o[2]);
+    H.col.resize(N);
+    for (int i = 0; i < N; ++i) H.col[i] = mk(p.mat[3 * i], p.mat[3 * i + 1], p.mat[3 * i + 2]);
+    const std::vector<V3>& c = H.col;
+    const V3& o = H.o;
+    auto K = [&](int i) { return p.kind[i]; };
+    auto T = [&](int i) { return p.T[i]; };
+    if (p.shape == MC_PARALLELEPIPED || p.shape == MC_TRIANGULAR_PRISM || p.shape == MC_TETRAHEDRON) {
+        if (N != 3) return fail(MC_ERR_ARG, "this shape takes a 3-column matrix");
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) H.M.m[3 * r + q] = c[q][r];
+        for (int k = 0; k < 3; ++k) H.div[k] = p.div[k];
+        const double d = det3(H.M);
+        if (p.shape == MC_PARALLELEPIPED) {
+            H.vol = d;
+            V3 fo[6] = {o, o, o, addv(o, c[0]), addv(o, c[1]), addv(o, c[2])};
+            V3 fi[6] = {c[1], c[2], c[0], c[2], c[0], c[1]};
+            V3 fj[6] = {c[2], c[0], c[1], c[1], c[2], c[0]};
+            for (int k = 0; k < 6; ++k) H.f.push_back(makeFace(K(k), T(k), fo[k], 0, fi[k], fj[k]));
+        } else if (p.shape == MC_TRIANGULAR_PRISM) {
+            H.vol = d / 2.;
+            H.f.push_back(makeFace(K(0), T(0), o, 0, c[1], c[2]));
+            H.f.push_back(makeFace(K(1), T(1), o, 0, c[2], c[0]));
+            H.f.push_back(makeFace(K(2), T(2), o, 1, c[0], c[1]));
+            H.f.push_back(makeFace(K(3), T(3), addv(o, c[0]), 0, c[2], subv(c[1], c[0])));
+            H.f.push_back(makeFace(K(4), T(4), addv(o, c[2]), 1, c[1], c[0]));
+        } else {
+            H.vol = d / 6.;
+            H.f.push_back(makeFace(K(0), T(0), o, 1, c[1], c[2]));
+            H.f.push_back(makeFace(K(1), T(1), o, 1, c[2], c[0]));
+            H.f.push_back(makeFace(K(2), T(2), o, 1, c[0], c[1]));
+            H.f.push_back(makeFace(K(3), T(3), addv(o, c[0]), 1, subv(c[2], c[0]), subv(c[1], c[0])));
+        }
+    } else if (p.shape == MC_PRISM || p.shape == MC_PYRAMID) {
+        if (N < 4 || N > MC_MAX_SDOM_COLS) return fail(MC_ERR_ARG, "Prism / Pyramid take 4 to 9 columns");
+        const bool prism = p.shape == MC_PRISM;
+        for (int r = 0; r < 3; ++r) { H.M.m[3 * r] = c[1][r]; H.M.m[3 * r + 1] = c[N - 1][r]; H.M.m[3 * r + 2] = c[0][r]; }
+        const long d1 = p.div[0] < 0 ? -1 : 0;
+        H.div[0] = H.div[1] = H.div[2] = d1;
+        // volume(mat): col(i) x col(i+1) . col(0) for i < N - 2 (as the
+        // reference computes it), / 2 (Prism) or / 6 (Pyramid)
+        double vs = 0.;
+        for (int i = 0; i < N - 2; ++i) {
+            H.subvol.push_back(dot(cross(c[i], c[i + 1]), c[0]) / (prism ? 2. : 6.));
+            vs += H.subvol.back();
+        }
+        H.vol = vs;
+        std::vector<V3> bot(c.begin() + 1, c.end());
+        H.f.push_back(makeFace(K(0), T(0), o, 2, mk(0, 0, 0), mk(0, 0, 0), bot));
+        int base = 1;
+        if (prism) {
+            std::vector<V3> top(bot.rbegin(), bot.rend());
+            H.f.push_back(makeFace(K(1), T(1), addv(o, c[0]), 2, mk(0, 0, 0), mk(0, 0, 0), top));
+            base = 2;
+        }
+        for (int ind = 0; ind < N; ++ind) {
+            V3 pp = ind != 0 ? c[ind] : mk(0, 0, 0);
+            V3 i = prism ? c[0] : (ind != 0 ? subv(c[0], c[ind]) : c[0]);
+            V3 j = sclv(-1., pp);
+            if (ind != N - 1) j = addv(j, c[ind + 1]);
+            H.f.push_back(makeFace(K(base + ind), T(base + ind), addv(o, pp), prism ? 0 : 1, i, j));
+        }
+    } else {
+        return fail(MC_ERR_ARG, "invalid subdomain shape");
+    }
+    if (!(H.vol >= DMIN)) return fail(MC_ERR_ARG, "Volume too small, check vector order");
+    for (const HostFace& F : H.f) {
+        if (F.kind < MC_SPEC || F.kind > MC_INTER) return fail(MC_ERR_ARG, "invalid face kind");
+        if ((F.kind == MC_SPEC || F.kind == MC_DIFF || F.kind == MC_INTER) && F.T != 0.)
+            return fail(MC_ERR_ARG, "Cannot specify temperature");
+    }
+    // device frame: the shape's own unit cell, except for Prism / Pyramid
+    // (a one-cell field): the box around the vertices in the matBase basis
+    H.fo = o;
+    H.FM = H.M;
+    if (p.shape == MC_PRISM || p.shape == MC_PYRAMID) {
+        M3 Mi = inv3(H.M);
+        double lo[3] = {0., 0., 0.}, hi[3] = {0., 0., 0.};
+        std::vector<V3> pts;
+        pts.push_back(mk(0, 0, 0));
+        for (int i = 1; i < N; ++i) pts.push_back(c[i]);
+        const size_t nb = pts.size();
+        if (p.shape == MC_PRISM)
+            for (size_t i = 0; i < nb; ++i) pts.push_back(addv(pts[i], c[0]));
+        else
+            pts.push_back(c[0]);
+        for (const V3& q : pts) {
+            V3 l = mvec(Mi, q);
+            for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], l[k]); hi[k] = std::max(hi[k], l[k]); }
+        }
+        H.fo = addv(o, mvec(H.M, mk(lo[0], lo[1], lo[2])));
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) H.FM.m[3 * r + q] = H.M.m[3 * r + q] * (hi[q] - lo[q]);
+    }
+    return MC_OK;
+}
+
+// Subdomain::cellVol (ParallelepipedImpl montecarlo/subdomain.cpp:269-273,
+// TriangularPrismImpl 283-307, TetrahedronImpl 321-346, PrismImpl and
+// PyramidImpl 394-397,428-431), as the reference computes them.
+double cellVolume(const HostSdom& H, const long sh[3], const long idx[3]) {
+    const double sp = (double)(sh[0] * sh[1] * sh[2]);
+    if (H.shape == MC_PARALLELEPIPED) return H.vol / sp;
+    if (H.shape == MC_PRISM || H.shape == MC_PYRAMID) return H.vol;
+    const int dim = H.shape == MC_TRIANGULAR_PRISM ? 2 : 3;
+    double f0 = 1.;
+    for (int k = 0; k < dim; ++k) f0 -= (double)idx[k] / (double)sh[k];
+    if (f0 <= 0.) return 0.;
+    double f1 = f0;
+    for (int k = 0; k < dim; ++k) f1 -= 1. / (double)sh[k];
+    if (f1 >= 0.) return H.vol / sp;
+    if (dim == 2) {
+        double frac = std::pow(f0, 2);
+        for (int i = 0; i < 2; ++i) {
+            double f = f0 - 1. / (double)sh[i];
+            if (f > 0.) frac += -1. * std::pow(f, 2);
+        }
+        return H.vol * frac / (2. * (double)sh[2]);
+    }
+    static const int pts[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 1, 1}, {1, 0, 1}, {1, 1, 0}};
+    double frac = std::pow(f0, 3);
+    for (int i = 0; i < 6; ++i) {
+        const int sum = pts[i][0] + pts[i][1] + pts[i][2];
+        double f = f0;
+        for (int k = 0; k < 3; ++k) f -= (double)pts[i][k] / (double)sh[k];
+        if (f > 0.) frac += ((sum % 2) ? -1. : 1.) * std::pow(f, 3);
+    }
+    return H.vol * frac / 6.;
+}
+
+// Emission pieces of a non-Parallelepiped emitter in the subdomain's frame
+// coordinates u = diag(S) FM^-1 (x - fo): u = U0 + L c for the folded
+// uniforms c of Emitter::drawPos (TriangularPrismImpl / TetrahedronImpl
+// montecarlo/subdomain.cpp:309-373, Prism / Pyramid volDist 399-441,
+// Triangle / Polygon<N> montecarlo/boundary.cpp:180-186,246-256).
+void setPiece(EmitterD& E, int k, const HostSdom& H, const double S[3], const V3& origin, const V3& e0,
+              const V3& e1, const V3& e2) {
+    M3 Fi = inv3(H.FM);
+    V3 u0 = mvec(Fi, subv(origin, H.fo));
+    V3 ev[3] = {mvec(Fi, e0), mvec(Fi, e1), mvec(Fi, e2)};
+    for (int r = 0; r < 3; ++r) {
+        E.U0[k][r] = S[r] * u0[r];
+        for (int q = 0; q < 3; ++q) E.L[k][3 * r + q] = S[r] * ev[q][r];
+    }
+}
+void setThresholds(EmitterD& E, const std::vector<double>& w) {
+    double acc = 0.;
+    for (double x : w) acc += x;
+    double pre = 0.;
+    for (size_t i = 0; i < w.size(); ++i) { pre += w[i]; E.thr[i] = thrOf(pre / acc); }
+}
+
 }  // namespace
 
 struct mc_domain_s {
-    std::vector<mc_pped_desc> pp;
-    std::vector<HostFace> faces;          // 6 per subdomain
+    std::vector<mc_sdom_desc> desc;
     std::vector<EmitterD> em;
     std::vector<double> emWeight;
     std::vector<long> colbeg;
@@ -274,53 +481,37 @@ struct mc_domain_s {
 
 namespace {
 
-int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_s** out) {
+int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_s** out) {
     if (!ps || n <= 0) return fail(MC_ERR_ARG, "Domain setup not complete");
     if (n > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 32 subdomains");
-    mc_domain_s* D = new mc_domain_s;
-    D->pp.assign(ps, ps + n);
-    D->faces.resize(6 * n);
+    std::unique_ptr<mc_domain_s> D(new mc_domain_s);
+    D->desc.assign(ps, ps + n);
     D->sd.resize(n);
+    std::vector<HostSdom> H(n);
     std::vector<std::vector<int>> faceEmit(n);
     for (int s = 0; s < n; ++s) {
-        const mc_pped_desc& p = ps[s];
-        M3 M; std::memcpy(M.m, p.M, sizeof(M.m));
-        double vol = det3(M);
-        if (!(vol >= DMIN)) { delete D; return fail(MC_ERR_ARG, "Volume too small, check vector order"); }
-        V3 c0 = colOf(M, 0), c1 = colOf(M, 1), c2 = colOf(M, 2);
-        V3 o = mk(p.o[0], p.o[1], p.o[2]);
-        // faces (montecarlo/subdomain.h:149-154)
-        V3 fo[6] = {o, o, o, mk(o[0] + c0[0], o[1] + c0[1], o[2] + c0[2]),
-                    mk(o[0] + c1[0], o[1] + c1[1], o[2] + c1[2]), mk(o[0] + c2[0], o[1] + c2[1], o[2] + c2[2])};
-        V3 fi[6] = {c1, c2, c0, c2, c0, c1};
-        V3 fj[6] = {c2, c0, c1, c1, c2, c0};
-        for (int f = 0; f < 6; ++f) {
-            HostFace& F = D->faces[6 * s + f];
-            F.kind = p.kind[f];
-            if (F.kind < MC_SPEC || F.kind > MC_INTER) { delete D; return fail(MC_ERR_ARG, "invalid face kind"); }
-            if ((F.kind == MC_SPEC || F.kind == MC_DIFF || F.kind == MC_INTER) && p.T[f] != 0.) {
-                delete D; return fail(MC_ERR_ARG, "Cannot specify temperature");
-            }
-            V3 cr = cross(fi[f], fj[f]);
-            F.n = unit(cr);
-            F.area = std::sqrt(dot(cr, cr));
-            F.o = fo[f];
-            F.T = p.T[f];
-            if ((F.kind == MC_ISOT || F.kind == MC_PERI) && F.area * std::fabs(F.T) != 0.) faceEmit[s].push_back(f);
-        }
-        for (int k = 0; k < 3; ++k) {
-            if (p.div[k] >= MAX_SHAPE) { delete D; return fail(MC_ERR_UNSUPPORTED, "more than 511 cells along an axis"); }
+        if (int rc = buildShape(ps[s], H[s])) return rc;
+        if ((int)H[s].f.size() > MAX_FACES)
+            return fail(MC_ERR_UNSUPPORTED, "the GPU kernels take subdomains of at most 6 faces");
+        for (int k = 0; k < 3; ++k)
+            if (H[s].div[k] >= MAX_SHAPE) return fail(MC_ERR_UNSUPPORTED, "more than 511 cells along an axis");
+        // construction registers the emitting faces whose weight is nonzero
+        // (montecarlo/subdomain.cpp:205-212)
+        for (size_t f = 0; f < H[s].f.size(); ++f) {
+            const HostFace& F = H[s].f[f];
+            if ((F.kind == MC_ISOT || F.kind == MC_PERI) && F.area * std::fabs(F.T) != 0.) faceEmit[s].push_back((int)f);
         }
     }
     for (int q = 0; q < nq; ++q) {
         const mc_pair_desc& P = qs[q];
-        if (P.sdom1 < 0 || P.sdom1 >= n || P.sdom2 < 0 || P.sdom2 >= n || P.face1 < 0 || P.face1 > 5 ||
-            P.face2 < 0 || P.face2 > 5) { delete D; return fail(MC_ERR_ARG, "pair index out of range"); }
-        HostFace& a = D->faces[6 * P.sdom1 + P.face1];
-        HostFace& b = D->faces[6 * P.sdom2 + P.face2];
-        if (a.kind != P.kind || b.kind != P.kind) { delete D; return fail(MC_ERR_ARG, "pair kind does not match faces"); }
+        if (P.sdom1 < 0 || P.sdom1 >= n || P.sdom2 < 0 || P.sdom2 >= n || P.face1 < 0 ||
+            P.face1 >= (int)H[P.sdom1].f.size() || P.face2 < 0 || P.face2 >= (int)H[P.sdom2].f.size())
+            return fail(MC_ERR_ARG, "pair index out of range");
+        HostFace& a = H[P.sdom1].f[P.face1];
+        HostFace& b = H[P.sdom2].f[P.face2];
+        if (a.kind != P.kind || b.kind != P.kind) return fail(MC_ERR_ARG, "pair kind does not match faces");
         if (P.kind == MC_PERI) {
-            if (a.pairS >= 0 || b.pairS >= 0) { delete D; return fail(MC_ERR_ARG, "Boundary already paired"); }
+            if (a.pairS >= 0 || b.pairS >= 0) return fail(MC_ERR_ARG, "Boundary already paired");
             M3 R; std::memcpy(R.m, P.rot, sizeof(R.m));
             V3 t = mk(P.transl[0], P.transl[1], P.transl[2]);
             double T1 = a.T, T2 = b.T;
@@ -332,83 +523,122 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             a.pairS = P.sdom2; a.pairF = P.face2;
             b.pairS = P.sdom1; b.pairF = P.face1;
         } else if (P.kind == MC_INTER) {
-            if (a.ninter > 0 || b.ninter > 0) {
-                delete D; return fail(MC_ERR_UNSUPPORTED, "more than one pair on an Inter face");
-            }
+            if (a.ninter > 0 || b.ninter > 0) return fail(MC_ERR_UNSUPPORTED, "more than one pair on an Inter face");
             a.ninter++; b.ninter++;
             a.pairS = P.sdom2; a.pairF = P.face2;
             b.pairS = P.sdom1; b.pairF = P.face1;
-        } else { delete D; return fail(MC_ERR_ARG, "pair kind must be Peri or Inter"); }
+        } else {
+            return fail(MC_ERR_ARG, "pair kind must be Peri or Inter");
+        }
     }
     for (int s = 0; s < n; ++s)
-        for (int f = 0; f < 6; ++f) {
-            const HostFace& F = D->faces[6 * s + f];
-            if ((F.kind == MC_PERI || F.kind == MC_INTER) && F.pairS < 0) {
-                delete D; return fail(MC_ERR_ARG, "Domain setup not complete: unpaired face");
-            }
-        }
+        for (const HostFace& F : H[s].f)
+            if ((F.kind == MC_PERI || F.kind == MC_INTER) && F.pairS < 0)
+                return fail(MC_ERR_ARG, "Domain setup not complete: unpaired face");
     // subdomain images, emitters and columns
     long cols = 0;
     for (int s = 0; s < n; ++s) {
-        const mc_pped_desc& p = ps[s];
+        const mc_sdom_desc& p = ps[s];
+        const HostSdom& h = H[s];
+        const bool gen = h.shape != MC_PARALLELEPIPED;
         SdomD<double>& S = D->sd[s];
         std::memset(&S, 0, sizeof(S));
-        M3 M; std::memcpy(M.m, p.M, sizeof(M.m));
-        M3 Mi = inv3(M);
-        std::memcpy(S.M, M.m, sizeof(M.m));
+        M3 Mi = inv3(h.FM);
+        std::memcpy(S.M, h.FM.m, sizeof(S.M));
         std::memcpy(S.Minv, Mi.m, sizeof(Mi.m));
         bool neg = false;
         int npos = 0;
         for (int k = 0; k < 3; ++k) {
-            S.o[k] = p.o[k];
-            if (p.div[k] < 0) neg = true;
-            if (p.div[k] > 0) ++npos;
+            S.o[k] = h.fo[k];
+            if (h.div[k] < 0) neg = true;
+            if (h.div[k] > 0) ++npos;
             S.gradT[k] = p.gradT[k];
         }
+        S.gen = gen ? 1 : 0;
+        S.nface = (int)h.f.size();
         // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
         if (neg) S.accum = -2;
         else if (npos == 0) S.accum = -1;
-        else if (npos == 1) { int d = 0; for (int k = 1; k < 3; ++k) if (p.div[k] > p.div[d]) d = k; S.accum = d; }
+        else if (npos == 1) { int d = 0; for (int k = 1; k < 3; ++k) if (h.div[k] > h.div[d]) d = k; S.accum = d; }
         else S.accum = npos + 1;
         // walk cells: the tally cells, refined to WALK_CELLS on axes without
         // tally cells when the field is 0-D or 1-D
-        int tsh[3];
+        long tsh[3];
         for (int k = 0; k < 3; ++k) {
-            tsh[k] = (int)std::max(p.div[k], 1L);
-            const bool virt = neg || (p.div[k] <= 0 && S.accum <= 2);
-            S.shape[k] = virt ? WALK_CELLS : tsh[k];
+            tsh[k] = std::max(h.div[k], 1L);
+            const bool virt = neg || (h.div[k] <= 0 && S.accum <= 2);
+            S.shape[k] = virt ? WALK_CELLS : (int)tsh[k];
             S.S[k] = S.shape[k];
         }
-        S.tstride[0] = (!neg && p.div[0] > 0) ? 1 : 0;
-        S.tstride[1] = (!neg && p.div[1] > 0) ? tsh[0] : 0;
-        S.tstride[2] = (!neg && p.div[2] > 0) ? tsh[0] * tsh[1] : 0;
+        S.tstride[0] = (!neg && h.div[0] > 0) ? 1 : 0;
+        S.tstride[1] = (!neg && h.div[1] > 0) ? (int)tsh[0] : 0;
+        S.tstride[2] = (!neg && h.div[2] > 0) ? (int)(tsh[0] * tsh[1]) : 0;
         M3 gr = rotZTo(unit(mk(p.gradT[0], p.gradT[1], p.gradT[2])));
         std::memcpy(S.grot, gr.m, sizeof(gr.m));
         double maxn = 0.;
-        for (int c = 0; c < 3; ++c) { V3 cc = colOf(M, c); maxn = std::max(maxn, std::sqrt(dot(cc, cc))); }
+        for (int c = 0; c < 3; ++c) { V3 cc = colOf(h.M, c); maxn = std::max(maxn, std::sqrt(dot(cc, cc))); }
         S.eps = 100. * DEPS * maxn;  // FP32 images rescale this
-        double vol = det3(M);
         double gn = std::sqrt(dot(mk(p.gradT[0], p.gradT[1], p.gradT[2]), mk(p.gradT[0], p.gradT[1], p.gradT[2])));
-        double vw = 2. * vol * gn;  // montecarlo/subdomain.cpp:250-253
-        if (vw != 0.) { D->em.push_back(EmitterD{s, -1}); D->emWeight.push_back(vw); }
+        double vw = 2. * h.vol * gn;  // montecarlo/subdomain.cpp:250-253
+        if (vw != 0.) {
+            EmitterD E;
+            std::memset(&E, 0, sizeof(E));
+            E.sdom = s; E.face = -1; E.fold = -1; E.ncoord = 3; E.npiece = 1;
+            if (gen) {
+                const std::vector<V3>& c = h.col;
+                if (h.shape == MC_PRISM || h.shape == MC_PYRAMID) {
+                    E.fold = h.shape == MC_PRISM ? FOLD_PRISM : FOLD_TETRA;
+                    E.npiece = (int)h.subvol.size();
+                    if (E.npiece > MAX_PIECES) return fail(MC_ERR_UNSUPPORTED, "too many sub-volumes");
+                    for (int k = 0; k < E.npiece; ++k) setPiece(E, k, h, S.S, h.o, c[k + 1], c[k + 2], c[0]);
+                    setThresholds(E, h.subvol);
+                } else {
+                    E.fold = h.shape == MC_TRIANGULAR_PRISM ? FOLD_PRISM : FOLD_TETRA;
+                    setPiece(E, 0, h, S.S, h.o, c[0], c[1], c[2]);
+                    E.thr[0] = 4294967296ull;
+                }
+            }
+            D->em.push_back(E);
+            D->emWeight.push_back(vw);
+        }
         for (int f : faceEmit[s]) {
-            const HostFace& F = D->faces[6 * s + f];
-            D->em.push_back(EmitterD{s, f});
+            const HostFace& F = h.f[f];
+            EmitterD E;
+            std::memset(&E, 0, sizeof(E));
+            E.sdom = s; E.face = f; E.fold = -1; E.ncoord = 2; E.npiece = 1;
+            if (gen) {
+                const V3 z = mk(0, 0, 0);
+                if (F.shape == 2) {
+                    E.fold = FOLD_TRIANGLE;
+                    E.npiece = (int)F.tri.size();
+                    if (E.npiece > MAX_PIECES) return fail(MC_ERR_UNSUPPORTED, "too many polygon vertices");
+                    for (int k = 0; k < E.npiece; ++k) setPiece(E, k, h, S.S, F.o, F.verts[k], F.verts[k + 1], z);
+                    setThresholds(E, F.tri);
+                } else {
+                    E.fold = F.shape == 1 ? FOLD_TRIANGLE : FOLD_NONE;
+                    setPiece(E, 0, h, S.S, F.o, F.si, F.sj, z);
+                    E.thr[0] = 4294967296ull;
+                }
+            }
+            D->em.push_back(E);
             D->emWeight.push_back(F.area * std::fabs(F.T));  // montecarlo/boundary.cpp:413-416
         }
-        long sp = neg ? 0 : (long)tsh[0] * tsh[1] * tsh[2];
+        long sp = neg ? 0 : tsh[0] * tsh[1] * tsh[2];
         if (sp == 0) { S.colbeg = -1; D->colbeg.push_back(-1); continue; }
         S.colbeg = (int)cols;
         D->colbeg.push_back(cols);
-        for (long c = 0; c < sp; ++c) D->cellVol.push_back(vol / (double)sp);
+        long idx[3];
+        for (idx[2] = 0; idx[2] < tsh[2]; ++idx[2])
+            for (idx[1] = 0; idx[1] < tsh[1]; ++idx[1])
+                for (idx[0] = 0; idx[0] < tsh[0]; ++idx[0]) D->cellVol.push_back(cellVolume(h, tsh, idx));
         cols += sp;
     }
     D->cols = cols;
-    // faces: normals, rotations, pair maps in reduced coordinates
+    // faces: normals, rotations, planes, pair maps in frame coordinates
     for (int s = 0; s < n; ++s) {
         SdomD<double>& S = D->sd[s];
-        for (int f = 0; f < 6; ++f) {
-            const HostFace& F = D->faces[6 * s + f];
+        for (int f = 0; f < S.nface; ++f) {
+            const HostFace& F = H[s].f[f];
             FaceD<double>& G = S.f[f];
             G.kind = F.kind;
             G.to = -1; G.toface = -1; G.ident = 1;
@@ -419,17 +649,27 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             std::memcpy(G.Rd, I.m, sizeof(I.m));
             std::memcpy(G.A, I.m, sizeof(I.m));
             G.T = F.T;
+            if (S.gen) {
+                // signed distance n.x - n.fo at x = o + M diag(1/S) u
+                M3 SM;
+                std::memcpy(SM.m, S.M, sizeof(SM.m));
+                V3 g = mvec(transp(SM), F.n);
+                for (int k = 0; k < 3; ++k) G.gp[k] = g[k] / S.S[k];
+                G.gp[3] = dot(F.n, subv(mk(S.o[0], S.o[1], S.o[2]), F.o));
+            }
             if (F.kind == MC_PERI || F.kind == MC_INTER) {
                 const int t = F.pairS;
-                G.to = t; G.toface = F.pairF;
+                const SdomD<double>& T2 = D->sd[t];
+                G.to = t;
+                G.toface = T2.gen ? -1 : F.pairF;
                 M3 R = F.kind == MC_PERI ? F.R : eye();
                 V3 tr = F.kind == MC_PERI ? F.t : mk(0, 0, 0);
                 bool id = true;
                 for (int i = 0; i < 9; ++i) if (R.m[i] != eye().m[i]) id = false;
+                if (S.gen && !id) return fail(MC_ERR_UNSUPPORTED, "Peri rotation on a non-Parallelepiped face");
                 G.ident = id ? 1 : 0;
-                std::memcpy(G.Rd, R.m, sizeof(R.m));
+                if (!S.gen) std::memcpy(G.Rd, R.m, sizeof(R.m));
                 // u' = diag(S') Minv' (R (o + M diag(1/S) u) + t - o')
-                const SdomD<double>& T2 = D->sd[t];
                 M3 Mi2; std::memcpy(Mi2.m, T2.Minv, sizeof(Mi2.m));
                 M3 M1; std::memcpy(M1.m, S.M, sizeof(M1.m));
                 M3 A = mmul(mmul(Mi2, R), M1);
@@ -443,7 +683,7 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
                 // tangential identity: same axis, A = I and no tangential
                 // shift (within rounding of the FP64 products)
                 const int ax = f % 3;
-                bool tang = (F.pairF % 3) == ax;
+                bool tang = !S.gen && !T2.gen && (F.pairF % 3) == ax;
                 for (int i = 0; i < 3 && tang; ++i) {
                     if (i == ax) continue;  // the normal coordinate is snapped
                     for (int j = 0; j < 3; ++j)
@@ -455,8 +695,21 @@ int buildDomain(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             }
         }
     }
-    *out = D;
+    *out = D.release();
     return MC_OK;
+}
+
+// A Parallelepiped description as a general one (mat column-major).
+mc_sdom_desc sdomOfPped(const mc_pped_desc& p) {
+    mc_sdom_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.shape = MC_PARALLELEPIPED;
+    d.ncols = 3;
+    for (int k = 0; k < 3; ++k) { d.o[k] = p.o[k]; d.div[k] = p.div[k]; d.gradT[k] = p.gradT[k]; }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) d.mat[3 * c + r] = p.M[3 * r + c];
+    for (int k = 0; k < 6; ++k) { d.kind[k] = p.kind[k]; d.T[k] = p.T[k]; }
+    return d;
 }
 
 // Field rows of a problem (montecarlo/problem.cpp:470-471,502-503,535-536,
@@ -520,7 +773,9 @@ void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
     b.eps = (R)(f32 ? a.eps / DEPS * (double)std::numeric_limits<float>::epsilon() : a.eps);
     b.accum = a.accum;
     b.colbeg = a.colbeg;
-    for (int f = 0; f < 6; ++f) {
+    b.gen = a.gen;
+    b.nface = a.nface;
+    for (int f = 0; f < MAX_FACES; ++f) {
         const FaceD<double>& x = a.f[f];
         FaceD<R>& y = b.f[f];
         y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident; y.tang = x.tang;
@@ -571,6 +826,7 @@ struct mc_session_s {
     double* log_d = nullptr;
     int* logcnt_d = nullptr;
     int lean = -1;                // static schedule: axis of the lean flight, or -1
+    bool gen = false;             // the domain has subdomains other than the Parallelepiped
     long long slots = 0;          // phonon slots per half of the state
     unsigned* reg_d = nullptr;    // static schedule: front / back live counts
                                   // per block region, one array per half
@@ -732,14 +988,17 @@ int setupSession(mc_session_s* S) {
     // static schedule with a shared 1-D field along one axis in every
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
+    S->gen = false;
+    for (const auto& x : D.sd) S->gen = S->gen || x.gen;
+    if (S->gen && S->replay) return fail(MC_ERR_UNSUPPORTED, "replay streams take Parallelepiped domains only");
     if (!S->dyn && !S->replay && !S->logging && S->tm == TM_SHARED) {
         const int k = D.sd[0].accum;
         bool same = k >= 0 && k <= 2;
-        for (const auto& x : D.sd) same = same && x.accum == k;
+        for (const auto& x : D.sd) same = same && x.accum == k && !x.gen;
         if (same) S->lean = k;
     }
     int occ = S->lean >= 0 ? advanceLeanOccupancy<R>(S->lean, S->block, S->smem)
-                           : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->block, S->smem);
+                           : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
     // state: two halves of (P0, P1, P2). The static schedule cuts each half
@@ -856,7 +1115,8 @@ int advanceT(mc_session_s* S, int nl, int* done) {
             P.live_in = cur;
             P.live_out = cur + 1;
             CK(cudaMemsetAsync(cur + 1, 0, sizeof(unsigned long long), S->stream));
-            CK(launchAdvance<R>(P, true, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+            CK(launchAdvance<R>(P, true, S->replay, S->logging, S->tm, S->gen, S->grid, S->block, S->smem,
+                                S->stream));
             S->launches++;
             S->step += S->desc.steps_per_launch;
             if (S->desc.compact_interval > 0 && ++S->sinceCompact >= S->desc.compact_interval &&
@@ -878,7 +1138,8 @@ int advanceT(mc_session_s* S, int nl, int* done) {
             P.regIn = S->reg_d + 2 * (size_t)S->grid * S->parity;
             P.regOut = S->reg_d + 2 * (size_t)S->grid * (S->parity ^ 1);
             if (S->lean >= 0) CK(launchAdvanceLean<R>(P, S->lean, S->grid, S->block, S->smem, S->stream));
-            else CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->grid, S->block, S->smem, S->stream));
+            else CK(launchAdvance<R>(P, false, S->replay, S->logging, S->tm, S->gen, S->grid, S->block, S->smem,
+                                     S->stream));
             S->parity ^= 1;
             S->step += S->desc.steps_per_launch;
             S->launches++;
@@ -981,6 +1242,7 @@ struct mc_batch_s {
     long long cap = 0;
     int block = 256, grid = 0;
     int tm = 2;                     // field mode of the advance launches (batchFieldMode)
+    bool gen = false;               // some instance has a subdomain other than the Parallelepiped
     SegD* segs = nullptr;           // work segments of the advance launches
     int* home = nullptr;            // first segment of each block
     unsigned long long* segNext = nullptr;
@@ -1201,7 +1463,10 @@ int setupBatch(mc_batch_s* B) {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     B->tm = batchFieldMode<R>(inst);
-    const int occ = advanceBatchOccupancy<R>(B->tm, batchSmemBytes<R>(P), B->block);
+    B->gen = false;
+    for (int i = 0; i < n; ++i)
+        for (const auto& x : B->doms[i]->sd) B->gen = B->gen || x.gen;
+    const int occ = advanceBatchOccupancy<R>(B->tm, B->gen, batchSmemBytes<R>(P), B->block);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
     B->grid = B->bd.grid_blocks > 0 ? B->bd.grid_blocks : occ * nsm;
     std::vector<SegD> segs;
@@ -1236,7 +1501,7 @@ int enqueueBatch(mc_batch_s* B) {
         setWindow(P);
         CK(cudaMemsetAsync(B->cnt + C_NCOUNTERS + 1, 0, sizeof(unsigned long long), B->stream));
         CK(cudaMemsetAsync(B->segNext, 0, sizeof(unsigned long long) * std::max(B->nseg, 1), B->stream));
-        CK(launchAdvanceBatch<R>(P, B->tm, B->grid, B->block, B->stream));
+        CK(launchAdvanceBatch<R>(P, B->tm, B->gen, B->grid, B->block, B->stream));
         ++launches;
     }
     CK(launchDifPrefix<R>(P, B->stream));
@@ -1481,7 +1746,7 @@ struct ServerT : ServerBase {
         double vol = 0.;
         for (double v : D.cellVol) vol += v;
         j->volume = j->req.volume > 0. ? j->req.volume : vol;
-        j->grad = j->req.gradient != 0. ? j->req.gradient : D.pp[0].gradT[j->req.axis];
+        j->grad = j->req.gradient != 0. ? j->req.gradient : D.desc[0].gradT[j->req.axis];
         if (j->grad == 0.) return fail(MC_ERR_ARG, "no temperature gradient along the kappa axis");
         InstD<R> I;
         std::memset(&I, 0, sizeof(I));
@@ -1531,7 +1796,10 @@ struct ServerT : ServerBase {
             }
         }
         const int tm = batchFieldMode<R>(inst);
-        const int occ = advanceBatchOccupancy<R>(tm, batchSmemBytes<R>(P), block);
+        bool gen = false;
+        for (SrvJob* j : run)
+            for (const auto& x : j->req.dom->sd) gen = gen || x.gen;
+        const int occ = advanceBatchOccupancy<R>(tm, gen, batchSmemBytes<R>(P), block);
         if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
         const int grid = std::min(occ, 64) * nsm;
         std::vector<SegD> segs;
@@ -1558,7 +1826,7 @@ struct ServerT : ServerBase {
         P.step0 = 0;
         setWindow(P);
         CK(launchEmitBatch<R>(P, stream));
-        CK(launchAdvanceBatch<R>(P, tm, grid, block, stream));
+        CK(launchAdvanceBatch<R>(P, tm, gen, grid, block, stream));
         CK(launchDifPrefix<R>(P, stream));
         CK(launchRoundReduce<R>(P, accs_d, gsum_d, stream));
         std::vector<double> gsum((size_t)n * MAX_GROUPS * 4);
@@ -1894,7 +2162,10 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int occ = advanceOccupancy<R>(true, false, false, S->tm, S->block, S->smem);
+    bool gen = false;
+    for (const auto& x : D.sd) gen = gen || x.gen;
+    S->gen = gen;
+    const int occ = advanceOccupancy<R>(true, false, false, S->tm, gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
     paramsOf<R>(S) = P;
@@ -1943,6 +2214,15 @@ int mc_material_tables(mc_material_h m, double* vel, double* tau) {
 void mc_material_destroy(mc_material_h m) { delete m; }
 
 int mc_domain_create(const mc_pped_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_h* out) {
+    if (!out) return fail(MC_ERR_ARG, "null output handle");
+    if (nq > 0 && !qs) return fail(MC_ERR_ARG, "null pair list");
+    if (!ps || n <= 0) return fail(MC_ERR_ARG, "Domain setup not complete");
+    std::vector<mc_sdom_desc> v;
+    for (int i = 0; i < n; ++i) v.push_back(sdomOfPped(ps[i]));
+    return buildDomain(v.data(), n, qs, nq, out);
+}
+
+int mc_domain_create_shapes(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_h* out) {
     if (!out) return fail(MC_ERR_ARG, "null output handle");
     if (nq > 0 && !qs) return fail(MC_ERR_ARG, "null pair list");
     return buildDomain(ps, n, qs, nq, out);

@@ -275,7 +275,7 @@ inline void setSingleLayout(Params<R>& P, const SmemLayout& L) {
 // next event lies beyond this window, take leanFlight; the walker runs for
 // the front range, for a back-range phonon that does meet an event, and in
 // the window that ends the horizon.
-template <typename R, bool REPLAY, bool LOG, int TM, int LEAN>
+template <typename R, bool REPLAY, bool LOG, int TM, int LEAN, bool GEN = false>
 __global__ void __launch_bounds__(STATIC_MAX_THREADS, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
 k_advance(Params<R> P) {
     static_assert(LEAN < 0 || (!REPLAY && !LOG && TM == TM_SHARED), "the lean flight needs a plain shared-field launch");
@@ -404,7 +404,7 @@ k_advance(Params<R> P) {
                 }
             }
             if (have && lean == LEAN_EVENT) {
-                Walker<R, REPLAY, LOG, TM, ParamView<R, TM>, true> wk;
+                Walker<R, REPLAY, LOG, TM, ParamView<R, TM>, true, GEN> wk;
                 wk.load(P, V, W, A0, A1, A2);
                 while (!wk.iterate(P, W)) {}
                 alive = wk.finishInto(P, W, nSteps, nEvents);
@@ -456,13 +456,13 @@ k_advance(Params<R> P) {
 // host compacts).
 constexpr int REFILL = 8;
 
-template <typename R, bool REPLAY, bool LOG, int TM, typename IA>
+template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool GEN = false>
 __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
                                             unsigned long long qbeg, unsigned long long qend,
                                             const IA& I, const Window<R>& W) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    Walker<R, REPLAY, LOG, TM, IA> wk;
+    Walker<R, REPLAY, LOG, TM, IA, false, GEN> wk;
     bool have = false;
     unsigned long long slot = 0;
     bool drained = qbeg >= qend;
@@ -517,7 +517,7 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
 }
 
 // Block b owns the live slots [b C, (b + 1) C) of the launch.
-template <typename R, bool REPLAY, bool LOG, int TM>
+template <typename R, bool REPLAY, bool LOG, int TM, bool GEN = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ unsigned long long qnext;
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     const unsigned long long qend = min(qbeg + chunk, n);
     ParamView<R, TM> V;
     V.init(P, smraw);
-    dynamicLoop<R, REPLAY, LOG, TM>(P, &qnext, qbeg, qend, V, W);
+    dynamicLoop<R, REPLAY, LOG, TM, ParamView<R, TM>, GEN>(P, &qnext, qbeg, qend, V, W);
     closeBlock<R, TM>(P, *I);
 }
 
@@ -604,7 +604,7 @@ __device__ __forceinline__ void flushBinding(const InstD<R>& I, int group) {
 // (TM_SHARED: all stage a shared field; TM_GLOBAL: all add to their global
 // field; TM_NONE: none keeps a field), else TM_AUTO (per instance): a launch
 // whose instances agree runs without the code of the other modes.
-template <typename R, int TM>
+template <typename R, int TM, bool GEN = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_batch(Params<R> P) {
     extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ int sSeg;
@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
             curInst = S.inst;
         }
         __syncthreads();
-        dynamicLoop<R, false, false, TM>(P, P.segNext + sg, (unsigned long long)S.beg,
+        dynamicLoop<R, false, false, TM, BatchView<R>, GEN>(P, P.segNext + sg, (unsigned long long)S.beg,
                                               (unsigned long long)S.end, BatchView<R>{&P, smraw, I}, W);
         __syncthreads();
         flushBinding<R>(*I, S.group);

@@ -13,8 +13,8 @@ cudaError_t launchEmit(const Params<R>& p, bool replay, cudaStream_t s);
 
 // tm: TM_SHARED or TM_GLOBAL; dyn: the dynamic-refill kernel
 template <typename R>
-cudaError_t launchAdvance(const Params<R>& p, bool dyn, bool replay, bool log, int tm, int grid, int block,
-                          size_t smem, cudaStream_t s);
+cudaError_t launchAdvance(const Params<R>& p, bool dyn, bool replay, bool log, int tm, bool gen, int grid,
+                          int block, size_t smem, cudaStream_t s);
 
 template <typename R>
 cudaError_t launchCompact(const Params<R>& p, int grid, cudaStream_t s);
@@ -31,11 +31,11 @@ cudaError_t launchEmitBatch(const Params<R>& p, cudaStream_t s);
 // tm: the launch's common field mode (TM_SHARED / TM_GLOBAL / TM_NONE) or
 // TM_AUTO (batchFieldMode)
 template <typename R>
-cudaError_t launchAdvanceBatch(const Params<R>& p, int tm, int grid, int block, cudaStream_t s);
+cudaError_t launchAdvanceBatch(const Params<R>& p, int tm, bool gen, int grid, int block, cudaStream_t s);
 template <typename R>
 cudaError_t launchDifPrefix(const Params<R>& p, cudaStream_t s);
 template <typename R>
-int advanceBatchOccupancy(int tm, size_t smem, int block);
+int advanceBatchOccupancy(int tm, bool gen, size_t smem, int block);
 template <typename R>
 cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
                               cudaStream_t s);
@@ -47,6 +47,6 @@ cudaError_t launchWaitCheck(unsigned* status, unsigned long long limitNs, unsign
 // Maximum resident blocks per SM of the advance kernel for this
 // configuration (0 if it cannot launch).
 template <typename R>
-int advanceOccupancy(bool dyn, bool replay, bool log, int tm, int block, size_t smem);
+int advanceOccupancy(bool dyn, bool replay, bool log, int tm, bool gen, int block, size_t smem);
 
 }  // namespace mcg

@@ -12,9 +12,11 @@ static cudaError_t prepare(K fn, size_t smem) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
-template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
+// GEN: the kernels that also take subdomains other than the Parallelepiped
+// (compiled for the non-replay launches only).
+template <typename R, bool DYN, bool REPLAY, bool LOG, int TM, bool GEN = false>
 static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t smem, cudaStream_t s) {
-    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM, -1>;
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM, GEN> : k_advance<R, REPLAY, LOG, TM, -1, GEN>;
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
     // the static kernel adds its producer warp to the `block` consumers
@@ -22,9 +24,9 @@ static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t sm
     return cudaGetLastError();
 }
 
-template <typename R, bool DYN, bool REPLAY, bool LOG, int TM>
+template <typename R, bool DYN, bool REPLAY, bool LOG, int TM, bool GEN = false>
 static int occOne(int block, size_t smem) {
-    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM> : k_advance<R, REPLAY, LOG, TM, -1>;
+    auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM, GEN> : k_advance<R, REPLAY, LOG, TM, -1, GEN>;
     if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, DYN ? block : block + STATIC_PRODUCER_THREADS, smem) !=
@@ -83,7 +85,8 @@ cudaError_t launchEmitBatch<MC_REAL>(const Params<MC_REAL>& p, cudaStream_t s) {
 }
 
 template <typename R>
-static auto batchKernel(int tm) {
+static auto batchKernel(int tm, bool gen) {
+    if (gen) return k_advance_batch<R, TM_AUTO, true>;
     return tm == TM_SHARED ? k_advance_batch<R, TM_SHARED>
          : tm == TM_GLOBAL ? k_advance_batch<R, TM_GLOBAL>
          : tm == TM_NONE   ? k_advance_batch<R, TM_NONE>
@@ -91,9 +94,10 @@ static auto batchKernel(int tm) {
 }
 
 template <>
-cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int tm, int grid, int block, cudaStream_t s) {
+cudaError_t launchAdvanceBatch<MC_REAL>(const Params<MC_REAL>& p, int tm, bool gen, int grid, int block,
+                                        cudaStream_t s) {
     const size_t smem = batchSmemBytes<MC_REAL>(p);
-    auto fn = batchKernel<MC_REAL>(tm);
+    auto fn = batchKernel<MC_REAL>(tm, gen);
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
     fn<<<grid, block, smem, s>>>(p);
@@ -114,8 +118,8 @@ cudaError_t launchRoundReduce<MC_REAL>(const Params<MC_REAL>& p, double* const* 
 }
 
 template <>
-int advanceBatchOccupancy<MC_REAL>(int tm, size_t smem, int block) {
-    auto fn = batchKernel<MC_REAL>(tm);
+int advanceBatchOccupancy<MC_REAL>(int tm, bool gen, size_t smem, int block) {
+    auto fn = batchKernel<MC_REAL>(tm, gen);
     if (prepare(fn, smem) != cudaSuccess) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem) != cudaSuccess) return 0;
@@ -123,6 +127,18 @@ int advanceBatchOccupancy<MC_REAL>(int tm, size_t smem, int block) {
 }
 
 #define MC_DISPATCH(F, ...)                                                                 \
+    if (gen) {                                                                             \
+        if (dyn) {                                                                         \
+            if (tm == TM_SHARED) return log ? F<MC_REAL, true, false, true, TM_SHARED, true>(__VA_ARGS__)  \
+                                            : F<MC_REAL, true, false, false, TM_SHARED, true>(__VA_ARGS__); \
+            return log ? F<MC_REAL, true, false, true, TM_GLOBAL, true>(__VA_ARGS__)          \
+                       : F<MC_REAL, true, false, false, TM_GLOBAL, true>(__VA_ARGS__);        \
+        }                                                                                  \
+        if (tm == TM_SHARED) return log ? F<MC_REAL, false, false, true, TM_SHARED, true>(__VA_ARGS__)     \
+                                        : F<MC_REAL, false, false, false, TM_SHARED, true>(__VA_ARGS__);    \
+        return log ? F<MC_REAL, false, false, true, TM_GLOBAL, true>(__VA_ARGS__)             \
+                   : F<MC_REAL, false, false, false, TM_GLOBAL, true>(__VA_ARGS__);           \
+    }                                                                                      \
     if (dyn) {                                                                             \
         if (tm == TM_SHARED) {                                                             \
             if (replay) return log ? F<MC_REAL, true, true, true, TM_SHARED>(__VA_ARGS__)   \
@@ -147,13 +163,13 @@ int advanceBatchOccupancy<MC_REAL>(int tm, size_t smem, int block) {
                : F<MC_REAL, false, false, false, TM_GLOBAL>(__VA_ARGS__);
 
 template <>
-cudaError_t launchAdvance<MC_REAL>(const Params<MC_REAL>& p, bool dyn, bool replay, bool log, int tm, int grid,
-                                   int block, size_t smem, cudaStream_t s) {
+cudaError_t launchAdvance<MC_REAL>(const Params<MC_REAL>& p, bool dyn, bool replay, bool log, int tm, bool gen,
+                                   int grid, int block, size_t smem, cudaStream_t s) {
     MC_DISPATCH(advanceOne, p, grid, block, smem, s)
 }
 
 template <>
-int advanceOccupancy<MC_REAL>(bool dyn, bool replay, bool log, int tm, int block, size_t smem) {
+int advanceOccupancy<MC_REAL>(bool dyn, bool replay, bool log, int tm, bool gen, int block, size_t smem) {
     MC_DISPATCH(occOne, block, smem)
 }
 

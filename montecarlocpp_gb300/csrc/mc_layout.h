@@ -50,23 +50,32 @@ enum Status {
     S_TIMEOUT = 8,  // a bounded device-side wait gave up (results discarded)
 };
 
-// One face of a Parallelepiped subdomain in reduced coordinates: face f
-// lies on axis f % 3 at u = 0 (f < 3) or u = S (f >= 3).
+// One face of a subdomain. A Parallelepiped's face f lies on axis f % 3 of
+// its reduced coordinates at u = 0 (f < 3) or u = S (f >= 3). The faces of
+// the other shapes (SdomD::gen) are planes in the subdomain's frame
+// coordinates: gp[0..2] . u + gp[3] is the signed distance from the face,
+// kept in place of Rd (such faces take Peri pairs without rotation only).
 template <typename R>
 struct FaceD {
     int kind;
     int to;       // destination subdomain (Peri / Inter), else -1
-    int toface;   // face of `to` the phonon arrives on
+    int toface;   // axis face of `to` the phonon arrives on, -1 for none
     int ident;    // 1 if the Peri rotation is the identity
     int tang;     // 1 if the map keeps the tangential cell coordinates
     int pad;
     R n[3];       // inward unit normal (Spec reflection)
     R rot[9];     // rotation z-hat -> n, row-major (Diff, Isot emission)
-    R Rd[9];      // Peri direction rotation, row-major
+    union {
+        R Rd[9];  // Peri direction rotation, row-major
+        R gp[4];  // plane in frame coordinates (general faces)
+    };
     R A[9];       // reduced-coordinate map into subdomain `to`: u' = A u + b
     R b[3];
     R T;          // emission temperature after pairing (Isot / Peri)
 };
+
+// Largest face count of a subdomain on the device.
+constexpr int MAX_FACES = 6;
 
 template <typename R>
 struct SdomD {
@@ -83,13 +92,32 @@ struct SdomD {
                      // no tally cells
     int accum;       // Subdomain::accumFlag (montecarlo/subdomain.cpp:47-70)
     int colbeg;      // first field column, -1 if the subdomain has none
-    FaceD<R> f[6];
+    int gen;         // 1: not a Parallelepiped (faces are frame-coordinate
+                     // planes, the frame a box around the shape)
+    int nface;       // faces in the reference's bdry<I>() order
+    FaceD<R> f[MAX_FACES];
 };
 
-// Emitter: a volume (face = -1) or a face of a subdomain.
+// Largest number of pieces (sub-triangles of a Polygon face, sub-volumes of
+// a Prism or Pyramid) of an emitter.
+constexpr int MAX_PIECES = 7;
+
+// Emitter: a volume (face = -1) or a face of a subdomain. Parallelepiped
+// emitters (fold < 0) draw in the subdomain's reduced coordinates. The
+// others draw a piece (one uniform against thr when npiece > 1), then
+// ncoord uniforms c folded per `fold`, and start at u = U0 + L c in the
+// subdomain's frame coordinates.
+enum { FOLD_NONE = 0, FOLD_PRISM = 1, FOLD_TETRA = 2, FOLD_TRIANGLE = 3 };
 struct EmitterD {
     int sdom;
     int face;
+    int fold;    // -1 Parallelepiped, else FOLD_*
+    int ncoord;  // 2 (faces) or 3 (volumes)
+    int npiece;
+    int pad;
+    unsigned long long thr[MAX_PIECES];  // piece i: first i with word < thr[i]
+    double U0[MAX_PIECES][3];
+    double L[MAX_PIECES][9];             // row-major
 };
 
 // Packed cell: 5-bit subdomain, three 9-bit cell indices.

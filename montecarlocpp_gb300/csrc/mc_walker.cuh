@@ -625,7 +625,7 @@ __device__ __forceinline__ void emitOne(const InstD<R>& I, long long n, G& g, Ph
         int mid = (lo + hi) >> 1;
         if (I.emitCdf[mid] <= n) lo = mid + 1; else hi = mid;
     }
-    const EmitterD E = I.em[lo];
+    const EmitterD& E = I.em[lo];
     const SdomD<R>& S = I.sd[E.sdom];
     g.setEvent(0);
     ph.s = E.sdom;
@@ -638,7 +638,50 @@ __device__ __forceinline__ void emitOne(const InstD<R>& I, long long n, G& g, Ph
     }
     R u[3];
     R dir[3];
-    if (E.face >= 0) {
+    if (E.fold >= 0) {
+        // a shape other than the Parallelepiped: the piece (Polygon
+        // triangle, Prism / Pyramid sub-volume), then the folded uniforms
+        // (montecarlo/subdomain.cpp:309-373,399-441,
+        // montecarlo/boundary.cpp:180-186,246-256)
+        int k = 0;
+        if (E.npiece > 1) {
+            const unsigned long long x = g.next();
+            while (k < E.npiece - 1 && x >= E.thr[k]) ++k;
+        }
+        R c0 = u01<R>(g.next()), c1 = u01<R>(g.next());
+        R c2 = E.ncoord == 3 ? u01<R>(g.next()) : R(0);
+        if (E.fold == FOLD_TRIANGLE) {
+            if (!(c0 + c1 < R(1))) { c0 = R(1) - c0; c1 = R(1) - c1; }
+        } else if (E.fold == FOLD_PRISM || E.fold == FOLD_TETRA) {
+            if (c0 + c1 > R(1)) { c0 = R(1) - c0; c1 = R(1) - c1; }
+            if (E.fold == FOLD_TETRA) {
+                if (c1 + c2 > R(1)) {
+                    const R t = c2;
+                    c2 = R(1) - c0 - c1;
+                    c1 = R(1) - t;
+                } else if (c0 + c1 + c2 > R(1)) {
+                    const R t = c2;
+                    c2 = c0 + c1 + c2 - R(1);
+                    c0 = R(1) - c1 - t;
+                }
+            }
+        }
+        const double cc[3] = {(double)c0, (double)c1, (double)c2};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            u[r] = (R)(E.U0[k][r] + ((E.L[k][3 * r] * cc[0] + E.L[k][3 * r + 1] * cc[1]) + E.L[k][3 * r + 2] * cc[2]));
+        R v[3];
+        if (E.face >= 0) {
+            const FaceD<R>& F = S.f[E.face];
+            drawAniso<R>(g, false, v);
+            rotate(F.rot, v, dir);
+            ph.neg = !(F.T >= R(0));
+        } else {
+            drawAniso<R>(g, true, v);
+            rotate(S.grot, v, dir);
+            ph.neg = !(((dir[0] * S.gradT[0] + dir[1] * S.gradT[1]) + dir[2] * S.gradT[2]) < R(0));
+        }
+    } else if (E.face >= 0) {
         // EmitBoundary: position on the face (montecarlo/boundary.cpp:147-152,
         // 418-421), cosine direction about the inward normal (423-426)
         const FaceD<R>& F = S.f[E.face];
@@ -720,6 +763,14 @@ __host__ __device__ inline void setWindow(Params<R>& P) {
     P.wNext = (R)(P.ksteps < after ? P.ksteps : after) * P.dt;
 }
 
+// Signed distance of the phonon from a general face (SdomD::gen), from its
+// frame coordinates u = idx + off.
+template <typename R>
+__device__ __forceinline__ R planeDist(const FaceD<R>& F, const Phn<R>& ph) {
+    const R u0 = (R)ph.idx[0] + ph.off[0], u1 = (R)ph.idx[1] + ph.off[1], u2 = (R)ph.idx[2] + ph.off[2];
+    return ((F.gp[0] * u0 + F.gp[1] * u1) + F.gp[2] * u2) + F.gp[3];
+}
+
 // Walker state that only the replay kernels carry.
 struct NoReplay {};
 template <bool REPLAY> struct ReplayState { using T = NoReplay; };
@@ -732,7 +783,9 @@ constexpr uint32_t PROP_DEAD = 1u << 25;
 // from it. iterate() runs one loop iteration of montecarlo/problem.cpp:401-435
 // (flight to the next event or to the end of the window, its tally, the
 // event); finish() closes the phonon's window.
-template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool COMPACT = false>
+// GEN: the kernel also takes subdomains other than the Parallelepiped
+// (their face planes and escape test); without it that code is compiled out.
+template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool COMPACT = false, bool GEN = false>
 struct Walker {
     Phn<R> ph;
     IA I;
@@ -783,19 +836,57 @@ struct Walker {
         // strict < keeps the first of equals
         R sev = ph.scatNext;
         int face = -1;
+        const bool gen = GEN && S->gen != 0;
+        if (!gen) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const R dist = (-(R)ph.idx[k] - ph.off[k]) * ia[k];
-            if (a[k] < R(0) && dist < sev) { sev = dist; face = k; }
-        }
+            for (int k = 0; k < 3; ++k) {
+                const R dist = (-(R)ph.idx[k] - ph.off[k]) * ia[k];
+                if (a[k] < R(0) && dist < sev) { sev = dist; face = k; }
+            }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const R dist = (((R)(S->shape[k] - ph.idx[k])) - ph.off[k]) * ia[k];
-            if (a[k] > R(0) && dist < sev) { sev = dist; face = k + 3; }
+            for (int k = 0; k < 3; ++k) {
+                const R dist = (((R)(S->shape[k] - ph.idx[k])) - ph.off[k]) * ia[k];
+                if (a[k] > R(0) && dist < sev) { sev = dist; face = k + 3; }
+            }
+        } else {
+            // general faces: planes in frame coordinates, approached when
+            // n . d < 0, at distance -(signed distance) / (n . d)
+            // (montecarlo/boundary.cpp:102-110)
+#pragma unroll 1
+            for (int j = 0; j < S->nface; ++j) {
+                const FaceD<R>& F = S->f[j];
+                const R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
+                if (!(nd < R(0))) continue;
+                const R dist = -planeDist(F, ph) / nd;
+                if (dist < sev) { sev = dist; face = j; }
+            }
         }
         const R tev = sev * iv;
         const bool event = tev <= budget;
         const R s = event ? sev : budget * v;
+        if (gen && event) {
+            // after the move: killed if it went back by more than eps or
+            // left the subdomain (montecarlo/subdomain.cpp:176-189); the
+            // flight is not tallied
+            bool out = sev < -S->eps;
+#pragma unroll 1
+            for (int j = 0; j < S->nface; ++j) {
+                const FaceD<R>& F = S->f[j];
+                const R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
+                if (planeDist(F, ph) + s * nd < -S->eps) out = true;
+            }
+            if (out) {
+                stop = C_ESCAPES;
+                if (LOG) {
+                    double x[3]; physPos(*S, ph, x);
+                    for (int k = 0; k < 3; ++k) x[k] += (double)s * (double)ph.d[k];
+                    logEvent(P, ph, ph.s, -3, ph.s, x,
+                             (double)P.step0 * (double)P.dt + (double)(W.len - budget) + (double)tev,
+                             ph.idx[0] * S->tstride[0] + ph.idx[1] * S->tstride[1] + ph.idx[2] * S->tstride[2]);
+                }
+                return true;
+            }
+        }
         // tally amounts per metre (montecarlo/problem.cpp:473-544)
         Tally<R, TM, IA> T;
         T.V = I;
@@ -833,7 +924,7 @@ struct Walker {
         // the event: a relaxation scatter (kind -1) or the face's boundary
         const FaceD<R>* F = face >= 0 ? &S->f[face] : nullptr;
         const int kind = face >= 0 ? F->kind : -1;
-        if (face >= 0) {
+        if (face >= 0 && !gen) {
             // the flight ends on the face: snap that coordinate
 #pragma unroll
             for (int k = 0; k < 3; ++k) {

@@ -1,21 +1,26 @@
-"""Domain descriptions: assemblies of Parallelepiped subdomains.
+"""Domain descriptions: assemblies of subdomains.
 
-A montecarlocpp Domain is a set of ``Parallelepiped<Bac, Lef, Bot, Fro, Rig,
-Top>`` subdomains (montecarlo/subdomain.h:128-198) joined by ``makePair``
-calls (Inter pairs montecarlo/boundary.cpp:361-369, Peri pairs
+A montecarlocpp Domain is a set of subdomains -- ``Parallelepiped``,
+``TriangularPrism``, ``Tetrahedron``, ``Prism<N>`` and ``Pyramid<N>``
+(montecarlo/subdomain.h:128-640) -- joined by ``makePair`` calls (Inter
+pairs montecarlo/boundary.cpp:361-369, Peri pairs
 montecarlo/boundary.cpp:524-550). This module keeps exactly those primitive
 constructor arguments -- origin, edge matrix, divisions, volumetric
 temperature gradient, the kind and temperature of each face, and the pair
 list -- and nothing derived from them; the library derives normals, plane
 offsets, rotations, emitter weights and field strides itself.
 
-Faces are numbered as the reference's ``bdry<I>()``: 0 Bac (origin, edges
-col1 x col2), 1 Lef, 2 Bot, 3 Fro (origin + col0), 4 Rig, 5 Top.
+Faces are numbered as the reference's ``bdry<I>()``. Parallelepiped: 0 Bac
+(origin, edges col1 x col2), 1 Lef, 2 Bot, 3 Fro (origin + col0), 4 Rig, 5
+Top. TriangularPrism: Bac, Lef, Bot, Dia, Top. Tetrahedron: Bac, Lef, Bot,
+Dia. Prism<N>: Bot, Top, then the N sides. Pyramid<N>: Bot, then the N
+sides.
 
-FilmDomain and BulkDomain restate montecarlo/domain.cpp:137-199. The
-cross-plane film and the periodic pore cell are assembled only from the
-reference's public building blocks (Parallelepiped, IsotBoundary,
-SpecBoundary, DiffBoundary, InterBoundary, PeriBoundary, makePair).
+FilmDomain, BulkDomain, PyrDomain, HexDomain, JctDomain, TeeDomain and
+TubeDomain restate montecarlo/domain.cpp:137-570. The cross-plane film and
+the periodic pore cell are assembled only from the reference's public
+building blocks (Parallelepiped, IsotBoundary, SpecBoundary, DiffBoundary,
+InterBoundary, PeriBoundary, makePair).
 """
 
 from __future__ import annotations
@@ -27,11 +32,14 @@ import numpy as np
 SPEC, DIFF, ISOT, PERI, INTER = 0, 1, 2, 3, 4
 KIND_NAMES = {SPEC: "Spec", DIFF: "Diff", ISOT: "Isot", PERI: "Peri", INTER: "Inter"}
 BAC, LEF, BOT, FRO, RIG, TOP = range(6)
+PARALLELEPIPED, TRIANGULAR_PRISM, TETRAHEDRON, PRISM, PYRAMID = range(5)
 
 __all__ = [
     "SPEC", "DIFF", "ISOT", "PERI", "INTER", "BAC", "LEF", "BOT", "FRO", "RIG", "TOP",
-    "Parallelepiped", "Pair", "Domain", "FilmDomain", "BulkDomain",
-    "CrossPlaneFilmDomain", "PoreCellDomain",
+    "PARALLELEPIPED", "TRIANGULAR_PRISM", "TETRAHEDRON", "PRISM", "PYRAMID",
+    "Parallelepiped", "TriangularPrism", "Tetrahedron", "Prism", "Pyramid", "Pair", "Domain",
+    "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "PyrDomain", "HexDomain",
+    "JctDomain", "TeeDomain", "TubeDomain",
 ]
 
 
@@ -44,6 +52,8 @@ class Parallelepiped:
     kinds: tuple  # 6 face kinds
     T: tuple = (0.0,) * 6
 
+    shape_kind = PARALLELEPIPED
+
     def shape(self):
         d = np.asarray(self.div)
         if (d < 0).any():
@@ -52,6 +62,87 @@ class Parallelepiped:
 
     def vol(self) -> float:
         return float(np.linalg.det(self.M))
+
+    def columns(self) -> np.ndarray:
+        return np.asarray(self.M, dtype=np.float64)
+
+    def divisions(self) -> np.ndarray:
+        return np.asarray(self.div, dtype=np.int64)
+
+
+@dataclass
+class TriangularPrism(Parallelepiped):
+    """TriangularPrism<Bac, Lef, Bot, Dia, Top>(o, mat, div, gradT, T)
+    (montecarlo/subdomain.h:207-279): the half of the parallelepiped
+    (o, mat) below the diagonal plane through o + col0 and o + col1; the
+    cells are those of the parallelepiped grid."""
+
+    T: tuple = (0.0,) * 5
+    shape_kind = TRIANGULAR_PRISM
+
+    def vol(self) -> float:
+        return float(np.linalg.det(self.M)) / 2.0
+
+
+@dataclass
+class Tetrahedron(Parallelepiped):
+    """Tetrahedron<Bac, Lef, Bot, Dia>(o, mat, div, gradT, T)
+    (montecarlo/subdomain.h:286-358): vertices o, o + col0, o + col1,
+    o + col2."""
+
+    T: tuple = (0.0,) * 4
+    shape_kind = TETRAHEDRON
+
+    def vol(self) -> float:
+        return float(np.linalg.det(self.M)) / 6.0
+
+
+@dataclass
+class Prism:
+    """Prism<Bot, Top, Sid...>(o, mat, div, gradT, T)
+    (montecarlo/subdomain.h:365-503): mat is 3 x N, column 0 the axis and
+    columns 1 .. N-1 the base vertices after o; div < 0 gives no field,
+    otherwise one column for the whole prism."""
+
+    o: np.ndarray
+    mat: np.ndarray
+    div: int
+    gradT: np.ndarray
+    kinds: tuple  # N + 2 face kinds: Bot, Top, sides
+    T: tuple = None
+
+    shape_kind = PRISM
+    _per = 2.0
+
+    def __post_init__(self):
+        if self.T is None:
+            self.T = (0.0,) * len(self.kinds)
+
+    def columns(self) -> np.ndarray:
+        return np.asarray(self.mat, dtype=np.float64)
+
+    def divisions(self) -> np.ndarray:
+        return np.array([self.div, 0, 0], dtype=np.int64)
+
+    def shape(self):
+        return np.zeros(3, dtype=np.int64) if self.div < 0 else np.ones(3, dtype=np.int64)
+
+    def vol(self) -> float:
+        # PrismImpl::volume / PyramidImpl::volume (montecarlo/subdomain.cpp:
+        # 384-392,416-424), summed as the reference sums them
+        m = self.columns()
+        n = m.shape[1]
+        return float(sum(np.dot(np.cross(m[:, i], m[:, i + 1]), m[:, 0]) for i in range(n - 2)) / self._per)
+
+
+@dataclass
+class Pyramid(Prism):
+    """Pyramid<Bot, Sid...>(o, mat, div, gradT, T)
+    (montecarlo/subdomain.h:505-640): column 0 the apex, columns 1 .. N-1
+    the base vertices after o."""
+
+    shape_kind = PYRAMID
+    _per = 6.0
 
 
 @dataclass
@@ -101,15 +192,23 @@ class Domain:
         return int(sum(int(np.prod(p.shape())) for p in self.ppeds))
 
     def cell_volumes(self) -> np.ndarray:
+        """Cell volumes of Parallelepiped-only domains (other shapes: the
+        library's mc_domain_cell_volumes)."""
         out = []
         for p in self.ppeds:
+            if p.shape_kind != PARALLELEPIPED:
+                raise ValueError("cell volumes of this shape come from the library")
             n = int(np.prod(p.shape()))
             if n:
                 out.extend([p.vol() / n] * n)
         return np.array(out)
 
     def max_dim(self) -> float:
-        return max(float(np.linalg.norm(p.M[:, c])) for p in self.ppeds for c in range(3))
+        return max(float(np.linalg.norm(p.columns()[:, c])) for p in self.ppeds
+                   for c in range(p.columns().shape[1]))
+
+    def parallelepipeds_only(self) -> bool:
+        return all(p.shape_kind == PARALLELEPIPED for p in self.ppeds)
 
 
 def _pped(o, dims, div, gradT, kinds, T=(0.0,) * 6):
@@ -235,3 +334,135 @@ class PoreCellDomain(Domain):
                     t[axis] = side
                     pairs.append(Pair(PERI, s, axis, nb(*m), axis + 3, t))
         super().__init__(ppeds, pairs)
+
+
+class PyrDomain(Domain):
+    """Square pyramid with specular walls and a volumetric gradient along
+    its axis: ``Pyramid<Spec, Spec x 4>`` (montecarlo/domain.cpp:299-314,
+    type montecarlo/domain.h:162-165); the CLI uses dim = (height, base,
+    base) and dT = 1e6 * height (montecarlo/main.cpp:330-337)."""
+
+    name = "PyrDomain"
+
+    def __init__(self, dim, dT):
+        dim = np.asarray(dim, dtype=np.float64)
+        self.dim, self.dT = dim, float(dT)
+        mat = np.array([[dim[0], 0.5 * dim[1], 0.5 * dim[2]],
+                        [0.0, dim[1], 0.0],
+                        [0.0, dim[1], dim[2]],
+                        [0.0, 0.0, dim[2]]]).T
+        p = Pyramid(np.zeros(3), mat, 0, np.array([-dT / dim[0], 0.0, 0.0]), (SPEC,) * 5)
+        super().__init__([p], [])
+
+    @classmethod
+    def from_cli(cls, height, base):
+        return cls((height, base, base), 1e6 * height)
+
+
+class HexDomain(Domain):
+    """Hexagonal rod, periodic along its axis with specular sides:
+    ``Prism<PeriP<Polygon<6>>, PeriP<Polygon<6>>, Spec x 6>``
+    (montecarlo/domain.cpp:238-256, type montecarlo/domain.h:139-142); the
+    CLI uses dim = (length, d, d, d) and dT = 1e6 * length
+    (montecarlo/main.cpp:320-328). Eight faces: the oracle takes it, the
+    GPU kernels (at most six faces per subdomain) do not."""
+
+    name = "HexDomain"
+
+    def __init__(self, dim, dT):
+        dim = np.asarray(dim, dtype=np.float64)
+        self.dim, self.dT = dim, float(dT)
+        mat = np.array([[dim[0], 0.0, 0.0],
+                        [0.0, dim[1], -dim[3]],
+                        [0.0, 2.0 * dim[1], 0.0],
+                        [0.0, 2.0 * dim[1], dim[2]],
+                        [0.0, dim[1], dim[2] + dim[3]],
+                        [0.0, 0.0, dim[2]]]).T
+        p = Prism(np.zeros(3), mat, 0, np.array([-dT / dim[0], 0.0, 0.0]), (PERI, PERI) + (SPEC,) * 6)
+        q = Pair(PERI, 0, 0, 0, 1, np.array([dim[0], 0.0, 0.0]))
+        super().__init__([p], [q])
+
+    @classmethod
+    def from_cli(cls, length, d):
+        return cls((length, d, d, d), 1e6 * length)
+
+
+class JctDomain(Domain):
+    """L-junction of three blocks (montecarlo/domain.cpp:353-383, type
+    montecarlo/domain.h:184-190): block 0's Rig face pairs with two Inter
+    faces, so a phonon crossing it goes to the first block that contains
+    it (montecarlo/boundary.cpp:349-359). The GPU kernels take one pair per
+    Inter face; the oracle takes this domain."""
+
+    name = "JctDomain"
+
+    def __init__(self, dim, div, dT):
+        d = np.asarray(dim, dtype=np.float64)
+        v = np.asarray(div, dtype=np.int64)
+        self.dim, self.div, self.dT = d, v, float(dT)
+        g = (-dT / (2.0 * d[0]), 0.0, 0.0)
+        p0 = _pped((0, 0, 0), (2 * d[0], d[1], d[3]), (2 * v[0], v[1], v[3]), g,
+                   (PERI, SPEC, DIFF, PERI, INTER, DIFF))
+        p1 = _pped((0, d[1], 0), (d[0], d[2], d[3]), (v[0], v[2], v[3]), g, (PERI, INTER, DIFF, INTER, SPEC, DIFF))
+        p2 = _pped((d[0], d[1], 0), (d[0], d[2], d[3]), (v[0], v[2], v[3]), g,
+                   (INTER, INTER, DIFF, PERI, SPEC, DIFF))
+        t = np.array([2.0 * d[0], 0.0, 0.0])
+        pairs = [Pair(INTER, 0, RIG, 1, LEF), Pair(INTER, 0, RIG, 2, LEF), Pair(INTER, 1, FRO, 2, BAC),
+                 Pair(PERI, 0, BAC, 0, FRO, t), Pair(PERI, 1, BAC, 2, FRO, t)]
+        super().__init__([p0, p1, p2], pairs)
+
+    @classmethod
+    def from_cli(cls, d0, d3):
+        return cls((d0, d0, d0, d3), (0, 0, 0, 0), 2e6 * d0)
+
+
+class TeeDomain(Domain):
+    """T-junction of four blocks (montecarlo/domain.cpp:430-462, type
+    montecarlo/domain.h:213-220); the CLI uses dim = (d, d, d, d, w),
+    div = (n, n, n, n, 0) and dT = 3e6 * d (montecarlo/main.cpp:350-362)."""
+
+    name = "TeeDomain"
+
+    def __init__(self, dim, div, dT):
+        d = np.asarray(dim, dtype=np.float64)
+        v = np.asarray(div, dtype=np.int64)
+        self.dim, self.div, self.dT = d, v, float(dT)
+        g = (-dT / (2.0 * d[0] + d[1]), 0.0, 0.0)
+        p0 = _pped((0, 0, 0), (d[0], d[2], d[4]), (v[0], v[2], v[4]), g, (PERI, DIFF, SPEC, INTER, DIFF, SPEC))
+        p1 = _pped((d[0], 0, 0), (d[1], d[2], d[4]), (v[1], v[2], v[4]), g, (INTER, SPEC, SPEC, INTER, INTER, SPEC))
+        p2 = _pped((d[0], d[2], 0), (d[1], d[3], d[4]), (v[1], v[3], v[4]), g, (DIFF, INTER, SPEC, DIFF, SPEC, SPEC))
+        p3 = _pped((d[0] + d[1], 0, 0), (d[0], d[2], d[4]), (v[0], v[2], v[4]), g,
+                   (INTER, DIFF, SPEC, PERI, DIFF, SPEC))
+        pairs = [Pair(INTER, 0, FRO, 1, BAC), Pair(INTER, 1, RIG, 2, LEF), Pair(INTER, 1, FRO, 3, BAC),
+                 Pair(PERI, 0, BAC, 3, FRO, np.array([2.0 * d[0] + d[1], 0.0, 0.0]))]
+        super().__init__([p0, p1, p2, p3], pairs)
+
+    @classmethod
+    def from_cli(cls, d0, w, n):
+        return cls((d0, d0, d0, d0, w), (n, n, n, n, 0), 3e6 * d0)
+
+
+class TubeDomain(Domain):
+    """Square tube of three blocks around an open corner, periodic along x
+    (montecarlo/domain.cpp:510-540, type montecarlo/domain.h:262-269); the
+    CLI uses dim = (L, a, a, t), div = (0, n, n, m) and dT = 1e6 * L
+    (montecarlo/main.cpp:364-374)."""
+
+    name = "TubeDomain"
+
+    def __init__(self, dim, div, dT):
+        d = np.asarray(dim, dtype=np.float64)
+        v = np.asarray(div, dtype=np.int64)
+        self.dim, self.div, self.dT = d, v, float(dT)
+        g = (-dT / d[0], 0.0, 0.0)
+        p0 = _pped((0, d[1], 0), (d[0], d[3], d[2]), (v[0], v[3], v[2]), g, (PERI, DIFF, SPEC, PERI, DIFF, INTER))
+        p1 = _pped((0, d[1], d[2]), (d[0], d[3], d[3]), (v[0], v[3], v[3]), g, (PERI, INTER, INTER, PERI, DIFF, DIFF))
+        p2 = _pped((0, 0, d[2]), (d[0], d[1], d[3]), (v[0], v[1], v[3]), g, (PERI, SPEC, DIFF, PERI, INTER, DIFF))
+        t = np.array([d[0], 0.0, 0.0])
+        pairs = [Pair(INTER, 1, LEF, 2, RIG), Pair(INTER, 1, BOT, 0, TOP),
+                 Pair(PERI, 0, BAC, 0, FRO, t), Pair(PERI, 1, BAC, 1, FRO, t), Pair(PERI, 2, BAC, 2, FRO, t)]
+        super().__init__([p0, p1, p2], pairs)
+
+    @classmethod
+    def from_cli(cls, L, a, t, n, m):
+        return cls((L, a, a, t), (0, n, n, m), 1e6 * L)

@@ -83,15 +83,20 @@ class Material:
 
 
 def domain_descs(dom: Domain):
+    """The C-ABI descriptions of a domain: one mc_sdom_desc per subdomain
+    (any shape) and the pair list."""
     n = len(dom.ppeds)
-    ps = (_lib.PpedDesc * n)()
+    ps = (_lib.SdomDesc * n)()
     for i, p in enumerate(dom.ppeds):
+        cols = p.columns()
+        ps[i].shape = int(p.shape_kind)
+        ps[i].ncols = int(cols.shape[1])
         ps[i].o[:] = [float(x) for x in p.o]
-        ps[i].M[:] = [float(x) for x in np.asarray(p.M, dtype=np.float64).reshape(-1)]
-        ps[i].div[:] = [int(x) for x in p.div]
+        ps[i].mat[:cols.size] = [float(x) for x in cols.reshape(-1, order="F")]
+        ps[i].div[:] = [int(x) for x in p.divisions()]
         ps[i].gradT[:] = [float(x) for x in p.gradT]
-        ps[i].kind[:] = [int(k) for k in p.kinds]
-        ps[i].T[:] = [float(t) for t in p.T]
+        ps[i].kind[:len(p.kinds)] = [int(k) for k in p.kinds]
+        ps[i].T[:len(p.T)] = [float(t) for t in p.T]
     m = len(dom.pairs)
     qs = (_lib.PairDesc * max(m, 1))()
     for i, q in enumerate(dom.pairs):
@@ -108,7 +113,7 @@ class DomainHandle:
         L = _lib.lib()
         ps, n, qs, m = domain_descs(dom)
         h = C.c_void_p()
-        _lib.check(L.mc_domain_create(ps, n, qs, m, C.byref(h)))
+        _lib.check(L.mc_domain_create_shapes(ps, n, qs, m, C.byref(h)))
         self.h = h
         self.dom = dom
         self.cols = L.mc_domain_cols(h)

@@ -47,6 +47,7 @@ struct V3 {
     double operator[](int i) const { return v[i]; }
 };
 inline V3 mk(double a, double b, double c) { V3 r; r[0] = a; r[1] = b; r[2] = c; return r; }
+inline V3 z3() { return mk(0., 0., 0.); }
 inline V3 add(const V3& a, const V3& b) { return mk(a[0] + b[0], a[1] + b[1], a[2] + b[2]); }
 inline V3 sub(const V3& a, const V3& b) { return mk(a[0] - b[0], a[1] - b[1], a[2] - b[2]); }
 inline V3 scl(double s, const V3& a) { return mk(a[0] * s, a[1] * s, a[2] * s); }
@@ -316,7 +317,10 @@ bool readNumbers(const char* path, std::vector<double>& out) {
 // ----------------------------------------------------------------- geometry
 struct Face {
     int kind = ORC_SPEC;
+    int shape = 0;     // 0 Parallelogram, 1 Triangle, 2 Polygon
     V3 n, o, si, sj;   // inward normal, face origin, shape vectors
+    std::vector<V3> verts;     // Polygon: the N - 1 vertices relative to o
+    std::vector<double> pcdf;  // Polygon: cumulative triangle areas
     double off = 0.;   // plane offset: signed distance = n.x + off
     double T = 0.;
     double area = 0.;
@@ -330,15 +334,18 @@ struct Face {
 };
 
 struct Sdom {
+    int shapeKind = ORC_PARALLELEPIPED;
     V3 o;
     M3 M, inv;
     long div[3], shape[3], max[3];
     int accum = -1;
     double eps = 0., vol = 0.;
-    Face f[6];
+    std::vector<Face> f;
     V3 gradT;
     M3 rot;
     long colbeg = -1;
+    std::vector<V3> mcol;      // Prism / Pyramid: the N matrix columns
+    std::vector<double> vcdf;  // Prism / Pyramid: volDist cumulative weights
     double emitWeight() const { return 2. * vol * norm(gradT); }
 };
 
@@ -363,7 +370,7 @@ struct orc_domain {
     bool isInside(int s, const V3& x) const {
         // montecarlo/subdomain.cpp:108-116
         const Sdom& d = sd[s];
-        for (int i = 0; i < 6; ++i)
+        for (size_t i = 0; i < d.f.size(); ++i)
             if (dot(d.f[i].n, x) + d.f[i].off < -d.eps) return false;
         return true;
     }
@@ -371,23 +378,71 @@ struct orc_domain {
 
 namespace {
 
-// montecarlo/subdomain.cpp:41-71 and montecarlo/subdomain.h:145-158
-void buildSdom(Sdom& s, const orc_pped& p) {
-    for (int i = 0; i < 3; ++i) s.o[i] = p.o[i];
-    for (int i = 0; i < 9; ++i) s.M.m[i] = p.M[i];
+// Discrete distribution over non-negative weights as its normalised
+// cumulative table (drawn with Dist::pick).
+std::vector<double> cdfOf(const std::vector<double>& w) {
+    std::vector<double> c(w.size());
+    double acc = 0.;
+    for (size_t i = 0; i < w.size(); ++i) { acc += w[i]; c[i] = acc; }
+    for (size_t i = 0; i < w.size(); ++i) c[i] /= acc;
+    return c;
+}
+
+// Boundary(o, shape) (montecarlo/boundary.cpp:50-54) with the shape's
+// normal and area: Parallelogram (montecarlo/boundary.cpp:121-152),
+// Triangle (154-186), Polygon<N> (188-258).
+Face makeFace(int kind, double T, const V3& o, int shape, const V3& si, const V3& sj,
+              const std::vector<V3>& verts = std::vector<V3>()) {
+    Face f;
+    f.kind = kind;
+    f.T = T;
+    f.o = o;
+    f.shape = shape;
+    f.si = si;
+    f.sj = sj;
+    if (shape == 2) {
+        f.verts = verts;
+        std::vector<double> a;
+        // montecarlo/boundary.cpp:199-210: triangles (v_n, v_n+1), n < N - 2
+        for (size_t k = 0; k + 1 < verts.size(); ++k) a.push_back(norm(cross(verts[k], verts[k + 1])) / 2.);
+        double tot = 0.;
+        for (double x : a) tot += x;
+        f.area = tot;
+        f.pcdf = cdfOf(a);
+        f.n = normalized(cross(verts[0], verts[1]));
+    } else {
+        V3 cr = cross(si, sj);
+        f.n = normalized(cr);
+        f.area = shape == 1 ? norm(cr) / 2. : norm(cr);
+    }
+    f.off = -dot(f.n, f.o);
+    M3 r = ident();
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) r(a, b) -= 2. * (f.n[a] * f.n[b]);
+    f.refl = r;
+    f.rot = rotZTo(f.n);
+    f.prot = ident();
+    f.ptransl = mk(0., 0., 0.);
+    return f;
+}
+
+// Subdomain::Subdomain (montecarlo/subdomain.cpp:41-71): inverse, shape,
+// escape tolerance and accumulation flag of (o, mat, div).
+void initSubdomain(Sdom& s, const V3& o, const M3& M, const long div[3]) {
+    s.o = o;
+    s.M = M;
     s.inv = inverse(s.M);
-    s.vol = det(s.M);
     double maxn = 0.;
     for (int c = 0; c < 3; ++c) maxn = std::max(maxn, norm(col(s.M, c)));
     s.eps = 100. * DEPS * maxn;
     bool anyNeg = false;
     long npos = 0;
     for (int i = 0; i < 3; ++i) {
-        s.div[i] = p.div[i];
-        s.shape[i] = std::max(p.div[i], 1L);
+        s.div[i] = div[i];
+        s.shape[i] = std::max(div[i], 1L);
         s.max[i] = s.shape[i] - 1;
-        if (p.div[i] < 0) anyNeg = true;
-        if (p.div[i] > 0) ++npos;
+        if (div[i] < 0) anyNeg = true;
+        if (div[i] > 0) ++npos;
     }
     if (anyNeg) {
         for (int i = 0; i < 3; ++i) { s.shape[i] = 0; s.max[i] = 0; }
@@ -401,29 +456,205 @@ void buildSdom(Sdom& s, const orc_pped& p) {
     } else {
         s.accum = (int)npos + 1;
     }
+}
+
+// Faces of each shape in the reference's bdry<I>() order, and the shape's
+// volume: Parallelepiped (montecarlo/subdomain.h:145-158), TriangularPrism
+// (subdomain.h:224-236), Tetrahedron (subdomain.h:303-314), Prism<N>
+// (subdomain.h:386-410 with InitSidesF 458-475; PrismImpl
+// montecarlo/subdomain.cpp:376-407) and Pyramid<N> (subdomain.h:524-547
+// with InitSidesF 595-613; PyramidImpl subdomain.cpp:409-441). Returns
+// false on an invalid description.
+bool buildShape(Sdom& s, const orc_sdom& p) {
+    const V3 o = mk(p.o[0], p.o[1], p.o[2]);
+    const int N = p.ncols;
+    std::vector<V3> c(N);
+    for (int i = 0; i < N; ++i) c[i] = mk(p.mat[3 * i], p.mat[3 * i + 1], p.mat[3 * i + 2]);
+    auto T = [&](int i) { return p.T[i]; };
+    auto K = [&](int i) { return p.kind[i]; };
+    M3 M;
+    long div[3] = {p.div[0], p.div[1], p.div[2]};
+    s.shapeKind = p.shape;
+    if (p.shape == ORC_PARALLELEPIPED || p.shape == ORC_TRIANGULAR_PRISM || p.shape == ORC_TETRAHEDRON) {
+        if (N != 3) return false;
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) M(r, q) = c[q][r];
+        initSubdomain(s, o, M, div);
+        const double d = det(M);
+        if (p.shape == ORC_PARALLELEPIPED) {
+            s.vol = d;
+            V3 fo[6] = {o, o, o, add(o, c[0]), add(o, c[1]), add(o, c[2])};
+            V3 fi[6] = {c[1], c[2], c[0], c[2], c[0], c[1]};
+            V3 fj[6] = {c[2], c[0], c[1], c[1], c[2], c[0]};
+            for (int k = 0; k < 6; ++k) s.f.push_back(makeFace(K(k), T(k), fo[k], 0, fi[k], fj[k]));
+        } else if (p.shape == ORC_TRIANGULAR_PRISM) {
+            s.vol = d / 2.;
+            s.f.push_back(makeFace(K(0), T(0), o, 0, c[1], c[2]));
+            s.f.push_back(makeFace(K(1), T(1), o, 0, c[2], c[0]));
+            s.f.push_back(makeFace(K(2), T(2), o, 1, c[0], c[1]));
+            s.f.push_back(makeFace(K(3), T(3), add(o, c[0]), 0, c[2], sub(c[1], c[0])));
+            s.f.push_back(makeFace(K(4), T(4), add(o, c[2]), 1, c[1], c[0]));
+        } else {
+            s.vol = d / 6.;
+            s.f.push_back(makeFace(K(0), T(0), o, 1, c[1], c[2]));
+            s.f.push_back(makeFace(K(1), T(1), o, 1, c[2], c[0]));
+            s.f.push_back(makeFace(K(2), T(2), o, 1, c[0], c[1]));
+            s.f.push_back(makeFace(K(3), T(3), add(o, c[0]), 1, sub(c[2], c[0]), sub(c[1], c[0])));
+        }
+    } else if (p.shape == ORC_PRISM || p.shape == ORC_PYRAMID) {
+        if (N < 4 || N > ORC_MAX_COLS) return false;
+        const bool prism = p.shape == ORC_PRISM;
+        // matBase = (col1, col(N-1), col0)
+        for (int r = 0; r < 3; ++r) { M(r, 0) = c[1][r]; M(r, 1) = c[N - 1][r]; M(r, 2) = c[0][r]; }
+        long d1 = p.div[0] < 0 ? -1 : 0;
+        long dv[3] = {d1, d1, d1};
+        initSubdomain(s, o, M, dv);
+        // volume(mat): col(i) x col(i+1) . col(0) for i < N - 2, / 2 or / 6
+        std::vector<double> v(N - 2);
+        double vs = 0.;
+        for (int i = 0; i < N - 2; ++i) {
+            v[i] = dot(cross(c[i], c[i + 1]), c[0]) / (prism ? 2. : 6.);
+            vs += v[i];
+        }
+        s.vol = vs;
+        s.vcdf = cdfOf(v);
+        s.mcol = c;
+        std::vector<V3> bot(c.begin() + 1, c.end());
+        s.f.push_back(makeFace(K(0), T(0), o, 2, z3(), z3(), bot));
+        int base = 1;
+        if (prism) {
+            std::vector<V3> top(bot.rbegin(), bot.rend());
+            s.f.push_back(makeFace(K(1), T(1), add(o, c[0]), 2, z3(), z3(), top));
+            base = 2;
+        }
+        for (int ind = 0; ind < N; ++ind) {
+            V3 pp = ind != 0 ? c[ind] : mk(0., 0., 0.);
+            V3 i = prism ? c[0] : (ind != 0 ? sub(c[0], c[ind]) : c[0]);
+            V3 j = scl(-1., pp);
+            if (ind != N - 1) j = add(j, c[ind + 1]);
+            s.f.push_back(makeFace(K(base + ind), T(base + ind), add(o, pp), prism ? 0 : 1, i, j));
+        }
+    } else {
+        return false;
+    }
+    if (!(s.vol >= DMIN)) return false;
+    for (size_t k = 0; k < s.f.size(); ++k) {
+        const Face& f = s.f[k];
+        if (f.kind < ORC_SPEC || f.kind > ORC_INTER) return false;
+        if ((f.kind == ORC_SPEC || f.kind == ORC_DIFF || f.kind == ORC_INTER) && f.T != 0.) return false;
+    }
     s.gradT = mk(p.gradT[0], p.gradT[1], p.gradT[2]);
     s.rot = rotZTo(normalized(s.gradT));
-    V3 c0 = col(s.M, 0), c1 = col(s.M, 1), c2 = col(s.M, 2);
-    V3 fo[6] = {s.o, s.o, s.o, add(s.o, c0), add(s.o, c1), add(s.o, c2)};
-    V3 fi[6] = {c1, c2, c0, c2, c0, c1};
-    V3 fj[6] = {c2, c0, c1, c1, c2, c0};
-    for (int k = 0; k < 6; ++k) {
-        Face& f = s.f[k];
-        f.kind = p.kind[k];
-        f.o = fo[k]; f.si = fi[k]; f.sj = fj[k];
-        V3 cr = cross(f.si, f.sj);
-        f.n = normalized(cr);
-        f.area = norm(cr);
-        f.off = -dot(f.n, f.o);
-        f.T = p.T[k];
-        M3 r = ident();
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) r(a, b) -= 2. * (f.n[a] * f.n[b]);
-        f.refl = r;
-        f.rot = rotZTo(f.n);
-        f.prot = ident();
-        f.ptransl = mk(0., 0., 0.);
+    return true;
+}
+
+int faceCount(int shape, int ncols) {
+    switch (shape) {
+    case ORC_PARALLELEPIPED: return 6;
+    case ORC_TRIANGULAR_PRISM: return 5;
+    case ORC_TETRAHEDRON: return 4;
+    case ORC_PRISM: return ncols + 2;
+    case ORC_PYRAMID: return ncols + 1;
+    default: return 0;
     }
+}
+
+// TriangularPrismImpl::drawPos (montecarlo/subdomain.cpp:309-319) and
+// TetrahedronImpl::drawPos (subdomain.cpp:348-373) in the unit cell of
+// (o, local); the three uniforms are consumed x, y, z.
+V3 drawTriPrism(Source& g, const V3& o, const M3& L) {
+    double c0 = g.u01(), c1 = g.u01(), c2 = g.u01();
+    if (c0 + c1 > 1.) { c0 = 1. - c0; c1 = 1. - c1; }
+    return add(o, mul(L, mk(c0, c1, c2)));
+}
+V3 drawTetra(Source& g, const V3& o, const M3& L) {
+    double c0 = g.u01(), c1 = g.u01(), c2 = g.u01();
+    if (c0 + c1 > 1.) { c0 = 1. - c0; c1 = 1. - c1; }
+    if (c1 + c2 > 1.) {
+        double tmp = c2;
+        c2 = 1. - c0 - c1;
+        c1 = 1. - tmp;
+    } else if (c0 + c1 + c2 > 1.) {
+        double tmp = c2;
+        c2 = c0 + c1 + c2 - 1.;
+        c0 = 1. - c1 - tmp;
+    }
+    return add(o, mul(L, mk(c0, c1, c2)));
+}
+
+// EmitSubdomain::drawPos of each shape (ParallelepipedImpl
+// montecarlo/subdomain.cpp:275-281; Prism / Pyramid: volDist, then the
+// sub-volume of columns (ind + 1, ind + 2, 0), subdomain.cpp:399-407,
+// 433-441).
+V3 drawVolumePos(const Sdom& s, Source& g) {
+    switch (s.shapeKind) {
+    case ORC_TRIANGULAR_PRISM: return drawTriPrism(g, s.o, s.M);
+    case ORC_TETRAHEDRON: return drawTetra(g, s.o, s.M);
+    case ORC_PRISM:
+    case ORC_PYRAMID: {
+        long ind = Dist::pick(s.vcdf.data(), (long)s.vcdf.size(), g.u01());
+        M3 L;
+        for (int r = 0; r < 3; ++r) { L(r, 0) = s.mcol[ind + 1][r]; L(r, 1) = s.mcol[ind + 2][r]; L(r, 2) = s.mcol[0][r]; }
+        return s.shapeKind == ORC_PRISM ? drawTriPrism(g, s.o, L) : drawTetra(g, s.o, L);
+    }
+    default: {
+        double c0 = g.u01(), c1 = g.u01(), c2 = g.u01();
+        return add(s.o, mul(s.M, mk(c0, c1, c2)));
+    }
+    }
+}
+
+// EmitBoundary::drawPos (montecarlo/boundary.cpp:418-421): the face origin
+// plus the shape's drawPos.
+V3 drawFacePos(const Face& f, Source& g) {
+    if (f.shape == 0) {
+        double r1 = g.u01(), r2 = g.u01();
+        return add(f.o, add(scl(r1, f.si), scl(r2, f.sj)));
+    }
+    V3 i = f.si, j = f.sj;
+    if (f.shape == 2) {
+        long n = Dist::pick(f.pcdf.data(), (long)f.pcdf.size(), g.u01());
+        i = f.verts[n];
+        j = f.verts[n + 1];
+    }
+    double r1 = g.u01(), r2 = g.u01();
+    V3 q = r1 + r2 < 1. ? add(scl(r1, i), scl(r2, j)) : add(scl(1. - r1, i), scl(1. - r2, j));
+    return add(f.o, q);
+}
+
+// Subdomain::cellVol (ParallelepipedImpl montecarlo/subdomain.cpp:269-273,
+// TriangularPrismImpl 283-307, TetrahedronImpl 321-346, PrismImpl and
+// PyramidImpl 394-397,428-431).
+double cellVolume(const Sdom& s, const long idx[3]) {
+    const double sp = (double)(s.shape[0] * s.shape[1] * s.shape[2]);
+    if (s.shapeKind == ORC_PARALLELEPIPED) return s.vol / sp;
+    if (s.shapeKind == ORC_PRISM || s.shapeKind == ORC_PYRAMID) return s.vol;
+    const int dim = s.shapeKind == ORC_TRIANGULAR_PRISM ? 2 : 3;
+    double f0 = 1.;
+    for (int k = 0; k < dim; ++k) f0 -= (double)idx[k] / (double)s.shape[k];
+    if (f0 <= 0.) return 0.;
+    double f1 = f0;
+    for (int k = 0; k < dim; ++k) f1 -= 1. / (double)s.shape[k];
+    if (f1 >= 0.) return s.vol / sp;
+    if (dim == 2) {
+        double frac = std::pow(f0, 2);
+        for (int i = 0; i < 2; ++i) {
+            // corners (1,0), (0,1): sign (-1)^1
+            double f = f0 - 1. / (double)s.shape[i];
+            if (f > 0.) frac += -1. * std::pow(f, 2);
+        }
+        return s.vol * frac / (2. * (double)s.shape[2]);
+    }
+    static const int pts[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 1, 1}, {1, 0, 1}, {1, 1, 0}};
+    double frac = std::pow(f0, 3);
+    for (int i = 0; i < 6; ++i) {
+        int sum = pts[i][0] + pts[i][1] + pts[i][2];
+        double sign = (sum % 2) ? -1. : 1.;
+        double f = f0;
+        for (int k = 0; k < 3; ++k) f -= (double)pts[i][k] / (double)s.shape[k];
+        if (f > 0.) frac += sign * std::pow(f, 3);
+    }
+    return s.vol * frac / 6.;
 }
 
 // ------------------------------------------------------------------ phonon
@@ -599,23 +830,32 @@ void orc_material_tables(const orc_material* m, double* vel, double* tau) {
     std::memcpy(tau, m->tau.data(), sizeof(double) * m->nw * m->np);
 }
 
-orc_domain* orc_domain_create(const orc_pped* s, int ns, const orc_pair* pr,
-                              int npairs) {
+orc_domain* orc_domain_create_shapes(const orc_sdom* s, int ns, const orc_pair* pr, int npairs) {
+    if (!s || ns <= 0) return nullptr;
     orc_domain* D = new orc_domain;
     D->sd.resize(ns);
-    // Parallelepiped construction registers emitting faces whose weight is
-    // nonzero at construction time (montecarlo/subdomain.cpp:205-212)
+    // construction registers the emitting faces whose weight is nonzero at
+    // construction time (montecarlo/subdomain.cpp:205-212)
     std::vector<std::vector<int> > faceEmit(ns);
     for (int i = 0; i < ns; ++i) {
-        buildSdom(D->sd[i], s[i]);
-        for (int k = 0; k < 6; ++k) {
+        if (s[i].ncols > ORC_MAX_COLS || faceCount(s[i].shape, s[i].ncols) > ORC_MAX_FACES ||
+            !buildShape(D->sd[i], s[i])) {
+            delete D;
+            return nullptr;
+        }
+        for (size_t k = 0; k < D->sd[i].f.size(); ++k) {
             const Face& f = D->sd[i].f[k];
             if ((f.kind == ORC_ISOT || f.kind == ORC_PERI) && f.area * std::fabs(f.T) != 0.)
-                faceEmit[i].push_back(k);
+                faceEmit[i].push_back((int)k);
         }
     }
     for (int q = 0; q < npairs; ++q) {
         const orc_pair& p = pr[q];
+        if (p.sdom1 < 0 || p.sdom1 >= ns || p.sdom2 < 0 || p.sdom2 >= ns || p.face1 < 0 ||
+            p.face1 >= (int)D->sd[p.sdom1].f.size() || p.face2 < 0 || p.face2 >= (int)D->sd[p.sdom2].f.size()) {
+            delete D;
+            return nullptr;
+        }
         Face& f1 = D->sd[p.sdom1].f[p.face1];
         Face& f2 = D->sd[p.sdom2].f[p.face2];
         if (p.kind == ORC_PERI) {
@@ -650,6 +890,62 @@ orc_domain* orc_domain_create(const orc_pped* s, int ns, const orc_pair* pr,
     }
     D->cols = cols;
     return D;
+}
+
+orc_domain* orc_domain_create(const orc_pped* s, int ns, const orc_pair* pr, int npairs) {
+    std::vector<orc_sdom> v(ns > 0 ? ns : 0);
+    for (int i = 0; i < ns; ++i) {
+        orc_sdom& d = v[i];
+        std::memset(&d, 0, sizeof(d));
+        d.shape = ORC_PARALLELEPIPED;
+        d.ncols = 3;
+        for (int k = 0; k < 3; ++k) { d.o[k] = s[i].o[k]; d.div[k] = s[i].div[k]; d.gradT[k] = s[i].gradT[k]; }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) d.mat[3 * c + r] = s[i].M[3 * r + c];
+        for (int k = 0; k < 6; ++k) { d.kind[k] = s[i].kind[k]; d.T[k] = s[i].T[k]; }
+    }
+    return orc_domain_create_shapes(v.data(), ns, pr, npairs);
+}
+
+void orc_domain_cell_volumes(const orc_domain* d, double* out) {
+    for (const Sdom& s : d->sd) {
+        if (s.colbeg < 0) continue;
+        long idx[3];
+        for (idx[2] = 0; idx[2] < s.shape[2]; ++idx[2])
+            for (idx[1] = 0; idx[1] < s.shape[1]; ++idx[1])
+                for (idx[0] = 0; idx[0] < s.shape[0]; ++idx[0])
+                    out[s.colbeg + flatIndex(s, idx)] = cellVolume(s, idx);
+    }
+}
+
+double orc_domain_sdom_volume(const orc_domain* d, int s) { return d->sd[s].vol; }
+
+long orc_domain_emitters(const orc_domain* d, double* weights, int* sdom, int* face) {
+    for (size_t i = 0; i < d->em.size(); ++i) {
+        if (weights) weights[i] = d->emitWeight(d->em[i]);
+        if (sdom) sdom[i] = d->em[i].sdom;
+        if (face) face[i] = d->em[i].face;
+    }
+    return (long)d->em.size();
+}
+
+void orc_domain_draw_positions(const orc_domain* d, long e, uint64_t seed, long n, double* out) {
+    const Emitter& E = d->em[e];
+    const Sdom& S = d->sd[E.sdom];
+    for (long i = 0; i < n; ++i) {
+        Source g;
+        g.kind = ORC_RNG_PHILOX;
+        g.key[0] = (uint32_t)seed; g.key[1] = (uint32_t)(seed >> 32);
+        g.id = (uint32_t)i;
+        g.setEvent(0);
+        g.word(); g.word();  // drawFluxProp
+        V3 x = E.face >= 0 ? drawFacePos(S.f[E.face], g) : drawVolumePos(S, g);
+        for (int k = 0; k < 3; ++k) out[3 * i + k] = x[k];
+    }
+}
+
+int orc_domain_is_inside(const orc_domain* d, int s, const double* x) {
+    return d->isInside(s, mk(x[0], x[1], x[2])) ? 1 : 0;
 }
 
 void orc_domain_free(orc_domain* d) { delete d; }
@@ -831,13 +1127,11 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
             bool sign;
             if (E.face >= 0) {
                 const Face& f = S->f[E.face];
-                double r1 = g.u01(), r2 = g.u01();
-                pos = add(f.o, add(scl(r1, f.si), scl(r2, f.sj)));
+                pos = drawFacePos(f, g);
                 dir = mul(f.rot, drawAniso(g, false));
                 sign = f.T >= 0.;
             } else {
-                double c0 = g.u01(), c1 = g.u01(), c2 = g.u01();
-                pos = add(S->o, mul(S->M, mk(c0, c1, c2)));
+                pos = drawVolumePos(*S, g);
                 dir = mul(S->rot, drawAniso(g, true));
                 sign = dot(dir, S->gradT) < 0.;
             }
@@ -855,7 +1149,7 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
                 // Subdomain::advect (montecarlo/subdomain.cpp:161-192)
                 double minD = ph.scatNext;
                 int hit = -1;
-                for (int k = 0; k < 6; ++k) {
+                for (int k = 0; k < (int)S->f.size(); ++k) {
                     const Face& f = S->f[k];
                     double nd = dot(f.n, ph.dir);
                     if (nd >= 0.) continue;
@@ -997,9 +1291,16 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
         const Sdom& s = D.sd[si];
         if (s.colbeg < 0) continue;
         long sp = s.shape[0] * s.shape[1] * s.shape[2];
-        double cv = s.vol / (double)sp;  // montecarlo/subdomain.cpp:269-273
+        std::vector<double> cvs((size_t)sp);
+        {
+            long idx[3];
+            for (idx[2] = 0; idx[2] < s.shape[2]; ++idx[2])
+                for (idx[1] = 0; idx[1] < s.shape[1]; ++idx[1])
+                    for (idx[0] = 0; idx[0] < s.shape[0]; ++idx[0]) cvs[flatIndex(s, idx)] = cellVolume(s, idx);
+        }
         for (long c = s.colbeg; c < s.colbeg + sp; ++c)
             for (long r = 0; r < rows; ++r) {
+                const double cv = cvs[c - s.colbeg];
                 double v = sum[c * rows + r];
                 if (P->problem == ORC_TEMP || P->problem == ORC_CUMTEMP || (P->problem == ORC_MULTI && r == 0))
                     v = v / m.energySum;

@@ -41,11 +41,41 @@ typedef struct {
     double T[6];
 } orc_pped;
 
+/* Subdomain shapes (montecarlo/subdomain.h:128-640). */
+enum {
+    ORC_PARALLELEPIPED = 0,   /* 3 columns, 6 faces Bac Lef Bot Fro Rig Top      */
+    ORC_TRIANGULAR_PRISM = 1, /* 3 columns, 5 faces Bac Lef Bot Dia Top          */
+    ORC_TETRAHEDRON = 2,      /* 3 columns, 4 faces Bac Lef Bot Dia              */
+    ORC_PRISM = 3,            /* N columns (axis, then the base vertices), N + 2
+                                 faces Bot Top Sid0 .. Sid(N-1)                  */
+    ORC_PYRAMID = 4           /* N columns (apex, then the base vertices), N + 1
+                                 faces Bot Sid0 .. Sid(N-1)                      */
+};
+#define ORC_MAX_COLS 9
+#define ORC_MAX_FACES 11
+
+/* One subdomain of any shape: the constructor arguments (o, mat, div,
+ * gradT, T) of Parallelepiped / TriangularPrism / Tetrahedron / Prism<N> /
+ * Pyramid<N> and the kind of each face, in the order of the reference's
+ * bdry<I>(). mat is column-major (column c at mat[3c .. 3c + 2]). Prism and
+ * Pyramid take one division count, div[0] (< 0: no field, else one
+ * column: montecarlo/subdomain.h:386-390,524-530). */
+typedef struct {
+    int shape;
+    int ncols;
+    double o[3];
+    double mat[3 * ORC_MAX_COLS];
+    long div[3];
+    double gradT[3];
+    int kind[ORC_MAX_FACES];
+    double T[ORC_MAX_FACES];
+} orc_sdom;
+
 /* One makePair call (montecarlo/boundary.cpp:361-369 for Inter,
  * montecarlo/boundary.cpp:524-550 for Peri). rot is row-major. */
 typedef struct {
     int kind;          /* ORC_PERI or ORC_INTER */
-    int sdom1, face1;  /* first face: subdomain index, face index 0..5 */
+    int sdom1, face1;  /* first face: subdomain index, face index (bdry<I>()) */
     int sdom2, face2;
     double transl[3];  /* Peri only */
     double rot[9];     /* Peri only, identity when unused */
@@ -127,8 +157,25 @@ void orc_material_tables(const orc_material* m, double* vel, double* tau);
 
 orc_domain* orc_domain_create(const orc_pped* s, int ns, const orc_pair* p,
                               int np);
+/* The same for subdomains of any shape; NULL on an invalid description. */
+orc_domain* orc_domain_create_shapes(const orc_sdom* s, int ns,
+                                     const orc_pair* p, int np);
 void orc_domain_free(orc_domain* d);
 long orc_domain_cols(const orc_domain* d);
+/* Subdomain::cellVol of every field column (cols entries). */
+void orc_domain_cell_volumes(const orc_domain* d, double* out);
+/* Volume of subdomain s (Subdomain::vol) and the emission weight of each
+ * emitter (nemitters entries, volume emitters first per subdomain as
+ * montecarlo/domain.cpp:88-102 registers them); returns the emitter count. */
+double orc_domain_sdom_volume(const orc_domain* d, int s);
+long orc_domain_emitters(const orc_domain* d, double* weights, int* sdom, int* face);
+/* Emitter::drawPos of emitter e from the words of a Philox stream keyed
+ * (seed, id) at event 0: n positions (3 doubles each) for ids 0 .. n-1.
+ * The words consumed are those of emission after drawFluxProp. */
+void orc_domain_draw_positions(const orc_domain* d, long e, uint64_t seed,
+                               long n, double* out);
+/* Subdomain::isInside (montecarlo/subdomain.cpp:108-116). */
+int orc_domain_is_inside(const orc_domain* d, int s, const double* x);
 /* Known-geometry builders restating montecarlo/domain.cpp:137-199. */
 orc_domain* orc_domain_film(double Lx, double Ly, double Lz, long divy,
                             double dT);

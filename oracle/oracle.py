@@ -28,6 +28,11 @@ class Pped(C.Structure):
                 ("gradT", C.c_double * 3), ("kind", C.c_int * 6), ("T", C.c_double * 6)]
 
 
+class SdomS(C.Structure):
+    _fields_ = [("shape", C.c_int), ("ncols", C.c_int), ("o", C.c_double * 3), ("mat", C.c_double * 27),
+                ("div", C.c_long * 3), ("gradT", C.c_double * 3), ("kind", C.c_int * 11), ("T", C.c_double * 11)]
+
+
 class PairS(C.Structure):
     _fields_ = [("kind", C.c_int), ("sdom1", C.c_int), ("face1", C.c_int),
                 ("sdom2", C.c_int), ("face2", C.c_int), ("transl", C.c_double * 3),
@@ -84,6 +89,16 @@ def lib():
         L.orc_material_tables.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.orc_domain_create.restype = C.c_void_p
         L.orc_domain_create.argtypes = [P(Pped), C.c_int, P(PairS), C.c_int]
+        L.orc_domain_create_shapes.restype = C.c_void_p
+        L.orc_domain_create_shapes.argtypes = [P(SdomS), C.c_int, P(PairS), C.c_int]
+        L.orc_domain_cell_volumes.argtypes = [C.c_void_p, P(C.c_double)]
+        L.orc_domain_sdom_volume.restype = C.c_double
+        L.orc_domain_sdom_volume.argtypes = [C.c_void_p, C.c_int]
+        L.orc_domain_emitters.restype = C.c_long
+        L.orc_domain_emitters.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int), P(C.c_int)]
+        L.orc_domain_draw_positions.argtypes = [C.c_void_p, C.c_long, C.c_uint64, C.c_long, P(C.c_double)]
+        L.orc_domain_is_inside.restype = C.c_int
+        L.orc_domain_is_inside.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
         L.orc_domain_film.restype = C.c_void_p
         L.orc_domain_film.argtypes = [C.c_double, C.c_double, C.c_double, C.c_long, C.c_double]
         L.orc_domain_bulk.restype = C.c_void_p
@@ -141,16 +156,20 @@ class OMaterial:
 
 
 def domain_structs(dom):
-    """Pack a montecarlocpp_gb300.domains.Domain description."""
+    """Pack a montecarlocpp_gb300.domains.Domain description (subdomains of
+    any shape) for orc_domain_create_shapes."""
     n = len(dom.ppeds)
-    ps = (Pped * n)()
+    ps = (SdomS * n)()
     for i, p in enumerate(dom.ppeds):
+        cols = np.asarray(p.columns(), dtype=np.float64)
+        ps[i].shape = int(p.shape_kind)
+        ps[i].ncols = int(cols.shape[1])
         ps[i].o[:] = [float(x) for x in p.o]
-        ps[i].M[:] = [float(x) for x in np.asarray(p.M).reshape(-1)]
-        ps[i].div[:] = [int(x) for x in p.div]
+        ps[i].mat[:cols.size] = [float(x) for x in cols.reshape(-1, order="F")]
+        ps[i].div[:] = [int(x) for x in p.divisions()]
         ps[i].gradT[:] = [float(x) for x in p.gradT]
-        ps[i].kind[:] = [int(k) for k in p.kinds]
-        ps[i].T[:] = [float(t) for t in p.T]
+        ps[i].kind[:len(p.kinds)] = [int(k) for k in p.kinds]
+        ps[i].T[:len(p.T)] = [float(t) for t in p.T]
     m = len(dom.pairs)
     qs = (PairS * max(m, 1))()
     for i, q in enumerate(dom.pairs):
@@ -167,7 +186,9 @@ class ODomain:
             self.h = handle
         else:
             ps, n, qs, m = domain_structs(dom)
-            self.h = L.orc_domain_create(ps, n, qs, m)
+            self.h = L.orc_domain_create_shapes(ps, n, qs, m)
+            if not self.h:
+                raise ValueError("oracle domain construction failed")
         self.cols = L.orc_domain_cols(self.h)
 
     @classmethod
@@ -177,6 +198,30 @@ class ODomain:
     @classmethod
     def bulk(cls, L, divx, dT):
         return cls(handle=lib().orc_domain_bulk(L, divx, dT))
+
+    def cell_volumes(self):
+        out = np.zeros(self.cols)
+        lib().orc_domain_cell_volumes(self.h, _dp(out))
+        return out
+
+    def sdom_volume(self, s):
+        return lib().orc_domain_sdom_volume(self.h, s)
+
+    def emitters(self):
+        n = lib().orc_domain_emitters(self.h, None, None, None)
+        w = np.zeros(n)
+        sd = (C.c_int * max(n, 1))()
+        fc = (C.c_int * max(n, 1))()
+        lib().orc_domain_emitters(self.h, _dp(w), sd, fc)
+        return w, list(sd[:n]), list(fc[:n])
+
+    def draw_positions(self, e, seed, n):
+        out = np.zeros((n, 3))
+        lib().orc_domain_draw_positions(self.h, e, seed, n, _dp(out))
+        return out
+
+    def is_inside(self, s, x):
+        return bool(lib().orc_domain_is_inside(self.h, s, _dp(np.ascontiguousarray(x, dtype=np.float64))))
 
     def accumulate(self, sdom, bpos, epos, amount, data):
         amount = np.ascontiguousarray(amount, dtype=np.float64)

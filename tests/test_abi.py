@@ -73,7 +73,16 @@ def test_domain_validation():
                          (M.PERI, M.SPEC, M.SPEC, M.PERI, M.SPEC, M.SPEC))
     ps, n, qs, m = M.problem.domain_descs(type("D", (), {"ppeds": [p], "pairs": []})())
     h = C.c_void_p()
-    assert _lib.lib().mc_domain_create(ps, n, qs, 0, C.byref(h)) == -1
+    assert _lib.lib().mc_domain_create_shapes(ps, n, qs, 0, C.byref(h)) == -1
+    # the same through the Parallelepiped entry point
+    pp = (_lib.PpedDesc * 1)()
+    pp[0].M[:] = [1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0]
+    pp[0].kind[:] = [M.PERI, M.SPEC, M.SPEC, M.PERI, M.SPEC, M.SPEC]
+    assert _lib.lib().mc_domain_create(pp, 1, qs, 0, C.byref(h)) == -1
+    pp[0].kind[:] = [M.SPEC] * 6
+    assert _lib.lib().mc_domain_create(pp, 1, qs, 0, C.byref(h)) == 0
+    assert _lib.lib().mc_domain_cols(h) == 1
+    _lib.lib().mc_domain_destroy(h)
     # more cells than the packed cell index holds
     big = M.FilmDomain.from_cli(1e-7, 1e-7, 600)
     with pytest.raises(_lib.McError) as e:

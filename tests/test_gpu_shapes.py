@@ -1,0 +1,98 @@
+"""GPU parity on subdomains other than the Parallelepiped and on the
+reference's Pyr, Tee and Tube domains: the sm_103a kernels through the C
+ABI against the CPU oracle on the same Philox streams.
+
+Tolerances: FP64 flight -- every trajectory's discrete fields identical,
+positions within 1e-9 of the domain size and event times within 1e-9
+relative, the field within 1e-9 of each row's largest magnitude; FP32
+flight -- discrete fields identical but for one trajectory, positions
+within 1e-4 of the domain size for 99 % of the events and 1e-2 for all, the
+field within 1e-2 (an FP32 face distance from frame coordinates carries
+~6e-8 of the domain size, which grazing flights enlarge; the
+Tetrahedron's cut cells, some with a thousandth of a full cell's volume,
+turn one diverged trajectory into 5.5e-3 of the row's largest density). (The kernels measure a general face's distance in the
+subdomain's frame coordinates and the oracle in physical ones: the two
+FP64 roundings differ by ~1e-23 m, which a nearly grazing flight turns
+into ~1e-11 of the domain size along the face; measured worst 2.5e-11.)
+Cells of zero volume (outside a Tetrahedron or TriangularPrism) are NaN
+in both, as the reference's division makes them."""
+
+import numpy as np
+import pytest
+
+import montecarlocpp_gb300 as M
+from oracle import oracle as O
+
+import shape_cases as SC
+from test_gpu_parity import compare_logs
+
+pytestmark = pytest.mark.gpu
+
+PROBLEM = {M.TEMP: M.TempProblem, M.FLUX: M.FluxProblem, M.MULTI: M.MultiProblem}
+CASES = SC.cases()
+
+
+def field_err_nan(a, b):
+    na, nb = np.isnan(a), np.isnan(b)
+    assert np.array_equal(na, nb)
+    a = np.where(na, 0.0, a)
+    b = np.where(nb, 0.0, b)
+    scale = np.abs(a).max(axis=1, keepdims=True)
+    scale[scale == 0] = 1
+    return float((np.abs(a - b) / scale).max())
+
+
+def run(gmat, omat, name, prec, K, seed=7, **kw):
+    dom, kind, nemit, dt, nsteps = CASES[name]
+    od = O.ODomain(dom)
+    o_out, o_st, ex = O.solve(omat, od, kind, nemit=nemit, maxscat=10**6, dt=dt, horizon=dt * nsteps,
+                              rng=O.RNG_PHILOX, seed=seed, log_cap=256, log_phonons=96)
+    P = PROBLEM[kind](gmat, dom, nemit, 10**6)
+    g_out = P.solve(dt=dt, nsteps=nsteps, seed=seed, precision=prec, steps_per_launch=K, log_cap=256,
+                    log_phonons=96, **kw)
+    return dom, (o_out, o_st, ex["log"]), (g_out, P.stats, P.log)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("K", [1, 100000])
+def test_fp64_trajectories_and_field(name, K, gmat, omat):
+    dom, (oo, ost, olog), (go, gst, glog) = run(gmat, omat, name, 64, K)
+    for k in ("nemit", "events", "scatters", "absorbed", "escapes", "horizon_stops", "phonon_steps"):
+        assert gst[k] == ost[k], k
+    compare_logs(olog, glog, dom.max_dim(), 1e-9)
+    (a_rec, a_cnt), (b_rec, b_cnt) = olog, glog
+    worst = 0.0
+    for i in range(min(len(a_cnt), len(b_cnt))):
+        n = int(min(a_cnt[i], b_cnt[i], a_rec.shape[1]))
+        t0, t1 = a_rec[i, :n, 8], b_rec[i, :n, 8]
+        if n:
+            worst = max(worst, float((np.abs(t0 - t1) / np.abs(t0)).max()))
+    assert worst < 1e-9, worst
+    assert field_err_nan(oo, go) < 1e-9
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp32_trajectories_and_field(name, gmat, omat):
+    dom, (oo, ost, olog), (go, gst, glog) = run(gmat, omat, name, 32, 50)
+    compare_logs(olog, glog, dom.max_dim(), 1e-4, allow_mismatch=1, pos_quantile=0.99, pos_cap=1e-2)
+    assert field_err_nan(oo, go) < 1e-2
+
+
+def test_batch_of_shapes_equals_single_solves_fp64(gmat):
+    """The batched kernel over instances of different shapes (one launch)
+    gives each instance's single-instance result."""
+    names = ["wedge", "tet", "prism4", "pyr5"]
+    probs, seeds = [], []
+    for i, n in enumerate(names):
+        dom, kind, nemit, dt, nsteps = CASES[n]
+        probs.append(PROBLEM[kind](gmat, dom, nemit, 10**6))
+        seeds.append(30 + i)
+    dt, nsteps = 0.5e-12, 300
+    B = M.Batch(probs, dt=dt, nsteps=nsteps, seeds=seeds, precision=64, use_graph=False)
+    B.run()
+    for i, (p, s) in enumerate(zip(probs, seeds)):
+        got, st = B.result(i)
+        ref = p.solve(dt=dt, nsteps=nsteps, precision=64, seed=s, steps_per_launch=nsteps)
+        assert st["nemit"] == p.stats["nemit"]
+        assert field_err_nan(ref, got) < 1e-9, names[i]
+    B.close()
