@@ -89,7 +89,7 @@ typedef struct {
 
 /* Domain assembly (montecarlo/domain.cpp:88-102 addSdom and the
  * init() of each domain). Limits: <= 32 subdomains, <= 512 cells per axis
- * per subdomain, one pair per Inter face. */
+ * per subdomain. */
 int mc_domain_create(const mc_pped_desc* ppeds, int n, const mc_pair_desc* pairs, int npairs,
                      mc_domain_h* out);
 
@@ -112,9 +112,11 @@ enum {
  * 524-547) and each face's kind, in bdry<I>() order. mat is column-major:
  * column c at mat[3c .. 3c + 2]. Prism and Pyramid take one division
  * count, div[0]: < 0 no field, else one column for the whole subdomain.
- * The GPU kernels take subdomains of at most 6 faces (Prism<N <= 4>,
- * Pyramid<N <= 5>), Peri faces off the parallelepiped frame only with the
- * identity rotation; MC_ERR_UNSUPPORTED otherwise. */
+ * A subdomain takes one device slot, two when it has more than 6 faces or
+ * an Inter face paired more than once (at most 32 slots, at most 6 faces
+ * plus pair candidates beyond the first 6 faces). Peri faces of the other
+ * shapes take the identity rotation only, and an Inter face paired more
+ * than once pairs with Parallelepipeds only; MC_ERR_UNSUPPORTED otherwise. */
 typedef struct {
     int shape;
     int ncols;

@@ -259,7 +259,7 @@ struct HostFace {
     int pairS = -1, pairF = -1;
     M3 R = eye();
     V3 t = mk(0, 0, 0);
-    int ninter = 0;
+    std::vector<std::pair<int, int>> inter;  // Inter pairs (subdomain, face) in makePair order
 };
 
 V3 addv(const V3& a, const V3& b) { return mk(a[0] + b[0], a[1] + b[1], a[2] + b[2]); }
@@ -471,6 +471,9 @@ void setThresholds(EmitterD& E, const std::vector<double>& w) {
 
 struct mc_domain_s {
     std::vector<mc_sdom_desc> desc;
+    std::vector<int> slot;                // device slot of each subdomain
+    std::vector<int> refOfSlot;           // subdomain of each slot (-1: a continuation)
+    bool needGen = false;                 // other shapes, continuations or several Inter pairs
     std::vector<EmitterD> em;
     std::vector<double> emWeight;
     std::vector<long> colbeg;
@@ -491,8 +494,6 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
     std::vector<std::vector<int>> faceEmit(n);
     for (int s = 0; s < n; ++s) {
         if (int rc = buildShape(ps[s], H[s])) return rc;
-        if ((int)H[s].f.size() > MAX_FACES)
-            return fail(MC_ERR_UNSUPPORTED, "the GPU kernels take subdomains of at most 6 faces");
         for (int k = 0; k < 3; ++k)
             if (H[s].div[k] >= MAX_SHAPE) return fail(MC_ERR_UNSUPPORTED, "more than 511 cells along an axis");
         // construction registers the emitting faces whose weight is nonzero
@@ -523,10 +524,10 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             a.pairS = P.sdom2; a.pairF = P.face2;
             b.pairS = P.sdom1; b.pairF = P.face1;
         } else if (P.kind == MC_INTER) {
-            if (a.ninter > 0 || b.ninter > 0) return fail(MC_ERR_UNSUPPORTED, "more than one pair on an Inter face");
-            a.ninter++; b.ninter++;
-            a.pairS = P.sdom2; a.pairF = P.face2;
-            b.pairS = P.sdom1; b.pairF = P.face1;
+            a.inter.push_back(std::make_pair(P.sdom2, P.face2));
+            b.inter.push_back(std::make_pair(P.sdom1, P.face1));
+            if (a.pairS < 0) { a.pairS = P.sdom2; a.pairF = P.face2; }
+            if (b.pairS < 0) { b.pairS = P.sdom1; b.pairF = P.face1; }
         } else {
             return fail(MC_ERR_ARG, "pair kind must be Peri or Inter");
         }
@@ -535,13 +536,43 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         for (const HostFace& F : H[s].f)
             if ((F.kind == MC_PERI || F.kind == MC_INTER) && F.pairS < 0)
                 return fail(MC_ERR_ARG, "Domain setup not complete: unpaired face");
+    // device slots: a subdomain with more than MAX_FACES faces, or with
+    // Inter faces paired more than once, also takes a continuation slot
+    std::vector<int> extraFaces(n, 0), cand(n, 0);
+    int nslot = 0;
+    D->slot.resize(n);
+    for (int s = 0; s < n; ++s) {
+        extraFaces[s] = std::max(0, (int)H[s].f.size() - MAX_FACES);
+        for (const HostFace& F : H[s].f)
+            if (F.inter.size() > 1) cand[s] += (int)F.inter.size();
+        if (extraFaces[s] + cand[s] > MAX_FACES)
+            return fail(MC_ERR_UNSUPPORTED, "too many faces and Inter pairs for one subdomain");
+        D->slot[s] = nslot;
+        D->refOfSlot.push_back(s);
+        ++nslot;
+        if (extraFaces[s] + cand[s] > 0) { D->refOfSlot.push_back(-1); ++nslot; }
+        if (H[s].shape != MC_PARALLELEPIPED || extraFaces[s] + cand[s] > 0) D->needGen = true;
+    }
+    if (nslot > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 32 subdomain slots");
+    for (int s = 0; s < n; ++s)
+        for (const HostFace& F : H[s].f)
+            if (F.inter.size() > 1)
+                for (const auto& q : F.inter)
+                    if (H[q.first].shape != MC_PARALLELEPIPED)
+                        return fail(MC_ERR_UNSUPPORTED, "several Inter pairs into a non-Parallelepiped subdomain");
+    D->sd.assign(nslot, SdomD<double>());
+    for (SdomD<double>& x : D->sd) {
+        std::memset(&x, 0, sizeof(x));
+        x.colbeg = -1;
+        x.accum = -2;
+    }
     // subdomain images, emitters and columns
     long cols = 0;
     for (int s = 0; s < n; ++s) {
         const mc_sdom_desc& p = ps[s];
         const HostSdom& h = H[s];
         const bool gen = h.shape != MC_PARALLELEPIPED;
-        SdomD<double>& S = D->sd[s];
+        SdomD<double>& S = D->sd[D->slot[s]];
         std::memset(&S, 0, sizeof(S));
         M3 Mi = inv3(h.FM);
         std::memcpy(S.M, h.FM.m, sizeof(S.M));
@@ -583,7 +614,7 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         if (vw != 0.) {
             EmitterD E;
             std::memset(&E, 0, sizeof(E));
-            E.sdom = s; E.face = -1; E.fold = -1; E.ncoord = 3; E.npiece = 1;
+            E.sdom = D->slot[s]; E.face = -1; E.fold = -1; E.ncoord = 3; E.npiece = 1;
             if (gen) {
                 const std::vector<V3>& c = h.col;
                 if (h.shape == MC_PRISM || h.shape == MC_PYRAMID) {
@@ -605,7 +636,7 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             const HostFace& F = h.f[f];
             EmitterD E;
             std::memset(&E, 0, sizeof(E));
-            E.sdom = s; E.face = f; E.fold = -1; E.ncoord = 2; E.npiece = 1;
+            E.sdom = D->slot[s]; E.face = f; E.fold = -1; E.ncoord = 2; E.npiece = 1;
             if (gen) {
                 const V3 z = mk(0, 0, 0);
                 if (F.shape == 2) {
@@ -635,13 +666,52 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
     }
     D->cols = cols;
     // faces: normals, rotations, planes, pair maps in frame coordinates
+    auto faceAt = [&](int s, int f) -> FaceD<double>& {
+        SdomD<double>* S = &D->sd[D->slot[s]];
+        return f < MAX_FACES ? S->f[f] : S[1].f[f - MAX_FACES];
+    };
+    // pair map of face f of subdomain s into face tf of subdomain ts:
+    // u' = diag(S') Minv' (R (o + M diag(1/S) u) + t - o')
+    auto setMap = [&](FaceD<double>& G, int s, int f, const M3& R, const V3& tr, int ts, int tf) {
+        const SdomD<double>& S = D->sd[D->slot[s]];
+        const SdomD<double>& T2 = D->sd[D->slot[ts]];
+        G.to = D->slot[ts];
+        G.toface = T2.gen ? -1 : tf;
+        bool id = true;
+        for (int i = 0; i < 9; ++i) if (R.m[i] != eye().m[i]) id = false;
+        G.ident = id ? 1 : 0;
+        if (!S.gen) std::memcpy(G.Rd, R.m, sizeof(R.m));
+        M3 Mi2; std::memcpy(Mi2.m, T2.Minv, sizeof(Mi2.m));
+        M3 M1; std::memcpy(M1.m, S.M, sizeof(M1.m));
+        M3 A = mmul(mmul(Mi2, R), M1);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) A.m[3 * i + j] = A.m[3 * i + j] * T2.S[i] / S.S[j];
+        V3 Ro = mvec(R, mk(S.o[0], S.o[1], S.o[2]));
+        V3 x0 = mk(Ro[0] + tr[0] - T2.o[0], Ro[1] + tr[1] - T2.o[1], Ro[2] + tr[2] - T2.o[2]);
+        V3 b = mvec(Mi2, x0);
+        std::memcpy(G.A, A.m, sizeof(A.m));
+        for (int k = 0; k < 3; ++k) G.b[k] = T2.S[k] * b[k];
+        // tangential identity: same axis, A = I and no tangential shift
+        // (within rounding of the FP64 products)
+        const int ax = f % 3;
+        bool tang = !S.gen && !T2.gen && f < 6 && (tf % 3) == ax;
+        for (int i = 0; i < 3 && tang; ++i) {
+            if (i == ax) continue;  // the normal coordinate is snapped
+            for (int j = 0; j < 3; ++j)
+                if (std::fabs(A.m[3 * i + j] - (i == j ? 1. : 0.)) > 1e-12) tang = false;
+        }
+        for (int k = 0; k < 3 && tang; ++k)
+            if (k != ax && std::fabs(G.b[k]) > 1e-12 * T2.S[k]) tang = false;
+        G.tang = tang ? 1 : 0;
+    };
     for (int s = 0; s < n; ++s) {
-        SdomD<double>& S = D->sd[s];
+        SdomD<double>& S = D->sd[D->slot[s]];
+        int nextCand = extraFaces[s];
         for (int f = 0; f < S.nface; ++f) {
             const HostFace& F = H[s].f[f];
-            FaceD<double>& G = S.f[f];
+            FaceD<double>& G = faceAt(s, f);
             G.kind = F.kind;
-            G.to = -1; G.toface = -1; G.ident = 1;
+            G.to = -1; G.toface = -1; G.ident = 1; G.more = 0;
             for (int k = 0; k < 3; ++k) G.n[k] = F.n[k];
             M3 r = rotZTo(F.n);
             std::memcpy(G.rot, r.m, sizeof(r.m));
@@ -657,41 +727,31 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
                 for (int k = 0; k < 3; ++k) G.gp[k] = g[k] / S.S[k];
                 G.gp[3] = dot(F.n, subv(mk(S.o[0], S.o[1], S.o[2]), F.o));
             }
-            if (F.kind == MC_PERI || F.kind == MC_INTER) {
-                const int t = F.pairS;
-                const SdomD<double>& T2 = D->sd[t];
-                G.to = t;
-                G.toface = T2.gen ? -1 : F.pairF;
-                M3 R = F.kind == MC_PERI ? F.R : eye();
-                V3 tr = F.kind == MC_PERI ? F.t : mk(0, 0, 0);
+            if (F.kind == MC_PERI) {
                 bool id = true;
-                for (int i = 0; i < 9; ++i) if (R.m[i] != eye().m[i]) id = false;
+                for (int i = 0; i < 9; ++i) if (F.R.m[i] != eye().m[i]) id = false;
                 if (S.gen && !id) return fail(MC_ERR_UNSUPPORTED, "Peri rotation on a non-Parallelepiped face");
-                G.ident = id ? 1 : 0;
-                if (!S.gen) std::memcpy(G.Rd, R.m, sizeof(R.m));
-                // u' = diag(S') Minv' (R (o + M diag(1/S) u) + t - o')
-                M3 Mi2; std::memcpy(Mi2.m, T2.Minv, sizeof(Mi2.m));
-                M3 M1; std::memcpy(M1.m, S.M, sizeof(M1.m));
-                M3 A = mmul(mmul(Mi2, R), M1);
-                for (int i = 0; i < 3; ++i)
-                    for (int j = 0; j < 3; ++j) A.m[3 * i + j] = A.m[3 * i + j] * T2.S[i] / S.S[j];
-                V3 Ro = mvec(R, mk(S.o[0], S.o[1], S.o[2]));
-                V3 x0 = mk(Ro[0] + tr[0] - T2.o[0], Ro[1] + tr[1] - T2.o[1], Ro[2] + tr[2] - T2.o[2]);
-                V3 b = mvec(Mi2, x0);
-                std::memcpy(G.A, A.m, sizeof(A.m));
-                for (int k = 0; k < 3; ++k) G.b[k] = T2.S[k] * b[k];
-                // tangential identity: same axis, A = I and no tangential
-                // shift (within rounding of the FP64 products)
-                const int ax = f % 3;
-                bool tang = !S.gen && !T2.gen && (F.pairF % 3) == ax;
-                for (int i = 0; i < 3 && tang; ++i) {
-                    if (i == ax) continue;  // the normal coordinate is snapped
-                    for (int j = 0; j < 3; ++j)
-                        if (std::fabs(A.m[3 * i + j] - (i == j ? 1. : 0.)) > 1e-12) tang = false;
+                setMap(G, s, f, F.R, F.t, F.pairS, F.pairF);
+            } else if (F.kind == MC_INTER && F.inter.size() == 1) {
+                setMap(G, s, f, eye(), mk(0, 0, 0), F.pairS, F.pairF);
+            } else if (F.kind == MC_INTER) {
+                // several pairs: the first whose subdomain holds the position
+                // (montecarlo/boundary.cpp:349-359); the candidates go to the
+                // continuation slot, each with S_k / height_k of its target
+                G.more = ((int)F.inter.size() << 8) | nextCand;
+                for (const auto& q : F.inter) {
+                    FaceD<double>& C = D->sd[D->slot[s] + 1].f[nextCand++];
+                    std::memset(&C, 0, sizeof(C));
+                    C.kind = MC_INTER;
+                    setMap(C, s, f, eye(), mk(0, 0, 0), q.first, q.second);
+                    const HostSdom& th = H[q.first];
+                    const SdomD<double>& T2 = D->sd[D->slot[q.first]];
+                    const double vol = std::fabs(det3(th.M));
+                    for (int k = 0; k < 3; ++k) {
+                        V3 cr = cross(colOf(th.M, (k + 1) % 3), colOf(th.M, (k + 2) % 3));
+                        C.n[k] = T2.S[k] / (vol / std::sqrt(dot(cr, cr)));
+                    }
                 }
-                for (int k = 0; k < 3 && tang; ++k)
-                    if (k != ax && std::fabs(G.b[k]) > 1e-12 * T2.S[k]) tang = false;
-                G.tang = tang ? 1 : 0;
             }
         }
     }
@@ -778,7 +838,7 @@ void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
     for (int f = 0; f < MAX_FACES; ++f) {
         const FaceD<double>& x = a.f[f];
         FaceD<R>& y = b.f[f];
-        y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident; y.tang = x.tang;
+        y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident; y.tang = x.tang; y.more = x.more;
         for (int i = 0; i < 3; ++i) { y.n[i] = (R)x.n[i]; y.b[i] = (R)x.b[i]; }
         for (int i = 0; i < 9; ++i) { y.rot[i] = (R)x.rot[i]; y.Rd[i] = (R)x.Rd[i]; y.A[i] = (R)x.A[i]; }
         y.T = (R)x.T;
@@ -988,13 +1048,12 @@ int setupSession(mc_session_s* S) {
     // static schedule with a shared 1-D field along one axis in every
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
-    S->gen = false;
-    for (const auto& x : D.sd) S->gen = S->gen || x.gen;
+    S->gen = D.needGen;
     if (S->gen && S->replay) return fail(MC_ERR_UNSUPPORTED, "replay streams take Parallelepiped domains only");
     if (!S->dyn && !S->replay && !S->logging && S->tm == TM_SHARED) {
         const int k = D.sd[0].accum;
         bool same = k >= 0 && k <= 2;
-        for (const auto& x : D.sd) same = same && x.accum == k && !x.gen;
+        for (const auto& x : D.sd) same = same && x.accum == k && !D.needGen;
         if (same) S->lean = k;
     }
     int occ = S->lean >= 0 ? advanceLeanOccupancy<R>(S->lean, S->block, S->smem)
@@ -1173,6 +1232,15 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
         CK(cudaMemcpy(S->desc.log, S->log_d, sizeof(double) * 12 * (size_t)ln * S->desc.log_cap, cudaMemcpyDeviceToHost));
         if (ln) CK(cudaMemcpy(lc.data(), S->logcnt_d, sizeof(int) * ln, cudaMemcpyDeviceToHost));
         for (long long i = 0; i < ln; ++i) S->desc.log_counts[i] = lc[i];
+        // device slots -> the caller's subdomain indices
+        const std::vector<int>& ref = S->dom->refOfSlot;
+        for (size_t q = 0; q < (size_t)ln * S->desc.log_cap; ++q) {
+            double* r = S->desc.log + 12 * q;
+            for (int k : {1, 3}) {
+                const double v = r[k];
+                if (v >= 0. && v < (double)ref.size()) r[k] = (double)ref[(size_t)v];
+            }
+        }
     }
     if (st) {
         std::memset(st, 0, sizeof(*st));
@@ -1464,8 +1532,7 @@ int setupBatch(mc_batch_s* B) {
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     B->tm = batchFieldMode<R>(inst);
     B->gen = false;
-    for (int i = 0; i < n; ++i)
-        for (const auto& x : B->doms[i]->sd) B->gen = B->gen || x.gen;
+    for (int i = 0; i < n; ++i) B->gen = B->gen || B->doms[i]->needGen;
     const int occ = advanceBatchOccupancy<R>(B->tm, B->gen, batchSmemBytes<R>(P), B->block);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
     B->grid = B->bd.grid_blocks > 0 ? B->bd.grid_blocks : occ * nsm;
@@ -1797,8 +1864,7 @@ struct ServerT : ServerBase {
         }
         const int tm = batchFieldMode<R>(inst);
         bool gen = false;
-        for (SrvJob* j : run)
-            for (const auto& x : j->req.dom->sd) gen = gen || x.gen;
+        for (SrvJob* j : run) gen = gen || j->req.dom->needGen;
         const int occ = advanceBatchOccupancy<R>(tm, gen, batchSmemBytes<R>(P), block);
         if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
         const int grid = std::min(occ, 64) * nsm;
@@ -2162,8 +2228,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    bool gen = false;
-    for (const auto& x : D.sd) gen = gen || x.gen;
+    const bool gen = D.needGen;
     S->gen = gen;
     const int occ = advanceOccupancy<R>(true, false, false, S->tm, gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");

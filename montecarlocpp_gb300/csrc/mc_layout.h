@@ -55,6 +55,12 @@ enum Status {
 // the other shapes (SdomD::gen) are planes in the subdomain's frame
 // coordinates: gp[0..2] . u + gp[3] is the signed distance from the face,
 // kept in place of Rd (such faces take Peri pairs without rotation only).
+//
+// An Inter face paired with several others (montecarlo/boundary.cpp:349-359)
+// keeps its candidates as entries of its subdomain's continuation slot:
+// more = count << 8 | first entry; each candidate entry holds the pair map
+// (to, toface, tang, A, b) and, in n[k], the factor that turns the target's
+// escape tolerance into frame units along axis k (S_k / height_k).
 template <typename R>
 struct FaceD {
     int kind;
@@ -62,7 +68,7 @@ struct FaceD {
     int toface;   // axis face of `to` the phonon arrives on, -1 for none
     int ident;    // 1 if the Peri rotation is the identity
     int tang;     // 1 if the map keeps the tangential cell coordinates
-    int pad;
+    int more;     // Inter candidates in the continuation slot (see above), 0 for one pair
     R n[3];       // inward unit normal (Spec reflection)
     R rot[9];     // rotation z-hat -> n, row-major (Diff, Isot emission)
     union {
@@ -74,7 +80,10 @@ struct FaceD {
     R T;          // emission temperature after pairing (Isot / Peri)
 };
 
-// Largest face count of a subdomain on the device.
+// Faces a subdomain slot holds. A subdomain with more faces, or with Inter
+// faces paired several times, also takes the next slot (its continuation):
+// faces MAX_FACES .. nface - 1 are the continuation's f[0 ..], followed by
+// the Inter candidates.
 constexpr int MAX_FACES = 6;
 
 template <typename R>

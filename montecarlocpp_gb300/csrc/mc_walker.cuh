@@ -763,6 +763,12 @@ __host__ __device__ inline void setWindow(Params<R>& P) {
     P.wNext = (R)(P.ksteps < after ? P.ksteps : after) * P.dt;
 }
 
+// Face j of a subdomain: the slot's own faces, then its continuation's.
+template <typename R>
+__device__ __forceinline__ const FaceD<R>& faceOf(const SdomD<R>* S, int j) {
+    return j < MAX_FACES ? S->f[j] : S[1].f[j - MAX_FACES];
+}
+
 // Signed distance of the phonon from a general face (SdomD::gen), from its
 // frame coordinates u = idx + off.
 template <typename R>
@@ -854,7 +860,7 @@ struct Walker {
             // (montecarlo/boundary.cpp:102-110)
 #pragma unroll 1
             for (int j = 0; j < S->nface; ++j) {
-                const FaceD<R>& F = S->f[j];
+                const FaceD<R>& F = faceOf(S, j);
                 const R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
                 if (!(nd < R(0))) continue;
                 const R dist = -planeDist(F, ph) / nd;
@@ -871,7 +877,7 @@ struct Walker {
             bool out = sev < -S->eps;
 #pragma unroll 1
             for (int j = 0; j < S->nface; ++j) {
-                const FaceD<R>& F = S->f[j];
+                const FaceD<R>& F = faceOf(S, j);
                 const R nd = (F.n[0] * ph.d[0] + F.n[1] * ph.d[1]) + F.n[2] * ph.d[2];
                 if (planeDist(F, ph) + s * nd < -S->eps) out = true;
             }
@@ -922,7 +928,7 @@ struct Walker {
         else g.init(I.key0(), I.key1(), ph.id, &P);
         g.setEvent(ph.nloop + 1);
         // the event: a relaxation scatter (kind -1) or the face's boundary
-        const FaceD<R>* F = face >= 0 ? &S->f[face] : nullptr;
+        const FaceD<R>* F = face >= 0 ? (GEN ? &faceOf(S, face) : &S->f[face]) : nullptr;
         const int kind = face >= 0 ? F->kind : -1;
         if (face >= 0 && !gen) {
             // the flight ends on the face: snap that coordinate
@@ -974,8 +980,32 @@ struct Walker {
         } else if (kind == F_ISOT) {  // montecarlo/boundary.cpp:455-460
             stop = C_ABSORBED;
         } else if (kind == F_PERI || kind == F_INTER) {
-            // montecarlo/boundary.cpp:516-522 (Peri), 349-359 (Inter, single pair)
-            if (F->to < 0) {
+            // montecarlo/boundary.cpp:516-522 (Peri), 349-359 (Inter)
+            if (GEN && kind == F_INTER && F->more != 0) {
+                // several pairs: the first whose subdomain holds the
+                // position, within that subdomain's escape tolerance; none
+                // kills the phonon
+                const FaceD<R>* cand = S[1].f + (F->more & 0xFF);
+                const int nc = F->more >> 8;
+                R u[3];
+                for (int j = 0; j < 3; ++j) u[j] = (R)ph.idx[j] + ph.off[j];
+                const FaceD<R>* pick = nullptr;
+                for (int c = 0; c < nc && pick == nullptr; ++c) {
+                    const FaceD<R>* C = cand + c;
+                    const SdomD<R>* T = &I.sd()[C->to];
+                    R u2[3];
+                    rotate(C->A, u, u2);
+                    bool in = true;
+                    for (int j = 0; j < 3; ++j) {
+                        u2[j] += C->b[j];
+                        const R tol = T->eps * C->n[j];
+                        if (u2[j] < -tol || u2[j] > T->S[j] + tol) in = false;
+                    }
+                    if (in) pick = C;
+                }
+                F = pick;
+            }
+            if (F == nullptr || F->to < 0) {
                 stop = C_ESCAPES;
             } else {
                 if (F->tang) {

@@ -364,8 +364,8 @@ class HexDomain(Domain):
     ``Prism<PeriP<Polygon<6>>, PeriP<Polygon<6>>, Spec x 6>``
     (montecarlo/domain.cpp:238-256, type montecarlo/domain.h:139-142); the
     CLI uses dim = (length, d, d, d) and dT = 1e6 * length
-    (montecarlo/main.cpp:320-328). Eight faces: the oracle takes it, the
-    GPU kernels (at most six faces per subdomain) do not."""
+    (montecarlo/main.cpp:320-328). Eight faces: the kernels keep the last
+    two in a continuation slot."""
 
     name = "HexDomain"
 
@@ -391,8 +391,8 @@ class JctDomain(Domain):
     """L-junction of three blocks (montecarlo/domain.cpp:353-383, type
     montecarlo/domain.h:184-190): block 0's Rig face pairs with two Inter
     faces, so a phonon crossing it goes to the first block that contains
-    it (montecarlo/boundary.cpp:349-359). The GPU kernels take one pair per
-    Inter face; the oracle takes this domain."""
+    it (montecarlo/boundary.cpp:349-359); the kernels test the candidates
+    in that order."""
 
     name = "JctDomain"
 

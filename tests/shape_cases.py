@@ -55,4 +55,6 @@ def cases():
         "pyr": (D.PyrDomain.from_cli(1e-7, 1e-7), M.MULTI, 1500, 0.5e-12, 400),
         "tee": (D.TeeDomain.from_cli(5e-8, 3e-8, 4), M.MULTI, 1500, 0.5e-12, 400),
         "tube": (D.TubeDomain.from_cli(1e-7, 5e-8, 2e-8, 5, 3), M.MULTI, 1500, 0.5e-12, 400),
+        "hex": (D.HexDomain.from_cli(1e-7, 4e-8), M.MULTI, 1500, 0.5e-12, 400),
+        "jct": (D.JctDomain((5e-8, 5e-8, 5e-8, 4e-8), (4, 3, 3, 0), 1e-1), M.MULTI, 1500, 0.5e-12, 400),
     }

@@ -91,14 +91,21 @@ def test_prism_and_pyramid_volumes_follow_the_reference():
 
 
 def test_library_refuses_what_the_kernels_do_not_take():
-    """HexDomain's Prism<6> has eight faces and JctDomain pairs one Inter
-    face with two others: the library answers MC_ERR_UNSUPPORTED; the
-    oracle builds both."""
-    for dom in (D.HexDomain.from_cli(1e-7, 5e-8), D.JctDomain.from_cli(1e-7, 1e-7)):
-        O.ODomain(dom)
-        with pytest.raises(M._lib.McError) as e:
-            M.problem.DomainHandle(dom)
-        assert e.value.code == -4
+    """HexDomain's Prism<6> (eight faces) and JctDomain (one Inter face
+    paired with two others) take a continuation slot each; more than 32
+    slots in all is MC_ERR_UNSUPPORTED, which the oracle does not limit."""
+    hexp = D.HexDomain.from_cli(1e-7, 5e-8).ppeds[0]
+    ppeds, pairs = [], []
+    for i in range(17):
+        ppeds.append(D.Prism(hexp.o + np.array([0.0, 3e-7 * i, 0.0]), hexp.mat, 0, hexp.gradT, hexp.kinds))
+        pairs.append(D.Pair(D.PERI, i, 0, i, 1, np.array([1e-7, 0.0, 0.0])))
+    dom = D.Domain(ppeds, pairs)
+    O.ODomain(dom)
+    with pytest.raises(M._lib.McError) as e:
+        M.problem.DomainHandle(dom)
+    assert e.value.code == -4
+    for d in (D.HexDomain.from_cli(1e-7, 5e-8), D.JctDomain.from_cli(1e-7, 1e-7)):
+        assert M.problem.DomainHandle(d).cols == O.ODomain(d).cols
 
 
 def test_library_and_oracle_agree_on_columns_and_weights():
