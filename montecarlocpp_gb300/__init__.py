@@ -8,16 +8,19 @@ ABI in include/mc_gb300.h). This package mirrors the reference's host API
 
 from .batch import Batch
 from .serve import Server
-from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PERI, RIG, SPEC, TOP, BulkDomain,
-                      CrossPlaneFilmDomain, Domain, FilmDomain, Pair, Parallelepiped, PoreCellDomain)
+from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PARALLELEPIPED, PERI, PRISM, PYRAMID, RIG, SPEC,
+                      TETRAHEDRON, TOP, TRIANGULAR_PRISM, BulkDomain, CrossPlaneFilmDomain, Domain, FilmDomain,
+                      HexDomain, JctDomain, Pair, Parallelepiped, PoreCellDomain, Prism, PyrDomain, Pyramid,
+                      TeeDomain, Tetrahedron, TriangularPrism, TubeDomain)
 from .materials import SiliconModel, silicon_tables, write_material_files
 from .problem import (CUMFLUX, CUMTEMP, FLUX, MULTI, TEMP, CumFluxProblem, CumTempProblem, FluxProblem,
                       Material, MultiProblem, Session, TempProblem, kappa_from_flux)
 
 __all__ = [
     "BAC", "LEF", "BOT", "FRO", "RIG", "TOP", "SPEC", "DIFF", "ISOT", "PERI", "INTER",
-    "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "Pair",
-    "Parallelepiped", "SiliconModel", "silicon_tables", "write_material_files", "Material",
+    "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "PyrDomain", "HexDomain",
+    "JctDomain", "TeeDomain", "TubeDomain", "Pair", "Parallelepiped", "TriangularPrism", "Tetrahedron", "Prism",
+    "Pyramid", "PARALLELEPIPED", "TRIANGULAR_PRISM", "TETRAHEDRON", "PRISM", "PYRAMID", "SiliconModel", "silicon_tables", "write_material_files", "Material",
     "TempProblem", "FluxProblem", "MultiProblem", "CumTempProblem", "CumFluxProblem", "Session", "TEMP",
     "FLUX", "MULTI", "CUMTEMP", "CUMFLUX",
     "kappa_from_flux", "Batch", "Server",

@@ -76,8 +76,39 @@ int main(int argc, char** argv) {
             ss >> d0 >> div[0];
             double dim[3] = {d0, d0, d0};
             dom.reset(new mcgb::BulkDomain(dim, div, 1e6 * d0));
+        } else if (domStr == "hex") {  // montecarlo/main.cpp:320-328
+            double dim[4];
+            ss >> dim[0] >> dim[1];
+            dim[2] = dim[3] = dim[1];
+            dom.reset(new mcgb::HexDomain(dim, 1e6 * dim[0]));
+        } else if (domStr == "pyr") {  // montecarlo/main.cpp:330-337
+            double dim[3];
+            ss >> dim[0] >> dim[1];
+            dim[2] = dim[1];
+            dom.reset(new mcgb::PyrDomain(dim, 1e6 * dim[0]));
+        } else if (domStr == "jct") {  // montecarlo/main.cpp:339-348
+            double dim[4];
+            long div[4] = {0, 0, 0, 0};
+            ss >> dim[0] >> dim[3];
+            dim[1] = dim[2] = dim[0];
+            dom.reset(new mcgb::JctDomain(dim, div, 2e6 * dim[0]));
+        } else if (domStr == "tee") {  // montecarlo/main.cpp:350-362
+            double d0;
+            double dim[5];
+            long div0;
+            ss >> d0 >> dim[4] >> div0;
+            dim[0] = dim[1] = dim[2] = dim[3] = d0;
+            long div[5] = {div0, div0, div0, div0, 0};
+            dom.reset(new mcgb::TeeDomain(dim, div, 3e6 * d0));
+        } else if (domStr == "tube") {  // montecarlo/main.cpp:364-374
+            double dim[4];
+            long div[4] = {0, 0, 0, 0};
+            ss >> dim[0] >> dim[1] >> dim[3] >> div[1] >> div[3];
+            dim[2] = dim[1];
+            div[2] = div[1];
+            dom.reset(new mcgb::TubeDomain(dim, div, 1e6 * dim[0]));
         } else {
-            std::fprintf(stderr, "Invalid domain (film and bulk are served by this driver)\n");
+            std::fprintf(stderr, "Invalid domain (this driver serves film, bulk, hex, pyr, jct, tee and tube)\n");
             return 1;
         }
         long nemit = 0, maxscat = 0, maxloop = 0, nsim = 1, size = 0;

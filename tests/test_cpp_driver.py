@@ -37,7 +37,7 @@ def test_driver_fails_loudly_without_device(tmp_path):
 def test_driver_rejects_bad_arguments(tmp_path):
     M.write_material_files(str(tmp_path))
     B.build()
-    r = subprocess.run([B.MAIN, str(tmp_path), "silicon", "300", "hex", "1", "2"], capture_output=True, text=True)
+    r = subprocess.run([B.MAIN, str(tmp_path), "silicon", "300", "octet", "1", "2"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid domain" in r.stderr
     r = subprocess.run([B.MAIN, "/nonexistent/dir", "silicon", "300"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid directory" in r.stderr
@@ -76,3 +76,28 @@ def test_driver_cumflux_with_replicas(tmp_path, gmat):
     assert mean.shape == rm.shape == (9, 10)
     assert np.allclose(mean, rm, rtol=1e-8, atol=1e-8 * np.abs(rm).max())
     assert np.allclose(sd, rs, rtol=1e-6, atol=1e-8 * np.abs(rs).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("args,dom", [
+    (["pyr", "1e-7", "8e-8"], lambda: M.PyrDomain.from_cli(1e-7, 8e-8)),
+    (["hex", "1e-7", "4e-8"], lambda: M.HexDomain.from_cli(1e-7, 4e-8)),
+    (["jct", "5e-8", "4e-8"], lambda: M.JctDomain.from_cli(5e-8, 4e-8)),
+    (["tee", "5e-8", "3e-8", "4"], lambda: M.TeeDomain.from_cli(5e-8, 3e-8, 4)),
+    (["tube", "1e-7", "5e-8", "2e-8", "5", "3"], lambda: M.TubeDomain.from_cli(1e-7, 5e-8, 2e-8, 5, 3)),
+])
+def test_driver_domains_match_python_binding(tmp_path, gmat, args, dom):
+    """The reference's other CLI domains (montecarlo/main.cpp:320-374)
+    through the C++ mirror give the Python binding's field."""
+    M.write_material_files(str(tmp_path))
+    B.build()
+    cmd = [B.MAIN, str(tmp_path), "silicon", "300", *args, "multi", "400", "1000000", "0", "1", "5e-13", "100",
+           "64", "4"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip() and not ln.startswith("Solution")]
+    field = np.array([[float(x) for x in ln.split()] for ln in lines])
+    P = M.MultiProblem(gmat, dom(), 400, 1000000)
+    ref = P.solve(dt=5e-13, nsteps=100, precision=64, seed=4)
+    assert field.shape == ref.shape
+    assert np.allclose(field, ref, rtol=1e-8, atol=1e-8 * np.abs(ref).max())
