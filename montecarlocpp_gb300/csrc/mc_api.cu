@@ -1033,18 +1033,6 @@ int setupSession(mc_session_s* S) {
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
     S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
     if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
-    {
-        const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
-                                             S->tm == TM_SHARED);
-        S->smem = L.total;
-        setSingleLayout(P, L);
-        // static schedule: the state stages after the tables
-        if (!S->dyn) S->smem = staticStageOffset(L.total) + STATIC_STAGES * staticStageBytes<R>(S->block);
-    }
-    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
-    int dev = 0, nsm = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     // static schedule with a shared 1-D field along one axis in every
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
@@ -1056,10 +1044,34 @@ int setupSession(mc_session_s* S) {
         for (const auto& x : D.sd) same = same && x.accum == k && !D.needGen;
         if (same) S->lean = k;
     }
+    // FP32 lean flights tally into a carry-free copy of the field (exact
+    // while a block runs at most 65536 of them per launch, checked below)
+    const bool split = S->lean >= 0 && sizeof(R) == 4;
+    {
+        const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
+                                             S->tm == TM_SHARED, split);
+        S->smem = L.total;
+        setSingleLayout(P, L);
+        // static schedule: the state stages after the tables
+        if (!S->dyn) S->smem = staticStageOffset(L.total) + STATIC_STAGES * staticStageBytes<R>(S->block);
+    }
+    if (S->smem > 227 * 1024) return fail(MC_ERR_UNSUPPORTED, "shared-memory tables exceed 227 KB");
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     int occ = S->lean >= 0 ? advanceLeanOccupancy<R>(S->lean, S->block, S->smem)
                            : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    if (split && (S->nemit + S->grid - 1) / S->grid > 65536) {
+        // too many phonons per block for the carry-free copy: the walker
+        // for every phonon
+        S->lean = -1;
+        P.smSplit = 0;
+        occ = advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
+        if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
+        S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    }
     // state: two halves of (P0, P1, P2). The static schedule cuts each half
     // into one region of C slots per block of its (fixed) grid.
     size_t n = (size_t)S->nemit;

@@ -91,6 +91,7 @@ struct Params {
     // (setSingleLayout, vel at 0) or, in batched launches, the batched one
     // (setBatchLayout)
     int smVt, smWthr, smGuide, smSd, smTal, smStage;
+    int smSplit;       // carry-free lean-flight field, 0 if none
     int smVel;  // batched launches: their layout's vel table (0 otherwise)
     uint32_t key0, key1;
     // state (ping-pong halves chosen by the host)

@@ -56,6 +56,10 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
     if (TM == TM_SHARED) {
         const int nz = (int)talEntries(P.rows, P.cols);
         for (int i = threadIdx.x; i < nz; i += blockDim.x) tal[i] = 0;
+        if (P.smSplit) {
+            unsigned* sp = reinterpret_cast<unsigned*>(smraw + P.smSplit);
+            for (int i = threadIdx.x; i < 2 * nz; i += blockDim.x) sp[i] = 0u;
+        }
     }
     if (threadIdx.x == 0) {
         I->vel = vel; I->vt = vt; I->wthr = wthr; I->wguide = wguide; I->pthr = P.pthr;
@@ -131,6 +135,18 @@ __device__ __forceinline__ void flushSharedField(const InstD<R>& I, double* dst)
 template <typename R, int TM>
 __device__ __forceinline__ void closeBlock(const Params<R>& P, const InstD<R>& I) {
     __syncthreads();
+    if (TM == TM_SHARED && P.smSplit) {
+        // fold the lean flights' carry-free field into the 64-bit one
+        const int nz = (int)talEntries(P.rows, P.cols);
+        const unsigned char* base = reinterpret_cast<const unsigned char*>(I.tal) - P.smTal;
+        const unsigned* lo = reinterpret_cast<const unsigned*>(base + P.smSplit);
+        const int* hi = reinterpret_cast<const int*>(lo) + nz;
+        for (int e = threadIdx.x; e < nz; e += blockDim.x) {
+            const long long v = (long long)hi[e] * 65536 + (long long)lo[e];
+            if (v != 0) I.tal[e] += v;
+        }
+        __syncthreads();
+    }
     if (TM == TM_SHARED) flushSharedField<R>(I, P.tally);
     __syncthreads();
     if ((int)threadIdx.x < rowClasses(I.problem, I.rows) && g_blk.csum[threadIdx.x] != 0)
@@ -267,6 +283,7 @@ inline void setSingleLayout(Params<R>& P, const SmemLayout& L) {
     P.smGuide = (int)L.guide;
     P.smSd = (int)L.sd;
     P.smTal = (int)L.tal;
+    P.smSplit = (int)L.split;
     P.smStage = (int)staticStageOffset(L.total);
 }
 
@@ -391,7 +408,8 @@ k_advance(Params<R> P) {
             if constexpr (LEAN >= 0) {
                 if (have && back && !W.last) {
                     R tnext;
-                    lean = leanFlight<R, (LEAN >= 0 ? LEAN : 0), ParamView<R, TM>>(V, W, A0, A1, A2, tnext);
+                    lean = leanFlight<R, (LEAN >= 0 ? LEAN : 0), ParamView<R, TM>, (sizeof(R) == 4)>(V, W, A0, A1,
+                                                                                                  A2, tnext);
                     if (lean != LEAN_EVENT) {
                         nSteps += (unsigned)W.keff;
                         alive = lean == LEAN_ALIVE;
@@ -666,6 +684,7 @@ inline void setBatchLayout(Params<R>& P) {
     P.smGuide = (int)L.guide;
     P.smSd = (int)L.sd;
     P.smTal = (int)L.tal;
+    P.smSplit = 0;
     P.smStage = 0;
 }
 

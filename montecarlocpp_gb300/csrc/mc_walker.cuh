@@ -21,9 +21,10 @@ __host__ __device__ inline size_t talEntries(int rows, int cols) {
 // scatter bin thresholds and guide table, the subdomains (when staged), the
 // instance descriptor, then the block's tally.
 struct SmemLayout {
-    size_t vel = 0, vt = 0, wthr = 0, guide = 0, sd = 0, inst = 0, tal = 0, total = 0;
+    size_t vel = 0, vt = 0, wthr = 0, guide = 0, sd = 0, inst = 0, tal = 0, split = 0, total = 0;
     template <typename R>
-    __host__ __device__ void init(int nw, int np, int nsdShared, int rows, int cols, bool sharedTally) {
+    __host__ __device__ void init(int nw, int np, int nsdShared, int rows, int cols, bool sharedTally,
+                                  bool splitTally = false) {
         auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
         const size_t nt = (size_t)nw * np;
         vel = 0;
@@ -34,16 +35,22 @@ struct SmemLayout {
         inst = al(sd + sizeof(SdomD<R>) * (size_t)nsdShared);
         tal = al(inst + sizeof(InstD<R>));
         total = tal + (sharedTally ? sizeof(long long) * talEntries(rows, cols) : 0);
+        if (splitTally) {
+            split = al(total);
+            total = split + 2 * sizeof(unsigned) * talEntries(rows, cols);
+        }
     }
 };
 
 // Shared layout of a single-instance advance launch (tables, every
 // subdomain image, descriptor, fixed-point field when the tally is shared);
 // the host sizes the launch with the same function.
+// splitTally: the lean flights' carry-free field (below) after the tally.
 template <typename R>
-__host__ __device__ inline SmemLayout singleLayout(int nw, int np, int nsd, int rows, int cols, bool sharedTally) {
+__host__ __device__ inline SmemLayout singleLayout(int nw, int np, int nsd, int rows, int cols, bool sharedTally,
+                                                   bool splitTally = false) {
     SmemLayout L;
-    L.init<R>(nw, np, nsd, rows, cols, sharedTally);
+    L.init<R>(nw, np, nsd, rows, cols, sharedTally, splitTally);
     return L;
 }
 
@@ -266,6 +273,10 @@ struct ParamView {
     __device__ __forceinline__ long long* dif() const {
         return reinterpret_cast<long long*>(sm + P->smTal) + (size_t)talStride(P->rows) * P->cols;
     }
+    // the carry-free field of the lean flights: low 16-bit parts, then the
+    // high parts, one 32-bit word each per entry of the 64-bit field
+    __device__ __forceinline__ unsigned* split() const { return reinterpret_cast<unsigned*>(sm + P->smSplit); }
+    __device__ __forceinline__ int entries() const { return (int)talEntries(P->rows, P->cols); }
     __device__ __forceinline__ double* tally() const { return P->tally; }
     __device__ __forceinline__ double* gdif() const { return nullptr; }
     __device__ __forceinline__ int groups() const { return 1; }
@@ -330,7 +341,13 @@ struct BatchView {
 };
 
 // Field accumulation for one flight of one instance.
-template <typename R, int TM, typename IA>
+// SPLIT (FP32 lean flights only): adds go to a carry-free copy of the
+// shared field instead -- the low 16 bits of the amount into one 32-bit
+// word, the rest (arithmetic shift) into another, both without a returned
+// value. A lean flight adds to an entry at most once and a block runs at
+// most regCap <= 65536 of them per launch, so neither word can overflow;
+// closeBlock folds the copy into the 64-bit field.
+template <typename R, int TM, typename IA, bool SPLIT = false>
 struct Tally {
     IA V;
     long long goff;  // offset of the phonon's field copy (global layouts)
@@ -351,14 +368,26 @@ struct Tally {
     __device__ __forceinline__ void csumAdd(int r, long long v) const { blkCsum(r, v); }
     // shared field and difference array, cell-major: row r of column c at
     // [c * talStride(rows) + r]
+    __device__ __forceinline__ void splitAdd(int e, Fix v) const {
+        unsigned* lo = V.split();
+        atomicAdd(lo + e, (unsigned)v & 0xFFFFu);
+        atomicAdd(reinterpret_cast<int*>(lo) + V.entries() + e, (int)(v >> 16));
+    }
     __device__ __forceinline__ void atomShared(int r, int col, Fix v) const {
-        sharedAdd64(&V.tal()[col * talStride(V.rows()) + rowBase + r], v);
+        if constexpr (SPLIT) splitAdd(col * talStride(V.rows()) + rowBase + r, v);
+        else sharedAdd64(&V.tal()[col * talStride(V.rows()) + rowBase + r], v);
     }
     __device__ __forceinline__ void atomRange(int r, int c0, int c1, Fix v) const {
-        long long* d = V.dif() + rowBase + r;
         const int st = talStride(V.rows());
-        sharedAdd64(d + c0 * st, v);
-        sharedAdd64(d + c1 * st, -v);
+        if constexpr (SPLIT) {
+            const int d = st * V.cols() + rowBase + r;
+            splitAdd(d + c0 * st, v);
+            splitAdd(d + c1 * st, -v);
+        } else {
+            long long* d = V.dif() + rowBase + r;
+            sharedAdd64(d + c0 * st, v);
+            sharedAdd64(d + c1 * st, -v);
+        }
     }
     __device__ __forceinline__ void addGlobal(int col, R t) const {
 #pragma unroll
@@ -388,8 +417,8 @@ struct Tally {
 // amount times the phonon's sign): the per-metre amounts rho and the rows'
 // place in the field, from the phonon's sign, 1/v, direction and scatter
 // count before the flight.
-template <typename R, int TM, typename IA>
-__device__ __forceinline__ void setFlightRows(Tally<R, TM, IA>& T, int problem, bool neg, R iv, const R d[3],
+template <typename R, int TM, typename IA, bool SPLIT>
+__device__ __forceinline__ void setFlightRows(Tally<R, TM, IA, SPLIT>& T, int problem, bool neg, R iv, const R d[3],
                                               uint32_t nscat, int cumStep) {
     const R sg = neg ? R(-1) : R(1);
     T.rowBase = 0;
@@ -448,9 +477,9 @@ __device__ __forceinline__ T pick3(const T v[3], int k) {
 // takes the integer remainder, so the cells add up to V exactly. Called
 // with a constant K the selects fold away (one copy per axis); with a
 // run-time K one copy serves every axis.
-template <typename R, int TM, typename IA>
+template <typename R, int TM, typename IA, bool SPLIT = false>
 __device__ __forceinline__ void fly1d(Phn<R>& ph, const SdomD<R>& S, const R a[3], const R ia[3], R s,
-                                      Tally<R, TM, IA>& T, const int K) {
+                                      Tally<R, TM, IA, SPLIT>& T, const int K) {
     const int cb = S.colbeg;
     const int b = pick3(ph.idx, K);
     const int n = S.shape[K];
@@ -1128,7 +1157,7 @@ enum { LEAN_EVENT = 0, LEAN_ALIVE = 1, LEAN_BAD = 2 };
 // tallied, the state packed back into A0..A2, *tnext set to the time from
 // the window end to the next event, and LEAN_ALIVE returned (LEAN_BAD for a
 // non-finite free path, which the caller counts as the walker would).
-template <typename R, int K, typename IA>
+template <typename R, int K, typename IA, bool SPLIT = false>
 __device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typename Vec4<R>::T& A0,
                                           typename Vec4<R>::T& A1, uint4& A2, R& tnext) {
     Phn<R> ph;
@@ -1159,11 +1188,11 @@ __device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typen
     }
     if (sev * iv <= W.len) return LEAN_EVENT;
     const R s = W.len * v;
-    Tally<R, TM_SHARED, IA> T;
+    Tally<R, TM_SHARED, IA, SPLIT> T;
     T.V = I;
     T.goff = 0;
     setFlightRows(T, I.problem(), ph.neg, iv, ph.d, ph.nscat, I.cumStep());
-    fly1d<R, TM_SHARED, IA>(ph, S, a, ia, s, T, K);
+    fly1d<R, TM_SHARED, IA, SPLIT>(ph, S, a, ia, s, T, K);
     ph.scatNext -= s;
     if (ph.scatNext < Lim<R>::tiny()) ph.scatNext = R(0);
     tnext = (sev - s) * iv;
