@@ -215,6 +215,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-pore", action="store_true")
+    ap.add_argument("--no-shapes", action="store_true")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-duration", type=float, default=3.0)
     ap.add_argument("--serve-drain", type=float, default=90.0)
@@ -352,6 +353,8 @@ def main():
         line["precision"] = precision_errors(prob, dom, W, K, seed, out)
     if not args.no_pore:
         line["pore_cell"] = bench_pore(K)
+    if not args.no_shapes:
+        line["other_shapes"] = bench_shapes(K)
     if not args.no_plain:
         line["plain_kernel"] = plain_kernel(prob, W, stream, peak, peak_kind)
     if not args.no_batched:
@@ -434,6 +437,30 @@ def bench_pore(K, nemit=50_000_000, nemit_fp64=5_000_000, nsteps=4000, dt=0.5e-1
     b = small.solve(precision=64, seed=seed, **kw)
     c = small.solve(precision=64, seed=seed + 7777, **kw)
     out["fp32_vs_fp64"] = dict(field_errors(a, b, c, dom), phonons=int(small.stats["nemit"]))
+    return out
+
+
+def bench_shapes(K, nemit=2_000_000, nsteps=4000, dt=0.5e-12, seed=5):
+    """The reference's domains with subdomains other than the Parallelepiped
+    or with an Inter face paired twice (CLI arguments of
+    montecarlo/main.cpp:320-348): hex rod (Prism<6>, eight faces), square
+    pyramid, L-junction; 2e6 phonons, dt 0.5 ps x 4000, FP32 flight, one
+    solve each through mc_solve, after a short warm-up solve."""
+    import montecarlocpp_gb300 as M
+    mat = M.Material.silicon(300.0)
+    doms = {"hex 100 nm x 40 nm": M.HexDomain.from_cli(1e-7, 4e-8),
+            "pyr 100 nm x 100 nm": M.PyrDomain.from_cli(1e-7, 1e-7),
+            "jct 100 nm x 50 nm": M.JctDomain.from_cli(1e-7, 5e-8)}
+    out = {}
+    for name, dom in doms.items():
+        prob = M.MultiProblem(mat, dom, nemit, 1_000_000)
+        prob.solve(dt=dt, nsteps=50, precision=32, steps_per_launch=50, seed=seed)
+        t0 = time.perf_counter()
+        prob.solve(dt=dt, nsteps=nsteps, precision=32, steps_per_launch=K, seed=seed)
+        el = time.perf_counter() - t0
+        st = prob.stats
+        out[name] = {"phonons": st["nemit"], "phonon_steps": st["phonon_steps"], "events": st["events"],
+                     "e2e_s": el, "e2e_phonon_steps_per_s": st["phonon_steps"] / el}
     return out
 
 

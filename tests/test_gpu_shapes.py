@@ -96,3 +96,57 @@ def test_batch_of_shapes_equals_single_solves_fp64(gmat):
         assert st["nemit"] == p.stats["nemit"]
         assert field_err_nan(ref, got) < 1e-9, names[i]
     B.close()
+
+
+@pytest.mark.parametrize("name,schedule,K", [("pyr5", 1, 1), ("jct", 2, 25), ("hex", 2, 25)])
+def test_snapshot_resume_on_shapes(name, schedule, K, gmat):
+    """A session of a shape domain restored from a half-way snapshot
+    continues exactly as the original."""
+    dom, kind, nemit, dt, nsteps = CASES[name]
+    P = PROBLEM[kind](gmat, dom, nemit, 10**6)
+    kw = dict(dt=dt, nsteps=200, precision=64, steps_per_launch=K, schedule=schedule, seed=8)
+    a = P.session(**kw)
+    a.emit()
+    a.advance(100 // K)
+    snap = a.snapshot()
+    a.advance(1 << 20)
+    fa, sa = a.result()
+    b = P.session(**kw)
+    b.restore(snap)
+    assert b.advance(1 << 20)
+    fb, sb = b.result()
+    for k in ("events", "scatters", "absorbed", "horizon_stops", "phonon_steps", "escapes"):
+        assert sa[k] == sb[k], k
+    assert field_err_nan(fa, fb) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["wedge", "jct"])
+def test_cumflux_on_shapes_fp64(name, gmat, omat):
+    """CumFlux (scatter-count bins) on a shape domain: the FP64 kernels
+    against the oracle."""
+    dom, _, nemit, dt, nsteps = CASES[name]
+    od = O.ODomain(dom)
+    o, ost, _ = O.solve(omat, od, O.CUMFLUX, nemit=nemit, maxscat=21, dt=dt, horizon=dt * 200, rng=O.RNG_PHILOX,
+                        seed=9, size=4)
+    P = M.CumFluxProblem(gmat, dom, nemit, 4, 21)
+    g = P.solve(dt=dt, nsteps=200, precision=64, seed=9, steps_per_launch=200)
+    assert P.stats["events"] == ost["events"]
+    assert field_err_nan(o, g) < 1e-9
+
+
+def test_batch_of_shapes_fp32_graph(gmat):
+    """FP32 batched shapes under a CUDA graph, replayed: identical results
+    on replay and the single solves' fields to FP32 summation order."""
+    names = ["pyr", "hex", "jct", "prism4"]
+    probs = [PROBLEM[CASES[n][1]](gmat, CASES[n][0], CASES[n][2], 10**6) for n in names]
+    dt, nsteps = 0.5e-12, 300
+    B = M.Batch(probs, dt=dt, nsteps=nsteps, precision=32, use_graph=True)
+    B.run()
+    first = [B.result(i)[0] for i in range(len(probs))]
+    B.run()
+    for i, p in enumerate(probs):
+        again = B.result(i)[0]
+        assert field_err_nan(first[i], again) < 1e-12, names[i]
+        ref = p.solve(dt=dt, nsteps=nsteps, precision=32, seed=i)
+        assert field_err_nan(ref, again) < 1e-5, names[i]
+    B.close()
