@@ -88,7 +88,7 @@ typedef struct {
 } mc_pair_desc;
 
 /* Domain assembly (montecarlo/domain.cpp:88-102 addSdom and the
- * init() of each domain). Limits: <= 32 subdomains, <= 512 cells per axis
+ * init() of each domain). Limits: <= 64 subdomains, <= 512 cells per axis
  * per subdomain. */
 int mc_domain_create(const mc_pped_desc* ppeds, int n, const mc_pair_desc* pairs, int npairs,
                      mc_domain_h* out);
@@ -113,10 +113,9 @@ enum {
  * column c at mat[3c .. 3c + 2]. Prism and Pyramid take one division
  * count, div[0]: < 0 no field, else one column for the whole subdomain.
  * A subdomain takes one device slot, two when it has more than 6 faces or
- * an Inter face paired more than once (at most 32 slots, at most 6 faces
- * plus pair candidates beyond the first 6 faces). Peri faces of the other
- * shapes take the identity rotation only, and an Inter face paired more
- * than once pairs with Parallelepipeds only; MC_ERR_UNSUPPORTED otherwise. */
+ * an Inter face paired more than once (at most 64 slots, at most 6 faces
+ * plus pair candidates beyond the first 6 faces); MC_ERR_UNSUPPORTED
+ * otherwise. */
 typedef struct {
     int shape;
     int ncols;

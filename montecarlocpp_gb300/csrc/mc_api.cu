@@ -305,6 +305,7 @@ struct HostSdom {
     std::vector<double> subvol;  // Prism / Pyramid: volume(mat)
     V3 fo;                // frame origin and matrix
     M3 FM;
+    double edge = 0.;     // longest matrix column
 };
 
 // Faces of each shape in bdry<I>() order and its volume: Parallelepiped
@@ -381,6 +382,7 @@ int buildShape(const mc_sdom_desc& p, HostSdom& H) {
         return fail(MC_ERR_ARG, "invalid subdomain shape");
     }
     if (!(H.vol >= DMIN)) return fail(MC_ERR_ARG, "Volume too small, check vector order");
+    for (const V3& x : H.col) H.edge = std::max(H.edge, std::sqrt(dot(x, x)));
     for (const HostFace& F : H.f) {
         if (F.kind < MC_SPEC || F.kind > MC_INTER) return fail(MC_ERR_ARG, "invalid face kind");
         if ((F.kind == MC_SPEC || F.kind == MC_DIFF || F.kind == MC_INTER) && F.T != 0.)
@@ -486,7 +488,7 @@ namespace {
 
 int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, mc_domain_s** out) {
     if (!ps || n <= 0) return fail(MC_ERR_ARG, "Domain setup not complete");
-    if (n > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 32 subdomains");
+    if (n > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 64 subdomains");
     std::unique_ptr<mc_domain_s> D(new mc_domain_s);
     D->desc.assign(ps, ps + n);
     D->sd.resize(n);
@@ -511,10 +513,21 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         HostFace& a = H[P.sdom1].f[P.face1];
         HostFace& b = H[P.sdom2].f[P.face2];
         if (a.kind != P.kind || b.kind != P.kind) return fail(MC_ERR_ARG, "pair kind does not match faces");
+        // the makePair checks (montecarlo/boundary.cpp:363-368,527-535):
+        // unit normals within 1e-12, plane offsets within 1e-9 of the
+        // larger subdomain edge
+        const double L = std::max(H[P.sdom1].edge, H[P.sdom2].edge);
+        auto near = [](const V3& x, const V3& y) { return std::sqrt(dot(subv(x, y), subv(x, y))) <= 1e-12; };
         if (P.kind == MC_PERI) {
             if (a.pairS >= 0 || b.pairS >= 0) return fail(MC_ERR_ARG, "Boundary already paired");
             M3 R; std::memcpy(R.m, P.rot, sizeof(R.m));
             V3 t = mk(P.transl[0], P.transl[1], P.transl[2]);
+            M3 RRt = mmul(R, transp(R));
+            for (int i = 0; i < 9; ++i)
+                if (std::fabs(RRt.m[i] - eye().m[i]) > 1e-12) return fail(MC_ERR_ARG, "Rotation matrix must be orthogonal");
+            if (!near(mvec(R, a.n), sclv(-1., b.n))) return fail(MC_ERR_ARG, "Rotation matrix incorrect");
+            const V3 tf = addv(sclv(dot(a.n, a.o), mvec(R, a.n)), t);
+            if (std::fabs(dot(b.n, tf) - dot(b.n, b.o)) > 1e-9 * L) return fail(MC_ERR_ARG, "Translation vector incorrect");
             double T1 = a.T, T2 = b.T;
             a.T = T1 - T2; b.T = T2 - T1;
             a.R = R; b.R = transp(R);
@@ -524,6 +537,8 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
             a.pairS = P.sdom2; a.pairF = P.face2;
             b.pairS = P.sdom1; b.pairF = P.face1;
         } else if (P.kind == MC_INTER) {
+            if (!near(a.n, sclv(-1., b.n))) return fail(MC_ERR_ARG, "Boundary normals not antiparallel");
+            if (std::fabs(dot(a.n, a.o) - dot(a.n, b.o)) > 1e-9 * L) return fail(MC_ERR_ARG, "Boundaries planes not the same");
             a.inter.push_back(std::make_pair(P.sdom2, P.face2));
             b.inter.push_back(std::make_pair(P.sdom1, P.face1));
             if (a.pairS < 0) { a.pairS = P.sdom2; a.pairF = P.face2; }
@@ -553,13 +568,7 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         if (extraFaces[s] + cand[s] > 0) { D->refOfSlot.push_back(-1); ++nslot; }
         if (H[s].shape != MC_PARALLELEPIPED || extraFaces[s] + cand[s] > 0) D->needGen = true;
     }
-    if (nslot > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 32 subdomain slots");
-    for (int s = 0; s < n; ++s)
-        for (const HostFace& F : H[s].f)
-            if (F.inter.size() > 1)
-                for (const auto& q : F.inter)
-                    if (H[q.first].shape != MC_PARALLELEPIPED)
-                        return fail(MC_ERR_UNSUPPORTED, "several Inter pairs into a non-Parallelepiped subdomain");
+    if (nslot > MAX_SDOM) return fail(MC_ERR_UNSUPPORTED, "more than 64 subdomain slots");
     D->sd.assign(nslot, SdomD<double>());
     for (SdomD<double>& x : D->sd) {
         std::memset(&x, 0, sizeof(x));
@@ -680,7 +689,7 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
         bool id = true;
         for (int i = 0; i < 9; ++i) if (R.m[i] != eye().m[i]) id = false;
         G.ident = id ? 1 : 0;
-        if (!S.gen) std::memcpy(G.Rd, R.m, sizeof(R.m));
+        std::memcpy(G.Rd, R.m, sizeof(R.m));
         M3 Mi2; std::memcpy(Mi2.m, T2.Minv, sizeof(Mi2.m));
         M3 M1; std::memcpy(M1.m, S.M, sizeof(M1.m));
         M3 A = mmul(mmul(Mi2, R), M1);
@@ -728,9 +737,6 @@ int buildDomain(const mc_sdom_desc* ps, int n, const mc_pair_desc* qs, int nq, m
                 G.gp[3] = dot(F.n, subv(mk(S.o[0], S.o[1], S.o[2]), F.o));
             }
             if (F.kind == MC_PERI) {
-                bool id = true;
-                for (int i = 0; i < 9; ++i) if (F.R.m[i] != eye().m[i]) id = false;
-                if (S.gen && !id) return fail(MC_ERR_UNSUPPORTED, "Peri rotation on a non-Parallelepiped face");
                 setMap(G, s, f, F.R, F.t, F.pairS, F.pairF);
             } else if (F.kind == MC_INTER && F.inter.size() == 1) {
                 setMap(G, s, f, eye(), mk(0, 0, 0), F.pairS, F.pairF);
@@ -841,6 +847,7 @@ void castSdom(const SdomD<double>& a, SdomD<R>& b, bool f32) {
         y.kind = x.kind; y.to = x.to; y.toface = x.toface; y.ident = x.ident; y.tang = x.tang; y.more = x.more;
         for (int i = 0; i < 3; ++i) { y.n[i] = (R)x.n[i]; y.b[i] = (R)x.b[i]; }
         for (int i = 0; i < 9; ++i) { y.rot[i] = (R)x.rot[i]; y.Rd[i] = (R)x.Rd[i]; y.A[i] = (R)x.A[i]; }
+        for (int i = 0; i < 4; ++i) y.gp[i] = (R)x.gp[i];
         y.T = (R)x.T;
     }
 }

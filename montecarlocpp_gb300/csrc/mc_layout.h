@@ -53,8 +53,7 @@ enum Status {
 // One face of a subdomain. A Parallelepiped's face f lies on axis f % 3 of
 // its reduced coordinates at u = 0 (f < 3) or u = S (f >= 3). The faces of
 // the other shapes (SdomD::gen) are planes in the subdomain's frame
-// coordinates: gp[0..2] . u + gp[3] is the signed distance from the face,
-// kept in place of Rd (such faces take Peri pairs without rotation only).
+// coordinates: gp[0..2] . u + gp[3] is the signed distance from the face.
 //
 // An Inter face paired with several others (montecarlo/boundary.cpp:349-359)
 // keeps its candidates as entries of its subdomain's continuation slot:
@@ -71,13 +70,11 @@ struct FaceD {
     int more;     // Inter candidates in the continuation slot (see above), 0 for one pair
     R n[3];       // inward unit normal (Spec reflection)
     R rot[9];     // rotation z-hat -> n, row-major (Diff, Isot emission)
-    union {
-        R Rd[9];  // Peri direction rotation, row-major
-        R gp[4];  // plane in frame coordinates (general faces)
-    };
+    R Rd[9];      // Peri direction rotation, row-major
     R A[9];       // reduced-coordinate map into subdomain `to`: u' = A u + b
     R b[3];
     R T;          // emission temperature after pairing (Isot / Peri)
+    R gp[4];      // plane in frame coordinates (general faces)
 };
 
 // Faces a subdomain slot holds. A subdomain with more faces, or with Inter
@@ -129,10 +126,11 @@ struct EmitterD {
     double L[MAX_PIECES][9];             // row-major
 };
 
-// Packed cell: 5-bit subdomain, three 9-bit cell indices.
+// Packed cell: the low 5 bits of the subdomain slot and three 9-bit cell
+// indices; the slot's sixth bit rides in bit 26 of the prop word.
 constexpr int CELL_BITS = 9;
 constexpr int MAX_SHAPE = 1 << CELL_BITS;
-constexpr int MAX_SDOM = 32;
+constexpr int MAX_SDOM = 64;
 // Walk cells on an axis that carries no tally cells (div = 0) of a
 // subdomain with a 0-D or 1-D field: positions are stored as cell index +
 // offset, so this sets the FP32 resolution along that axis.

@@ -754,8 +754,8 @@ __device__ __forceinline__ void packPhonon(const Phn<R>& ph, typename Vec4<R>::T
                                            uint4& A2) {
     A0.x = ph.off[0]; A0.y = ph.off[1]; A0.z = ph.off[2]; A0.w = ph.scatNext;
     A1.x = ph.d[0]; A1.y = ph.d[1]; A1.z = ph.d[2]; A1.w = idToReal<R>(ph.id);
-    A2.x = packCell(ph.s, ph.idx);
-    A2.y = packProp(ph.w, ph.p, ph.neg);
+    A2.x = packCell(ph.s & 31, ph.idx);
+    A2.y = packProp(ph.w, ph.p, ph.neg) | ((uint32_t)(ph.s >> 5) << 26);
     A2.z = ph.nscat;
     A2.w = ph.nloop;
 }
@@ -840,6 +840,7 @@ struct Walker {
                                          const uint4& A2) {
         I = inst;
         unpackCell(A2.x, ph.s, ph.idx);
+        ph.s |= (int)((A2.y >> 26) & 1u) << 5;
         ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
         ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
         ph.id = realToId<R>(A1.w);
@@ -1024,11 +1025,19 @@ struct Walker {
                     const SdomD<R>* T = &I.sd()[C->to];
                     R u2[3];
                     rotate(C->A, u, u2);
+                    for (int j = 0; j < 3; ++j) u2[j] += C->b[j];
                     bool in = true;
-                    for (int j = 0; j < 3; ++j) {
-                        u2[j] += C->b[j];
-                        const R tol = T->eps * C->n[j];
-                        if (u2[j] < -tol || u2[j] > T->S[j] + tol) in = false;
+                    if (T->gen) {
+                        // Subdomain::isInside over the target's faces
+                        for (int j = 0; j < T->nface; ++j) {
+                            const FaceD<R>& G = faceOf(T, j);
+                            if (((G.gp[0] * u2[0] + G.gp[1] * u2[1]) + G.gp[2] * u2[2]) + G.gp[3] < -T->eps) in = false;
+                        }
+                    } else {
+                        for (int j = 0; j < 3; ++j) {
+                            const R tol = T->eps * C->n[j];
+                            if (u2[j] < -tol || u2[j] > T->S[j] + tol) in = false;
+                        }
                     }
                     if (in) pick = C;
                 }
@@ -1162,6 +1171,7 @@ __device__ __forceinline__ int leanFlight(const IA& I, const Window<R>& W, typen
                                           typename Vec4<R>::T& A1, uint4& A2, R& tnext) {
     Phn<R> ph;
     unpackCell(A2.x, ph.s, ph.idx);
+        ph.s |= (int)((A2.y >> 26) & 1u) << 5;
     ph.off[0] = A0.x; ph.off[1] = A0.y; ph.off[2] = A0.z; ph.scatNext = A0.w;
     ph.d[0] = A1.x; ph.d[1] = A1.y; ph.d[2] = A1.z;
     ph.id = realToId<R>(A1.w);

@@ -39,7 +39,7 @@ __all__ = [
     "PARALLELEPIPED", "TRIANGULAR_PRISM", "TETRAHEDRON", "PRISM", "PYRAMID",
     "Parallelepiped", "TriangularPrism", "Tetrahedron", "Prism", "Pyramid", "Pair", "Domain",
     "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "PyrDomain", "HexDomain",
-    "JctDomain", "TeeDomain", "TubeDomain",
+    "JctDomain", "TeeDomain", "TubeDomain", "OctetDomain",
 ]
 
 
@@ -466,3 +466,184 @@ class TubeDomain(Domain):
     @classmethod
     def from_cli(cls, L, a, t, n, m):
         return cls((L, a, a, t), (0, n, n, m), 1e6 * L)
+
+
+class OctetDomain(Domain):
+    """One cell of an octet-truss lattice (montecarlo/domain.cpp:591-1238,
+    types montecarlo/domain.h:298-344): 42 subdomains -- Prism<4> slabs
+    and nodes, TriangularPrisms, Pyramids and Parallelepipeds -- joined by
+    Inter pairs (ten faces paired with two others), with five Peri pairs
+    mapped by the reflection diag(-1, 1, 1) and the translation
+    (s/2, 0, -s/2). The ten vertical struts (16-25) carry the cells and the
+    gradient. dim = (s, d1, d2, t): a = pi/5 (d1 + d2) - (4 - pi)/5 t and
+    b = a/4; div = (div0 .. div3) as the reference's CLI `octet` takes them
+    (montecarlo/main.cpp:376-386)."""
+
+    name = "OctetDomain"
+    # face kinds per subdomain in bdry<I>() order (Prism: Bot, Top, sides;
+    # Pyramid: Bot, sides; TriangularPrism: Bac, Lef, Bot, Dia, Top)
+    _I, _D, _S, _P = INTER, DIFF, SPEC, PERI
+    KINDS = [
+        (_I, _P, _I, _D, _S, _D), (_D, _I, _I, _D, _S, _I), (_D, _D, _I, _I, _S, _S), (_I, _P, _D, _I, _I, _D),
+        (_I, _I, _D, _I, _I, _I), (_I, _S, _D, _D, _I, _I), (_S, _I, _P, _D, _I, _D), (_I, _D, _P, _D, _I, _I),
+        (_D, _D, _P, _I, _I, _I), (_D, _D, _I, _I, _I, _I), (_I, _D, _I, _I, _D, _I), (_S, _I, _D, _I, _D, _I),
+        (_D, _I, _I, _S, _I), (_I, _D, _I, _S, _I), (_I, _I, _D, _S, _I), (_D, _D, _I, _I, _S, _S),
+        (_D, _S, _I, _D, _I, _I), (_I, _I, _I, _D, _D, _I), (_I, _D, _I, _I, _D, _I), (_D, _I, _I, _I, _D, _I),
+        (_D, _S, _I, _D, _I, _I), (_D, _S, _I, _D, _I, _I), (_D, _I, _I, _I, _D, _I), (_I, _D, _I, _I, _D, _I),
+        (_I, _I, _I, _D, _D, _I), (_D, _S, _I, _D, _I, _I), (_D, _D, _I, _I, _S, _S), (_I, _I, _D, _S, _I),
+        (_I, _D, _I, _S, _I), (_D, _I, _I, _S, _I), (_S, _I, _D, _I, _D, _I), (_I, _D, _I, _I, _D, _I),
+        (_D, _D, _I, _I, _I, _I), (_D, _D, _P, _I, _I, _I), (_I, _D, _P, _D, _I, _I), (_S, _I, _P, _D, _I, _D),
+        (_I, _S, _D, _D, _I, _I), (_I, _I, _D, _I, _I, _I), (_I, _P, _D, _I, _I, _D), (_D, _D, _I, _I, _S, _S),
+        (_D, _I, _I, _D, _S, _I), (_I, _P, _I, _D, _S, _D),
+    ]
+    INTER_PAIRS = [
+        (0, 0, 1, 1), (1, 5, 2, 3), (0, 2, 3, 4), (1, 2, 4, 4), (2, 2, 5, 5), (3, 0, 4, 1), (4, 5, 5, 4),
+        (3, 3, 8, 5), (4, 3, 8, 5), (4, 0, 9, 2), (5, 0, 9, 2), (5, 0, 12, 4),
+        (6, 1, 7, 0), (7, 5, 8, 3), (9, 4, 10, 2), (10, 0, 11, 1), (9, 5, 12, 1), (9, 5, 13, 0), (10, 5, 14, 1),
+        (11, 5, 15, 2), (12, 2, 13, 2), (13, 4, 14, 4), (14, 0, 15, 3),
+        (6, 4, 16, 5), (7, 4, 17, 5), (8, 4, 18, 5), (9, 3, 18, 5), (10, 3, 19, 5), (11, 3, 20, 5),
+        (16, 4, 17, 1), (17, 0, 18, 3), (18, 0, 19, 3), (19, 1, 20, 4),
+        (16, 2, 21, 2), (17, 2, 22, 2), (18, 2, 23, 2), (19, 2, 24, 2), (20, 2, 25, 2),
+        (21, 4, 22, 1), (22, 3, 23, 0), (23, 3, 24, 0), (24, 1, 25, 4),
+        (21, 5, 30, 3), (22, 5, 31, 3), (23, 5, 32, 3), (23, 5, 33, 4), (24, 5, 34, 4), (25, 5, 35, 4),
+        (26, 3, 27, 0), (27, 4, 28, 4), (28, 2, 29, 2), (26, 2, 30, 5), (27, 1, 31, 5), (28, 0, 32, 5),
+        (29, 1, 32, 5), (30, 1, 31, 0), (31, 2, 32, 4), (33, 3, 34, 5), (34, 0, 35, 1),
+        (29, 4, 36, 0), (32, 2, 36, 0), (32, 2, 37, 0), (33, 5, 37, 3), (33, 5, 38, 3),
+        (36, 4, 37, 5), (37, 1, 38, 0), (36, 5, 39, 2), (37, 4, 40, 2), (38, 4, 41, 2), (39, 3, 40, 5),
+        (40, 1, 41, 0),
+    ]
+    PERI_PAIRS = [(0, 1, 41, 1), (3, 1, 38, 1), (6, 2, 35, 2), (7, 2, 34, 2), (8, 2, 33, 2)]
+    AVERAGED = range(16, 26)
+
+    def __init__(self, dim, div, dT):
+        d = np.asarray(dim, dtype=np.float64)
+        v = np.asarray(div, dtype=np.int64)
+        self.dim, self.div, self.dT = d, v, float(dT)
+        r = np.sqrt(2.0)
+        s = d[0]
+        a = np.pi / 5.0 * (d[1] + d[2]) - (4.0 - np.pi) / 5.0 * d[3]
+        b = a / 4.0
+        t = d[3]
+        if not (b > t and a > (r + 1) * (b + t) and s / 2 > a + (r + 1) * (b + t) + t):
+            raise ValueError("Invalid dimensions")
+        self.a, self.b, self.t = a, b, t
+        den = s - 2 * a - 2 * (r + 1) * b - 2 * (2 + r) * t
+        g = np.array([dT / den, 0.0, -dT / den])
+        z = np.zeros(3)
+        h = 0.5
+        q1, q2 = (r + 1) * h, (2 + r) * h  # (sqrt2 + 1) / 2, (2 + sqrt2) / 2
+        P = lambda o, *cols: ("prism", o, cols)
+        Y = lambda o, *cols: ("pyr", o, cols)
+        T3 = lambda o, *cols: ("tri", o, cols)
+        B3 = lambda o, cols, dv=None: ("box", o, cols, dv)
+        # slab ends shared by sdom 00/01 and 40/41, 02 and 39, nodes
+        e0 = ((r * t, 0, 0), (s / 4 - (2 + r) * h * b - (2 - r) * h * t, s / 4 - (2 + r) * h * (b + t), 0),
+              (s / 4 - (2 + r) * h * b - t, s / 4 - (2 + r) * h * b - t, 0))
+        e3 = (((r + 1) * t, 0, 0), ((r + 1) * t, t, 0), (t, t, 0))
+        e6 = ((r * t, 0, 0), (q1 * b + (r + 1) * t, 0, -q1 * b - t), (q1 * b + q2 * t, 0, -q1 * b - q2 * t))
+        e10 = (((r - 1) * h * b + t / r, 0, -(r - 1) * h * b - t / r), ((r - 1) * h * b, 0, -(r - 1) * h * b - r * t),
+               (0, 0, -r * t))
+        up = (-s / 4 + a / 2 + q1 * b + q2 * t, 0, s / 4 - a / 2 - q1 * b - q2 * t)  # strut axis, top
+        dn = (s / 4 - a / 2 - q1 * b - q2 * t, 0, -s / 4 + a / 2 + q1 * b + q2 * t)  # strut axis, bottom
+        e30 = ((-(r - 1) * h * b - t / r, 0, (r - 1) * h * b + t / r), (-(r - 1) * h * b, 0, (r - 1) * h * b + r * t),
+               (0, 0, r * t))
+        e34 = ((-r * t, 0, 0), (-q1 * b - (r + 1) * t, 0, q1 * b + t), (-q1 * b - q2 * t, 0, q1 * b + q2 * t))
+        e37 = ((-(r + 1) * t, 0, 0), (-(r + 1) * t, t, 0), (-t, t, 0))
+        e40 = ((-r * t, 0, 0), (-s / 4 + (2 + r) * h * b + (2 - r) * h * t, s / 4 - (2 + r) * h * (b + t), 0),
+               (-s / 4 + (2 + r) * h * b + t, s / 4 - (2 + r) * h * b - t, 0))
+        ts = t / r
+        dv = lambda i, j, k: (v[i], v[j], v[k])
+        spec = [
+            P(((r + 1) * b + t, b + t, -a), (0, 0, a), *e0),                                       # 00
+            P(((r + 1) * b + t, b + t, -a - t), (0, 0, t), *e0),                                   # 01
+            P((b + t, b + t, -a - t), (0, 0, t), (r * b, 0, 0),
+              (s / 4 - (2 - r) * h * b - t, s / 4 - (2 + r) * h * b - t, 0), (s / 4 - b - t, s / 4 - b - t, 0)),  # 02
+            P(((r + 1) * b, b, -a), (0, 0, a), *e3),                                               # 03
+            P(((r + 1) * b, b, -a - t), (0, 0, t), *e3),                                           # 04
+            B3((b, b, -a - t), ((0, 0, t), (r * b, 0, 0), (t, t, 0))),                            # 05
+            P((a, 0, 0), (0, b, 0), *e6),                                                          # 06
+            P((a, b, 0), (0, t, 0), *e6),                                                          # 07
+            P(((r + 1) * (b + t), b, 0), (0, t, 0), (a - (r + 1) * (b + t), 0, 0),
+              (a - q1 * b - t / r, 0, -q1 * b - q2 * t), (0, 0, -a - t)),                          # 08
+            P((b + t, b, -a - t), (0, t, 0), (r * (b + t), 0, 0),
+              ((r - 1) * h * b + t / r, 0, -q1 * b - t / r), (0, 0, -b)),                          # 09
+            P((b + t, b, -a - b - t), (0, t, 0), *e10),                                            # 10
+            P((b + t, 0, -a - b - t), (0, b, 0), *e10),                                            # 11
+            T3((b + t, b, -a - b), (0, t, 0), (-t, 0, 0), (0, 0, b - t)),                         # 12
+            Y((b + t, b, -a - b - t), (-t, 0, t), (0, 0, t), (0, t, t), (0, t, 0)),               # 13
+            T3((b + t, b, -a - b - (r + 1) * t), (0, t, 0), (-t, 0, t), (0, 0, r * t)),           # 14
+            P((b + t, 0, -a - b - (r + 1) * t), (0, 0, r * t), (0, b, 0), (-t, b, t), (-b - t, 0, b + t)),  # 15
+            B3((s / 4 + a / 2, 0, -s / 4 + a / 2), ((ts, 0, ts), (0, b, 0), up), dv(3, 2, 0)),    # 16
+            B3((s / 4 + a / 2, b, -s / 4 + a / 2), ((ts, 0, ts), (0, t, 0), up), dv(3, 3, 0)),    # 17
+            B3((s / 4 - a / 2, b, -s / 4 - a / 2), ((a, 0, a), (0, t, 0), up), dv(1, 3, 0)),      # 18
+            B3((s / 4 - a / 2 - ts, b, -s / 4 - a / 2 - ts), ((ts, 0, ts), (0, t, 0), up), dv(3, 3, 0)),  # 19
+            B3((s / 4 - a / 2 - ts, 0, -s / 4 - a / 2 - ts), ((ts, 0, ts), (0, b, 0), up), dv(3, 2, 0)),  # 20
+            B3((s / 4 + a / 2 + ts, 0, -s / 4 + a / 2 + ts), ((-ts, 0, -ts), (0, b, 0), dn), dv(3, 2, 0)),  # 21
+            B3((s / 4 + a / 2 + ts, b, -s / 4 + a / 2 + ts), ((-ts, 0, -ts), (0, t, 0), dn), dv(3, 3, 0)),  # 22
+            B3((s / 4 + a / 2, b, -s / 4 + a / 2), ((-a, 0, -a), (0, t, 0), dn), dv(1, 3, 0)),    # 23
+            B3((s / 4 - a / 2, b, -s / 4 - a / 2), ((-ts, 0, -ts), (0, t, 0), dn), dv(3, 3, 0)),  # 24
+            B3((s / 4 - a / 2, 0, -s / 4 - a / 2), ((-ts, 0, -ts), (0, b, 0), dn), dv(3, 2, 0)),  # 25
+            P((s / 2 - b - t, 0, -s / 2 + a + b + (r + 1) * t), (0, 0, -r * t), (0, b, 0), (t, b, -t),
+              (b + t, 0, -b - t)),                                                                 # 26
+            T3((s / 2 - b - t, b, -s / 2 + a + b + (r + 1) * t), (0, t, 0), (t, 0, -t), (0, 0, -r * t)),  # 27
+            Y((s / 2 - b - t, b, -s / 2 + a + b + t), (t, 0, -t), (0, 0, -t), (0, t, -t), (0, t, 0)),     # 28
+            T3((s / 2 - b - t, b, -s / 2 + a + b), (0, t, 0), (t, 0, 0), (0, 0, -b + t)),         # 29
+            P((s / 2 - b - t, 0, -s / 2 + a + b + t), (0, b, 0), *e30),                           # 30
+            P((s / 2 - b - t, b, -s / 2 + a + b + t), (0, t, 0), *e30),                           # 31
+            P((s / 2 - b - t, b, -s / 2 + a + t), (0, t, 0), (-r * (b + t), 0, 0),
+              (-(r - 1) * h * b - t / r, 0, q1 * b + t / r), (0, 0, b)),                           # 32
+            P((s / 2 - (r + 1) * (b + t), b, -s / 2), (0, t, 0), (-a + (r + 1) * (b + t), 0, 0),
+              (-a + q1 * b + t / r, 0, q1 * b + q2 * t), (0, 0, a + t)),                           # 33
+            P((s / 2 - a, b, -s / 2), (0, t, 0), *e34),                                            # 34
+            P((s / 2 - a, 0, -s / 2), (0, b, 0), *e34),                                            # 35
+            B3((s / 2 - b, b, -s / 2 + a + t), ((0, 0, -t), (-r * b, 0, 0), (-t, t, 0))),         # 36
+            P((s / 2 - (r + 1) * b, b, -s / 2 + a + t), (0, 0, -t), *e37),                         # 37
+            P((s / 2 - (r + 1) * b, b, -s / 2 + a), (0, 0, -a), *e37),                             # 38
+            P((s / 2 - b - t, b + t, -s / 2 + a + t), (0, 0, -t), (-r * b, 0, 0),
+              (-s / 4 + (2 - r) * h * b + t, s / 4 - (2 + r) * h * b - t, 0), (-s / 4 + b + t, s / 4 - b - t, 0)),  # 39
+            P((s / 2 - (r + 1) * b - t, b + t, -s / 2 + a + t), (0, 0, -t), *e40),                 # 40
+            P((s / 2 - (r + 1) * b - t, b + t, -s / 2 + a), (0, 0, -a), *e40),                     # 41
+        ]
+        ppeds = []
+        for i, sp in enumerate(spec):
+            kinds = self.KINDS[i]
+            o = np.array(sp[1], dtype=np.float64)
+            if sp[0] == "box":
+                M = np.array(sp[2], dtype=np.float64).T
+                dvs = sp[3]
+                if dvs is None:
+                    ppeds.append(Parallelepiped(o, M, np.array([-1, -1, -1]), z.copy(), kinds))
+                else:
+                    ppeds.append(Parallelepiped(o, M, np.array(dvs), g.copy(), kinds))
+            elif sp[0] == "tri":
+                M = np.array(sp[2], dtype=np.float64).T
+                ppeds.append(TriangularPrism(o, M, np.array([-1, -1, -1]), z.copy(), kinds))
+            else:
+                mat = np.array(sp[2], dtype=np.float64).T
+                cls = Prism if sp[0] == "prism" else Pyramid
+                ppeds.append(cls(o, mat, -1, z.copy(), kinds))
+        R = np.diag([-1.0, 1.0, 1.0])
+        tr = np.array([s / 2, 0.0, -s / 2])
+        pairs = [Pair(INTER, *q) for q in self.INTER_PAIRS]
+        pairs += [Pair(PERI, *q, transl=tr, rot=R) for q in self.PERI_PAIRS]
+        super().__init__(ppeds, pairs)
+
+    @classmethod
+    def from_cli(cls, d0, d1, d2, d3, v0, v1, v2, v3, dT):
+        return cls((d0, d1, d2, d3), (v0, v1, v2, v3), dT)
+
+    def average(self, field, cell_volumes):
+        """OctetDomain::average (montecarlo/domain.cpp:1252-1280): the
+        rows of `field` averaged over the cells of the vertical struts
+        16-25 whose third index is 0, weighted by cell volume."""
+        field = np.asarray(field)
+        w = np.zeros(field.shape[1])
+        col = 0
+        for i, p in enumerate(self.ppeds):
+            sh = p.shape()
+            n = int(np.prod(sh))
+            if n and i in self.AVERAGED:
+                first = int(sh[0] * sh[1])  # index(2) == 0: the first layer
+                w[col:col + first] = cell_volumes[col:col + first]
+            col += n
+        return (field * w).sum(axis=1) / w.sum()

@@ -57,4 +57,5 @@ def cases():
         "tube": (D.TubeDomain.from_cli(1e-7, 5e-8, 2e-8, 5, 3), M.MULTI, 1500, 0.5e-12, 400),
         "hex": (D.HexDomain.from_cli(1e-7, 4e-8), M.MULTI, 1500, 0.5e-12, 400),
         "jct": (D.JctDomain((5e-8, 5e-8, 5e-8, 4e-8), (4, 3, 3, 0), 1e-1), M.MULTI, 1500, 0.5e-12, 400),
+        "octet": (D.OctetDomain((3e-7, 5e-8, 5e-8, 5e-9), (4, 3, 2, 2), 1e-1), M.MULTI, 2000, 0.5e-12, 400),
     }

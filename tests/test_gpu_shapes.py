@@ -15,7 +15,23 @@ subdomain's frame coordinates and the oracle in physical ones: the two
 FP64 roundings differ by ~1e-23 m, which a nearly grazing flight turns
 into ~1e-11 of the domain size along the face; measured worst 2.5e-11.)
 Cells of zero volume (outside a Tetrahedron or TriangularPrism) are NaN
-in both, as the reference's division makes them."""
+in both, as the reference's division makes them.
+
+OctetDomain: every count identical and the logged trajectories identical
+in FP64, the field within 1e-6 (its struts are sheared parallelepipeds with
+3-D cells: the kernels walk cell crossings in reduced coordinates, the
+oracle sorts physical crossing parameters, and a flight that grazes a cell
+edge splits its path differently between the two cells; measured 2.3e-7
+with 2000 phonons, 4e-10 with 200); FP32 with up to 6 of the 96 logged
+trajectories differing and positions within 5e-3 of the cell size for 99 %
+of the events, 2e-2 for all (0.22 wall events per phonon-step on 5 nm
+struts in a 300 nm cell, each adding FP32 rounding; measured 6.7e-4 and
+2.5e-3). Its diverged FP32 trajectories make the FP32 field another
+sample of the same statistics: the strut average (OctetDomain::average) is
+compared with the FP64 one against the seed-to-seed spread instead."""
+FIELD_TOL64 = {"octet": 1e-6}
+MISMATCH32 = {"octet": 6}
+POS32 = {"octet": (5e-3, 2e-2)}
 
 import numpy as np
 import pytest
@@ -68,14 +84,25 @@ def test_fp64_trajectories_and_field(name, K, gmat, omat):
         if n:
             worst = max(worst, float((np.abs(t0 - t1) / np.abs(t0)).max()))
     assert worst < 1e-9, worst
-    assert field_err_nan(oo, go) < 1e-9
+    assert field_err_nan(oo, go) < FIELD_TOL64.get(name, 1e-9)
 
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_fp32_trajectories_and_field(name, gmat, omat):
     dom, (oo, ost, olog), (go, gst, glog) = run(gmat, omat, name, 32, 50)
-    compare_logs(olog, glog, dom.max_dim(), 1e-4, allow_mismatch=1, pos_quantile=0.99, pos_cap=1e-2)
-    assert field_err_nan(oo, go) < 1e-2
+    q, cap = POS32.get(name, (1e-4, 1e-2))
+    compare_logs(olog, glog, dom.max_dim(), q, allow_mismatch=MISMATCH32.get(name, 1), pos_quantile=0.99,
+                 pos_cap=cap)
+    if name != "octet":
+        assert field_err_nan(oo, go) < 1e-2
+        return
+    _, kind, nemit, dt, nsteps = CASES[name]
+    P = PROBLEM[kind](gmat, dom, nemit, 10**6)
+    cv = P.handle.cell_volumes()
+    avg = lambda f: dom.average(f, cv)
+    a64 = [avg(P.solve(dt=dt, nsteps=nsteps, seed=sd, precision=64, steps_per_launch=50)) for sd in (7, 8, 9, 10)]
+    spread = np.std(np.array(a64), axis=0, ddof=1)
+    assert (np.abs(avg(go) - a64[0]) < 4 * spread).all(), (avg(go), a64[0], spread)
 
 
 def test_batch_of_shapes_equals_single_solves_fp64(gmat):

@@ -92,11 +92,11 @@ def test_prism_and_pyramid_volumes_follow_the_reference():
 
 def test_library_refuses_what_the_kernels_do_not_take():
     """HexDomain's Prism<6> (eight faces) and JctDomain (one Inter face
-    paired with two others) take a continuation slot each; more than 32
+    paired with two others) take a continuation slot each; more than 64
     slots in all is MC_ERR_UNSUPPORTED, which the oracle does not limit."""
     hexp = D.HexDomain.from_cli(1e-7, 5e-8).ppeds[0]
     ppeds, pairs = [], []
-    for i in range(17):
+    for i in range(33):
         ppeds.append(D.Prism(hexp.o + np.array([0.0, 3e-7 * i, 0.0]), hexp.mat, 0, hexp.gradT, hexp.kinds))
         pairs.append(D.Pair(D.PERI, i, 0, i, 1, np.array([1e-7, 0.0, 0.0])))
     dom = D.Domain(ppeds, pairs)
@@ -115,3 +115,48 @@ def test_library_and_oracle_agree_on_columns_and_weights():
         assert h.cols == od.cols, name
         cv = od.cell_volumes()
         assert np.array_equal(h.cell_volumes(), cv), name
+
+
+def test_octet_domain_assembles_and_averages():
+    """OctetDomain: 42 subdomains whose Inter and Peri pairs pass the
+    makePair checks (the library refuses mismatched planes); its field
+    columns are the ten struts' cells, and average() weights the first cell
+    layer of struts 16-25 by cell volume (montecarlo/domain.cpp:1252-1280)."""
+    dom = D.OctetDomain((3e-7, 5e-8, 5e-8, 5e-9), (4, 3, 2, 2), 1e-1)
+    assert len(dom.ppeds) == 42
+    h = M.problem.DomainHandle(dom)
+    od = O.ODomain(dom)
+    assert h.cols == od.cols == dom.cols() == 176
+    cv = h.cell_volumes()
+    assert np.array_equal(cv, od.cell_volumes())
+    f = np.vstack([np.ones(h.cols), np.arange(h.cols, dtype=float)])
+    avg = dom.average(f, cv)
+    assert avg[0] == pytest.approx(1.0)
+    # by hand: the first layer of each strut
+    num = den = 0.0
+    col = 0
+    for i, p in enumerate(dom.ppeds):
+        n = int(np.prod(p.shape()))
+        if n and 16 <= i < 26:
+            k = int(p.shape()[0] * p.shape()[1])
+            num += float((cv[col:col + k] * np.arange(col, col + k)).sum())
+            den += float(cv[col:col + k].sum())
+        col += n
+    assert avg[1] == pytest.approx(num / den)
+
+
+def test_makepair_checks():
+    """makePair refuses Inter faces whose planes differ (montecarlo/
+    boundary.cpp:363-368) and Peri maps that do not carry one face onto the
+    other (boundary.cpp:527-535)."""
+    box = lambda o: D._pped(o, (1e-7, 1e-7, 1e-7), (0, 0, 0), (0, 0, 0), (D.INTER, D.SPEC, D.SPEC, D.SPEC, D.SPEC, D.SPEC))
+    box2 = lambda o: D._pped(o, (1e-7, 1e-7, 1e-7), (0, 0, 0), (0, 0, 0), (D.SPEC, D.SPEC, D.SPEC, D.INTER, D.SPEC, D.SPEC))
+    ok = D.Domain([box((1e-7, 0, 0)), box2((0, 0, 0))], [D.Pair(D.INTER, 0, 0, 1, 3)])
+    M.problem.DomainHandle(ok)
+    gap = D.Domain([box((1.1e-7, 0, 0)), box2((0, 0, 0))], [D.Pair(D.INTER, 0, 0, 1, 3)])
+    with pytest.raises(M._lib.McError):
+        M.problem.DomainHandle(gap)
+    film = D.FilmDomain.from_cli(1e-7, 1e-7, 4)
+    film.pairs[0].transl = np.array([1.2e-7, 0.0, 0.0])
+    with pytest.raises(M._lib.McError):
+        M.problem.DomainHandle(film)
