@@ -14,7 +14,9 @@
 #ifndef MC_GB300_HPP
 #define MC_GB300_HPP
 
+#include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -245,6 +247,179 @@ public:
         pairs_.push_back(peri(0, 0, 0, 3, t));
         pairs_.push_back(peri(1, 0, 1, 3, t));
         pairs_.push_back(peri(2, 0, 2, 3, t));
+    }
+};
+
+// OctetDomain: one octet-truss cell of 42 subdomains (montecarlo/domain.cpp:
+// 591-1238, types montecarlo/domain.h:298-344); dim = (s, d1, d2, t), div =
+// (div0 .. div3). average() is OctetDomain::average
+// (montecarlo/domain.cpp:1252-1280).
+class OctetDomain : public Domain {
+public:
+    OctetDomain(const double dim[4], const long div[4], double dT) {
+        using C = std::array<double, 3>;
+        const double r = std::sqrt(2.), h = 0.5, pi = 3.141592653589793;
+        const double s = dim[0], t = dim[3];
+        const double a = pi / 5. * (dim[1] + dim[2]) - (4. - pi) / 5. * t, b = a / 4.;
+        if (!(b > t && a > (r + 1) * (b + t) && s / 2 > a + (r + 1) * (b + t) + t))
+            throw Error(MC_ERR_ARG, "Invalid dimensions");
+        const double q1 = (r + 1) * h, q2 = (2 + r) * h, ts = t / r;
+        const double den = s - 2 * a - 2 * (r + 1) * b - 2 * (2 + r) * t;
+        const double g[3] = {dT / den, 0., -dT / den}, z[3] = {0., 0., 0.};
+        const long none[3] = {-1, -1, -1};
+        const int I = MC_INTER, D = MC_DIFF, S = MC_SPEC, P = MC_PERI;
+        const std::vector<std::vector<int>> kinds = {
+            {I, P, I, D, S, D}, {D, I, I, D, S, I}, {D, D, I, I, S, S}, {I, P, D, I, I, D}, {I, I, D, I, I, I},
+            {I, S, D, D, I, I}, {S, I, P, D, I, D}, {I, D, P, D, I, I}, {D, D, P, I, I, I}, {D, D, I, I, I, I},
+            {I, D, I, I, D, I}, {S, I, D, I, D, I}, {D, I, I, S, I}, {I, D, I, S, I}, {I, I, D, S, I},
+            {D, D, I, I, S, S}, {D, S, I, D, I, I}, {I, I, I, D, D, I}, {I, D, I, I, D, I}, {D, I, I, I, D, I},
+            {D, S, I, D, I, I}, {D, S, I, D, I, I}, {D, I, I, I, D, I}, {I, D, I, I, D, I}, {I, I, I, D, D, I},
+            {D, S, I, D, I, I}, {D, D, I, I, S, S}, {I, I, D, S, I}, {I, D, I, S, I}, {D, I, I, S, I},
+            {S, I, D, I, D, I}, {I, D, I, I, D, I}, {D, D, I, I, I, I}, {D, D, P, I, I, I}, {I, D, P, D, I, I},
+            {S, I, P, D, I, D}, {I, S, D, D, I, I}, {I, I, D, I, I, I}, {I, P, D, I, I, D}, {D, D, I, I, S, S},
+            {D, I, I, D, S, I}, {I, P, I, D, S, D}};
+        const std::vector<C> e0 = {C{r * t, 0, 0},
+                                   C{s / 4 - (2 + r) * h * b - (2 - r) * h * t, s / 4 - (2 + r) * h * (b + t), 0},
+                                   C{s / 4 - (2 + r) * h * b - t, s / 4 - (2 + r) * h * b - t, 0}};
+        const std::vector<C> e3 = {C{(r + 1) * t, 0, 0}, C{(r + 1) * t, t, 0}, C{t, t, 0}};
+        const std::vector<C> e6 = {C{r * t, 0, 0}, C{q1 * b + (r + 1) * t, 0, -q1 * b - t},
+                                   C{q1 * b + q2 * t, 0, -q1 * b - q2 * t}};
+        const std::vector<C> e10 = {C{(r - 1) * h * b + t / r, 0, -(r - 1) * h * b - t / r},
+                                    C{(r - 1) * h * b, 0, -(r - 1) * h * b - r * t}, C{0, 0, -r * t}};
+        const C up{-s / 4 + a / 2 + q1 * b + q2 * t, 0, s / 4 - a / 2 - q1 * b - q2 * t};
+        const C dn{s / 4 - a / 2 - q1 * b - q2 * t, 0, -s / 4 + a / 2 + q1 * b + q2 * t};
+        const std::vector<C> e30 = {C{-(r - 1) * h * b - t / r, 0, (r - 1) * h * b + t / r},
+                                    C{-(r - 1) * h * b, 0, (r - 1) * h * b + r * t}, C{0, 0, r * t}};
+        const std::vector<C> e34 = {C{-r * t, 0, 0}, C{-q1 * b - (r + 1) * t, 0, q1 * b + t},
+                                    C{-q1 * b - q2 * t, 0, q1 * b + q2 * t}};
+        const std::vector<C> e37 = {C{-(r + 1) * t, 0, 0}, C{-(r + 1) * t, t, 0}, C{-t, t, 0}};
+        const std::vector<C> e40 = {C{-r * t, 0, 0},
+                                    C{-s / 4 + (2 + r) * h * b + (2 - r) * h * t, s / 4 - (2 + r) * h * (b + t), 0},
+                                    C{-s / 4 + (2 + r) * h * b + t, s / 4 - (2 + r) * h * b - t, 0}};
+        auto cat = [](C c0, const std::vector<C>& rest) {
+            std::vector<C> v{c0};
+            v.insert(v.end(), rest.begin(), rest.end());
+            return v;
+        };
+        int k = 0;
+        auto prism = [&](C o, std::vector<C> cols, int shape = MC_PRISM) {
+            sdoms_.push_back(sdom(shape, o.data(), cols, none, z, kinds[k], {}));
+            ++k;
+        };
+        auto box = [&](C o, std::vector<C> cols, const long* dv = nullptr) {
+            sdoms_.push_back(sdom(MC_PARALLELEPIPED, o.data(), cols, dv ? dv : none, dv ? g : z, kinds[k], {}));
+            ++k;
+        };
+        auto tri = [&](C o, std::vector<C> cols) {
+            sdoms_.push_back(sdom(MC_TRIANGULAR_PRISM, o.data(), cols, none, z, kinds[k], {}));
+            ++k;
+        };
+        const long v320[3] = {div[3], div[2], div[0]}, v330[3] = {div[3], div[3], div[0]},
+                   v130[3] = {div[1], div[3], div[0]};
+        prism({(r + 1) * b + t, b + t, -a}, cat({0, 0, a}, e0));                                        // 00
+        prism({(r + 1) * b + t, b + t, -a - t}, cat({0, 0, t}, e0));                                    // 01
+        prism({b + t, b + t, -a - t}, {{0, 0, t}, {r * b, 0, 0},
+              {s / 4 - (2 - r) * h * b - t, s / 4 - (2 + r) * h * b - t, 0}, {s / 4 - b - t, s / 4 - b - t, 0}});  // 02
+        prism({(r + 1) * b, b, -a}, cat({0, 0, a}, e3));                                                // 03
+        prism({(r + 1) * b, b, -a - t}, cat({0, 0, t}, e3));                                            // 04
+        box({b, b, -a - t}, {{0, 0, t}, {r * b, 0, 0}, {t, t, 0}});                                     // 05
+        prism({a, 0, 0}, cat({0, b, 0}, e6));                                                           // 06
+        prism({a, b, 0}, cat({0, t, 0}, e6));                                                           // 07
+        prism({(r + 1) * (b + t), b, 0}, {{0, t, 0}, {a - (r + 1) * (b + t), 0, 0},
+              {a - q1 * b - t / r, 0, -q1 * b - q2 * t}, {0, 0, -a - t}});                              // 08
+        prism({b + t, b, -a - t}, {{0, t, 0}, {r * (b + t), 0, 0}, {(r - 1) * h * b + t / r, 0, -q1 * b - t / r},
+              {0, 0, -b}});                                                                             // 09
+        prism({b + t, b, -a - b - t}, cat({0, t, 0}, e10));                                             // 10
+        prism({b + t, 0, -a - b - t}, cat({0, b, 0}, e10));                                             // 11
+        tri({b + t, b, -a - b}, {{0, t, 0}, {-t, 0, 0}, {0, 0, b - t}});                                // 12
+        prism({b + t, b, -a - b - t}, {{-t, 0, t}, {0, 0, t}, {0, t, t}, {0, t, 0}}, MC_PYRAMID);       // 13
+        tri({b + t, b, -a - b - (r + 1) * t}, {{0, t, 0}, {-t, 0, t}, {0, 0, r * t}});                  // 14
+        prism({b + t, 0, -a - b - (r + 1) * t}, {{0, 0, r * t}, {0, b, 0}, {-t, b, t}, {-b - t, 0, b + t}});  // 15
+        box({s / 4 + a / 2, 0, -s / 4 + a / 2}, {{ts, 0, ts}, {0, b, 0}, up}, v320);                    // 16
+        box({s / 4 + a / 2, b, -s / 4 + a / 2}, {{ts, 0, ts}, {0, t, 0}, up}, v330);                    // 17
+        box({s / 4 - a / 2, b, -s / 4 - a / 2}, {{a, 0, a}, {0, t, 0}, up}, v130);                      // 18
+        box({s / 4 - a / 2 - ts, b, -s / 4 - a / 2 - ts}, {{ts, 0, ts}, {0, t, 0}, up}, v330);          // 19
+        box({s / 4 - a / 2 - ts, 0, -s / 4 - a / 2 - ts}, {{ts, 0, ts}, {0, b, 0}, up}, v320);          // 20
+        box({s / 4 + a / 2 + ts, 0, -s / 4 + a / 2 + ts}, {{-ts, 0, -ts}, {0, b, 0}, dn}, v320);        // 21
+        box({s / 4 + a / 2 + ts, b, -s / 4 + a / 2 + ts}, {{-ts, 0, -ts}, {0, t, 0}, dn}, v330);        // 22
+        box({s / 4 + a / 2, b, -s / 4 + a / 2}, {{-a, 0, -a}, {0, t, 0}, dn}, v130);                    // 23
+        box({s / 4 - a / 2, b, -s / 4 - a / 2}, {{-ts, 0, -ts}, {0, t, 0}, dn}, v330);                  // 24
+        box({s / 4 - a / 2, 0, -s / 4 - a / 2}, {{-ts, 0, -ts}, {0, b, 0}, dn}, v320);                  // 25
+        prism({s / 2 - b - t, 0, -s / 2 + a + b + (r + 1) * t}, {{0, 0, -r * t}, {0, b, 0}, {t, b, -t},
+              {b + t, 0, -b - t}});                                                                     // 26
+        tri({s / 2 - b - t, b, -s / 2 + a + b + (r + 1) * t}, {{0, t, 0}, {t, 0, -t}, {0, 0, -r * t}});  // 27
+        prism({s / 2 - b - t, b, -s / 2 + a + b + t}, {{t, 0, -t}, {0, 0, -t}, {0, t, -t}, {0, t, 0}},
+              MC_PYRAMID);                                                                              // 28
+        tri({s / 2 - b - t, b, -s / 2 + a + b}, {{0, t, 0}, {t, 0, 0}, {0, 0, -b + t}});                // 29
+        prism({s / 2 - b - t, 0, -s / 2 + a + b + t}, cat({0, b, 0}, e30));                             // 30
+        prism({s / 2 - b - t, b, -s / 2 + a + b + t}, cat({0, t, 0}, e30));                             // 31
+        prism({s / 2 - b - t, b, -s / 2 + a + t}, {{0, t, 0}, {-r * (b + t), 0, 0},
+              {-(r - 1) * h * b - t / r, 0, q1 * b + t / r}, {0, 0, b}});                               // 32
+        prism({s / 2 - (r + 1) * (b + t), b, -s / 2}, {{0, t, 0}, {-a + (r + 1) * (b + t), 0, 0},
+              {-a + q1 * b + t / r, 0, q1 * b + q2 * t}, {0, 0, a + t}});                               // 33
+        prism({s / 2 - a, b, -s / 2}, cat({0, t, 0}, e34));                                             // 34
+        prism({s / 2 - a, 0, -s / 2}, cat({0, b, 0}, e34));                                             // 35
+        box({s / 2 - b, b, -s / 2 + a + t}, {{0, 0, -t}, {-r * b, 0, 0}, {-t, t, 0}});                  // 36
+        prism({s / 2 - (r + 1) * b, b, -s / 2 + a + t}, cat({0, 0, -t}, e37));                          // 37
+        prism({s / 2 - (r + 1) * b, b, -s / 2 + a}, cat({0, 0, -a}, e37));                              // 38
+        prism({s / 2 - b - t, b + t, -s / 2 + a + t}, {{0, 0, -t}, {-r * b, 0, 0},
+              {-s / 4 + (2 - r) * h * b + t, s / 4 - (2 + r) * h * b - t, 0}, {-s / 4 + b + t, s / 4 - b - t, 0}});  // 39
+        prism({s / 2 - (r + 1) * b - t, b + t, -s / 2 + a + t}, cat({0, 0, -t}, e40));                  // 40
+        prism({s / 2 - (r + 1) * b - t, b + t, -s / 2 + a}, cat({0, 0, -a}, e40));                      // 41
+        const int ip[][4] = {
+            {0, 0, 1, 1}, {1, 5, 2, 3}, {0, 2, 3, 4}, {1, 2, 4, 4}, {2, 2, 5, 5}, {3, 0, 4, 1}, {4, 5, 5, 4},
+            {3, 3, 8, 5}, {4, 3, 8, 5}, {4, 0, 9, 2}, {5, 0, 9, 2}, {5, 0, 12, 4},
+            {6, 1, 7, 0}, {7, 5, 8, 3}, {9, 4, 10, 2}, {10, 0, 11, 1}, {9, 5, 12, 1}, {9, 5, 13, 0}, {10, 5, 14, 1},
+            {11, 5, 15, 2}, {12, 2, 13, 2}, {13, 4, 14, 4}, {14, 0, 15, 3},
+            {6, 4, 16, 5}, {7, 4, 17, 5}, {8, 4, 18, 5}, {9, 3, 18, 5}, {10, 3, 19, 5}, {11, 3, 20, 5},
+            {16, 4, 17, 1}, {17, 0, 18, 3}, {18, 0, 19, 3}, {19, 1, 20, 4},
+            {16, 2, 21, 2}, {17, 2, 22, 2}, {18, 2, 23, 2}, {19, 2, 24, 2}, {20, 2, 25, 2},
+            {21, 4, 22, 1}, {22, 3, 23, 0}, {23, 3, 24, 0}, {24, 1, 25, 4},
+            {21, 5, 30, 3}, {22, 5, 31, 3}, {23, 5, 32, 3}, {23, 5, 33, 4}, {24, 5, 34, 4}, {25, 5, 35, 4},
+            {26, 3, 27, 0}, {27, 4, 28, 4}, {28, 2, 29, 2}, {26, 2, 30, 5}, {27, 1, 31, 5}, {28, 0, 32, 5},
+            {29, 1, 32, 5}, {30, 1, 31, 0}, {31, 2, 32, 4}, {33, 3, 34, 5}, {34, 0, 35, 1},
+            {29, 4, 36, 0}, {32, 2, 36, 0}, {32, 2, 37, 0}, {33, 5, 37, 3}, {33, 5, 38, 3},
+            {36, 4, 37, 5}, {37, 1, 38, 0}, {36, 5, 39, 2}, {37, 4, 40, 2}, {38, 4, 41, 2}, {39, 3, 40, 5},
+            {40, 1, 41, 0}};
+        for (const auto& q : ip) pairs_.push_back(inter(q[0], q[1], q[2], q[3]));
+        const int pp[][4] = {{0, 1, 41, 1}, {3, 1, 38, 1}, {6, 2, 35, 2}, {7, 2, 34, 2}, {8, 2, 33, 2}};
+        const double tr[3] = {s / 2, 0., -s / 2};
+        for (const auto& q : pp) {
+            mc_pair_desc x = peri(q[0], q[1], q[2], q[3], tr);
+            x.rot[0] = -1.;
+            pairs_.push_back(x);
+        }
+    }
+    // OctetDomain::average: the rows averaged over the struts 16-25's
+    // first cell layer (third index 0), weighted by cell volume; field is
+    // rows x cols column-major.
+    std::vector<double> average(const std::vector<double>& field, long rows) const {
+        const std::vector<double> cv = cellVolumes();
+        std::vector<double> out((size_t)rows, 0.);
+        double wsum = 0.;
+        long col = 0;
+        for (size_t i = 0; i < sdoms_.size(); ++i) {
+            const mc_sdom_desc& p = sdoms_[i];
+            long n = 0, first = 0;
+            if (p.shape == MC_PARALLELEPIPED && p.div[0] >= 0 && p.div[1] >= 0 && p.div[2] >= 0) {
+                const long s0 = std::max(p.div[0], 1L), s1 = std::max(p.div[1], 1L), s2 = std::max(p.div[2], 1L);
+                n = s0 * s1 * s2;
+                first = s0 * s1;
+            } else if ((p.shape == MC_PRISM || p.shape == MC_PYRAMID) && p.div[0] >= 0) {
+                n = 1;
+            } else if ((p.shape == MC_TRIANGULAR_PRISM || p.shape == MC_TETRAHEDRON) && p.div[0] >= 0 &&
+                       p.div[1] >= 0 && p.div[2] >= 0) {
+                n = std::max(p.div[0], 1L) * std::max(p.div[1], 1L) * std::max(p.div[2], 1L);
+            }
+            if (i >= 16 && i < 26)
+                for (long c = col; c < col + first; ++c) {
+                    wsum += cv[(size_t)c];
+                    for (long r = 0; r < rows; ++r) out[(size_t)r] += field[(size_t)(c * rows + r)] * cv[(size_t)c];
+                }
+            col += n;
+        }
+        for (double& x : out) x /= wsum;
+        return out;
     }
 };
 

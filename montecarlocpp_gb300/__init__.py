@@ -10,7 +10,7 @@ from .batch import Batch
 from .serve import Server
 from .domains import (BAC, BOT, DIFF, FRO, INTER, ISOT, LEF, PARALLELEPIPED, PERI, PRISM, PYRAMID, RIG, SPEC,
                       TETRAHEDRON, TOP, TRIANGULAR_PRISM, BulkDomain, CrossPlaneFilmDomain, Domain, FilmDomain,
-                      HexDomain, JctDomain, Pair, Parallelepiped, PoreCellDomain, Prism, PyrDomain, Pyramid,
+                      HexDomain, JctDomain, OctetDomain, Pair, Parallelepiped, PoreCellDomain, Prism, PyrDomain, Pyramid,
                       TeeDomain, Tetrahedron, TriangularPrism, TubeDomain)
 from .materials import SiliconModel, silicon_tables, write_material_files
 from .problem import (CUMFLUX, CUMTEMP, FLUX, MULTI, TEMP, CumFluxProblem, CumTempProblem, FluxProblem,
@@ -19,7 +19,7 @@ from .problem import (CUMFLUX, CUMTEMP, FLUX, MULTI, TEMP, CumFluxProblem, CumTe
 __all__ = [
     "BAC", "LEF", "BOT", "FRO", "RIG", "TOP", "SPEC", "DIFF", "ISOT", "PERI", "INTER",
     "Domain", "FilmDomain", "BulkDomain", "CrossPlaneFilmDomain", "PoreCellDomain", "PyrDomain", "HexDomain",
-    "JctDomain", "TeeDomain", "TubeDomain", "Pair", "Parallelepiped", "TriangularPrism", "Tetrahedron", "Prism",
+    "JctDomain", "TeeDomain", "TubeDomain", "OctetDomain", "Pair", "Parallelepiped", "TriangularPrism", "Tetrahedron", "Prism",
     "Pyramid", "PARALLELEPIPED", "TRIANGULAR_PRISM", "TETRAHEDRON", "PRISM", "PYRAMID", "SiliconModel", "silicon_tables", "write_material_files", "Material",
     "TempProblem", "FluxProblem", "MultiProblem", "CumTempProblem", "CumFluxProblem", "Session", "TEMP",
     "FLUX", "MULTI", "CUMTEMP", "CUMFLUX",

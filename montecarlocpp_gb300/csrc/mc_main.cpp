@@ -107,8 +107,18 @@ int main(int argc, char** argv) {
             dim[2] = dim[1];
             div[2] = div[1];
             dom.reset(new mcgb::TubeDomain(dim, div, 1e6 * dim[0]));
+        } else if (domStr == "octet") {  // montecarlo/main.cpp:376-386
+            double dim[4];
+            long div[4];
+            double dT;
+            ss >> dim[0] >> dim[1] >> dim[2] >> dim[3] >> div[0] >> div[1] >> div[2] >> div[3] >> dT;
+            if (!(dim[0] > 0 && dim[1] > 0 && dim[2] > 0 && dim[3] > 0)) {
+                std::fprintf(stderr, "Dimensions must be positive\n");
+                return 1;
+            }
+            dom.reset(new mcgb::OctetDomain(dim, div, dT));
         } else {
-            std::fprintf(stderr, "Invalid domain (this driver serves film, bulk, hex, pyr, jct, tee and tube)\n");
+            std::fprintf(stderr, "Invalid domain (this driver serves film, bulk, hex, pyr, jct, tee, tube and octet)\n");
             return 1;
         }
         long nemit = 0, maxscat = 0, maxloop = 0, nsim = 1, size = 0;

@@ -37,7 +37,7 @@ def test_driver_fails_loudly_without_device(tmp_path):
 def test_driver_rejects_bad_arguments(tmp_path):
     M.write_material_files(str(tmp_path))
     B.build()
-    r = subprocess.run([B.MAIN, str(tmp_path), "silicon", "300", "octet", "1", "2"], capture_output=True, text=True)
+    r = subprocess.run([B.MAIN, str(tmp_path), "silicon", "300", "torus", "1", "2"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid domain" in r.stderr
     r = subprocess.run([B.MAIN, "/nonexistent/dir", "silicon", "300"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid directory" in r.stderr
@@ -85,6 +85,8 @@ def test_driver_cumflux_with_replicas(tmp_path, gmat):
     (["jct", "5e-8", "4e-8"], lambda: M.JctDomain.from_cli(5e-8, 4e-8)),
     (["tee", "5e-8", "3e-8", "4"], lambda: M.TeeDomain.from_cli(5e-8, 3e-8, 4)),
     (["tube", "1e-7", "5e-8", "2e-8", "5", "3"], lambda: M.TubeDomain.from_cli(1e-7, 5e-8, 2e-8, 5, 3)),
+    (["octet", "3e-7", "5e-8", "5e-8", "5e-9", "4", "3", "2", "2", "0.1"],
+     lambda: M.OctetDomain((3e-7, 5e-8, 5e-8, 5e-9), (4, 3, 2, 2), 0.1)),
 ])
 def test_driver_domains_match_python_binding(tmp_path, gmat, args, dom):
     """The reference's other CLI domains (montecarlo/main.cpp:320-374)
