@@ -1044,7 +1044,6 @@ int setupSession(mc_session_s* S) {
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
     S->gen = D.needGen;
-    if (S->gen && S->replay) return fail(MC_ERR_UNSUPPORTED, "replay streams take Parallelepiped domains only");
     if (!S->dyn && !S->replay && !S->logging && S->tm == TM_SHARED) {
         const int k = D.sd[0].accum;
         bool same = k >= 0 && k <= 2;

@@ -12,8 +12,8 @@ static cudaError_t prepare(K fn, size_t smem) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
-// GEN: the kernels that also take subdomains other than the Parallelepiped
-// (compiled for the non-replay launches only).
+// GEN: the kernels that also take subdomains other than the Parallelepiped,
+// continuation slots and Inter faces paired more than once.
 template <typename R, bool DYN, bool REPLAY, bool LOG, int TM, bool GEN = false>
 static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t smem, cudaStream_t s) {
     auto fn = DYN ? k_advance_dyn<R, REPLAY, LOG, TM, GEN> : k_advance<R, REPLAY, LOG, TM, -1, GEN>;
@@ -127,6 +127,18 @@ int advanceBatchOccupancy<MC_REAL>(int tm, bool gen, size_t smem, int block) {
 }
 
 #define MC_DISPATCH(F, ...)                                                                 \
+    if (gen && replay) {                                                                   \
+        if (dyn) {                                                                         \
+            if (tm == TM_SHARED) return log ? F<MC_REAL, true, true, true, TM_SHARED, true>(__VA_ARGS__)   \
+                                            : F<MC_REAL, true, true, false, TM_SHARED, true>(__VA_ARGS__);  \
+            return log ? F<MC_REAL, true, true, true, TM_GLOBAL, true>(__VA_ARGS__)           \
+                       : F<MC_REAL, true, true, false, TM_GLOBAL, true>(__VA_ARGS__);         \
+        }                                                                                  \
+        if (tm == TM_SHARED) return log ? F<MC_REAL, false, true, true, TM_SHARED, true>(__VA_ARGS__)      \
+                                        : F<MC_REAL, false, true, false, TM_SHARED, true>(__VA_ARGS__);     \
+        return log ? F<MC_REAL, false, true, true, TM_GLOBAL, true>(__VA_ARGS__)              \
+                   : F<MC_REAL, false, true, false, TM_GLOBAL, true>(__VA_ARGS__);            \
+    }                                                                                      \
     if (gen) {                                                                             \
         if (dyn) {                                                                         \
             if (tm == TM_SHARED) return log ? F<MC_REAL, true, false, true, TM_SHARED, true>(__VA_ARGS__)  \

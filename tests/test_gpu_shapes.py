@@ -177,3 +177,19 @@ def test_batch_of_shapes_fp32_graph(gmat):
         ref = p.solve(dt=dt, nsteps=nsteps, precision=32, seed=i)
         assert field_err_nan(ref, again) < 1e-5, names[i]
     B.close()
+
+
+@pytest.mark.parametrize("name", ["wedge", "pyr5", "jct", "hex"])
+def test_replay_of_reference_stream_on_shapes(name, gmat, omat):
+    """The reference's uniform scheme (mt19937 engines over static phonon
+    chunks) recorded by the oracle and replayed by the FP64 kernels on a
+    shape domain: the same trajectories and event counts."""
+    from test_gpu_parity import run_pair
+    dom, kind, nemit, dt, nsteps = CASES[name]
+    (oo, ost, olog), (go, gst, glog) = run_pair(
+        gmat, omat, dom, kind, 800, dt, 200, 64, 37, seed=0, rng=O.RNG_MT, replay="from_oracle",
+        oracle_kw=dict(nchunk=4, record_cap=8192))
+    assert gst["status"] == 0
+    assert gst["events"] == ost["events"]
+    compare_logs(olog, glog, dom.max_dim(), 1e-9)
+    assert field_err_nan(oo, go) < 1e-9
