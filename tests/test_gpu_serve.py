@@ -129,3 +129,34 @@ def test_rounds_grow_to_the_target(mats):
     srv.close()
     assert r["status"] == 0 and r["kappa_se"] <= 0.01 * abs(r["kappa"])
     assert r["rounds"] <= 4 and r["phonons"] > 20 * 2000
+
+
+def test_shape_domains_alone_and_in_the_mix(mats):
+    """Requests on the reference's hex rod and L-junction (kernels with the
+    general face code) served beside a film: each result is the same alone
+    and in the mix, and a one-round hex request equals the single solve."""
+    reqs = [
+        (mats[300.0], M.HexDomain.from_cli(1e-7, 4e-8), 30000, 5),
+        (mats[150.0], M.FilmDomain.from_cli(1e-7, 1e-7, 50), 30000, 6),
+        (mats[300.0], M.JctDomain.from_cli(1e-7, 5e-8), 30000, 7),
+    ]
+    kw = dict(dt=DT, nsteps=NSTEPS, precision=32, groups=8, target_rel_se=0.05, min_rounds=1, max_rounds=20)
+    alone = []
+    for mat, dom, n, seed in reqs:
+        srv = M.Server(**kw)
+        alone.append(srv.wait(srv.submit(mat, dom, n, seed=seed)))
+        srv.close()
+    srv = M.Server(**kw)
+    tickets = [srv.submit(mat, dom, n, seed=seed) for mat, dom, n, seed in reqs]
+    mixed = [srv.wait(t) for t in tickets]
+    srv.close()
+    for a, b in zip(alone, mixed):
+        assert a["status"] == b["status"] == 0
+        assert a["rounds"] == b["rounds"]
+        assert b["kappa"] == pytest.approx(a["kappa"], rel=1e-9)
+    dom = M.HexDomain.from_cli(1e-7, 4e-8)
+    srv = M.Server(dt=DT, nsteps=NSTEPS, precision=64, groups=4, min_rounds=1, max_rounds=1)
+    r = srv.wait(srv.submit(mats[300.0], dom, 20000, problem=M.MULTI, seed=78))
+    srv.close()
+    f = M.MultiProblem(mats[300.0], dom, 20000, 10**6).solve(dt=DT, nsteps=NSTEPS, precision=64, seed=78)
+    assert r["kappa"] == pytest.approx(M.kappa_from_flux(f, dom, 0, flux_row0=1), rel=1e-9)
