@@ -223,6 +223,8 @@ def main():
                     help="run the 64-film batch once (FP32, one graph launch) and exit")
     ap.add_argument("--profile-case", action="store_true",
                     help="one device-resident solve of the workload (for ncu), no JSON line")
+    ap.add_argument("--profile-domain", default="film", choices=["film", "hex", "pyr", "jct", "octet"],
+                    help="domain of --profile-case: the film workload or a reference domain of other shapes")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -648,7 +650,12 @@ def profile_case(args):
     import montecarlocpp_gb300 as M
     W = dict(WORKLOAD, nemit=args.nemit, nsteps=args.nsteps)
     mat = M.Material.silicon(W["T"])
-    dom = M.FilmDomain.from_cli(W["length"], W["thickness"], W["cells"])
+    doms = {"film": lambda: M.FilmDomain.from_cli(W["length"], W["thickness"], W["cells"]),
+            "hex": lambda: M.HexDomain.from_cli(1e-7, 4e-8),
+            "pyr": lambda: M.PyrDomain.from_cli(1e-7, 1e-7),
+            "jct": lambda: M.JctDomain.from_cli(1e-7, 5e-8),
+            "octet": lambda: M.OctetDomain((3e-7, 5e-8, 5e-8, 5e-9), (4, 3, 2, 2), 0.1)}
+    dom = doms[args.profile_domain]()
     prob = M.MultiProblem(mat, dom, W["nemit"], W["maxscat"])
     K = args.k or W["nsteps"]
     s = prob.session(dt=W["dt"], nsteps=W["nsteps"], precision=32, steps_per_launch=K, seed=1)
