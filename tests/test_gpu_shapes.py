@@ -108,7 +108,7 @@ def test_fp32_trajectories_and_field(name, gmat, omat):
 def test_batch_of_shapes_equals_single_solves_fp64(gmat):
     """The batched kernel over instances of different shapes (one launch)
     gives each instance's single-instance result."""
-    names = ["wedge", "tet", "prism4", "pyr5"]
+    names = ["wedge", "tet", "prism4", "pyr5", "octet"]
     probs, seeds = [], []
     for i, n in enumerate(names):
         dom, kind, nemit, dt, nsteps = CASES[n]
