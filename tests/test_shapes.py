@@ -160,3 +160,44 @@ def test_makepair_checks():
     film.pairs[0].transl = np.array([1.2e-7, 0.0, 0.0])
     with pytest.raises(M._lib.McError):
         M.problem.DomainHandle(film)
+
+
+def _random_shapes(rng):
+    """Random convex subdomains of each shape with positive volume."""
+    out = []
+    for _ in range(4):
+        M = np.diag(rng.uniform(0.5e-7, 2e-7, 3)) + rng.uniform(-2e-8, 2e-8, (3, 3))
+        div = rng.integers(1, 5, 3)
+        out.append(D.TriangularPrism(rng.uniform(-1e-7, 1e-7, 3), M, div, np.zeros(3), (D.SPEC,) * 5))
+        out.append(D.Tetrahedron(rng.uniform(-1e-7, 1e-7, 3), M, div, np.zeros(3), (D.SPEC,) * 4))
+        # a convex base polygon in the y-z plane, counter-clockwise, and an
+        # axis or apex along +x
+        n = int(rng.integers(4, 7))
+        ang = np.linspace(0, 2 * np.pi, n, endpoint=False) + rng.uniform(0, 0.3)
+        pts = np.stack([np.zeros(n), np.cos(ang), np.sin(ang)], axis=1) * 5e-8
+        base = pts[1:] - pts[0]
+        axis = np.array([1e-7, *rng.uniform(-2e-8, 2e-8, 2)])
+        mat = np.vstack([axis, base]).T
+        out.append(D.Prism(pts[0], mat, int(rng.integers(-1, 1)), np.zeros(3), (D.SPEC,) * (n + 2)))
+        apex = pts.mean(axis=0) - pts[0] + np.array([1e-7, 0, 0])
+        out.append(D.Pyramid(pts[0], np.vstack([apex, base]).T, 0, np.zeros(3), (D.SPEC,) * (n + 1)))
+    return out
+
+
+def test_random_shapes_library_matches_oracle():
+    """Random TriangularPrisms, Tetrahedra, Prisms and Pyramids: the
+    library and the oracle give the same columns and cell volumes, and the
+    oracle's emission positions (a gradient makes every shape a volume
+    emitter) lie inside."""
+    rng = np.random.default_rng(11)
+    for p in _random_shapes(rng):
+        p.gradT = np.array([-1e6, 0.0, 0.0])
+        dom = D.Domain([p], [])
+        od = O.ODomain(dom)
+        h = M.problem.DomainHandle(dom)
+        assert h.cols == od.cols
+        assert np.array_equal(h.cell_volumes(), od.cell_volumes())
+        w, sd, fc = od.emitters()
+        assert len(w) == 1 and fc[0] == -1
+        x = od.draw_positions(0, 5, 300)
+        assert all(od.is_inside(0, xi) for xi in x), type(p).__name__
