@@ -249,8 +249,9 @@ int mc_check_bounded_wait(double limit_ms, unsigned* status, double* waited_ms);
  * Arguments, output and results are those of mc_solve, except: replay
  * streams and trajectory logs are rejected (MC_ERR_UNSUPPORTED); the
  * schedule is always the in-place dynamic one (p->schedule and
- * p->compact_interval are ignored); a NULL p->stream means the legacy
- * default stream; st->kernel_ms is 0. Synchronous.
+ * p->compact_interval are validated as mc_solve validates them, then not
+ * used); a NULL p->stream means the legacy default stream; st->kernel_ms
+ * is 0. Synchronous.
  *
  * The first call on a device looks up the array's device address there
  * (which can also load this library's device code on that device): make

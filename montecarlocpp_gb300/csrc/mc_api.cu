@@ -2384,8 +2384,15 @@ struct SnapHeader {
     int32_t prec, dyn, grid, block, rows, replay;
     int64_t nemit, slots, cols;
     int32_t step, parity, launches, sinceCompact;
+    // the problem the state belongs to: a session that differs in any of
+    // these would continue on another Philox key, window or stop rule
+    int32_t problem, stepsPerLaunch;
+    int64_t nsteps, maxscat, maxloop, cumSize;
+    uint64_t seed;
+    double dt;
 };
 constexpr uint32_t SNAP_MAGIC = 0x5353434Du;  // "MCSS"
+constexpr uint32_t SNAP_VERSION = 2;
 
 struct SnapPart { void* dev; size_t bytes; };
 
@@ -2419,11 +2426,14 @@ std::vector<SnapPart> snapParts(mc_session_s* S) {
 SnapHeader snapHeader(const mc_session_s* S) {
     SnapHeader h;
     std::memset(&h, 0, sizeof(h));
-    h.magic = SNAP_MAGIC; h.version = 1;
+    h.magic = SNAP_MAGIC; h.version = SNAP_VERSION;
     h.prec = S->prec; h.dyn = S->dyn ? 1 : 0; h.grid = S->grid; h.block = S->block; h.rows = S->rows;
     h.replay = S->replay ? 1 : 0;
     h.nemit = S->nemit; h.slots = S->slots; h.cols = S->dom->cols;
     h.step = S->step; h.parity = S->parity; h.launches = S->launches; h.sinceCompact = S->sinceCompact;
+    h.problem = S->desc.problem; h.stepsPerLaunch = S->desc.steps_per_launch;
+    h.nsteps = S->desc.nsteps; h.maxscat = S->desc.maxscat; h.maxloop = S->maxloop; h.cumSize = S->desc.cum_size;
+    h.seed = S->desc.seed; h.dt = S->desc.dt;
     return h;
 }
 }  // namespace
@@ -2458,16 +2468,22 @@ int mc_session_restore(mc_session_h s, const void* buf, size_t bytes) {
     SnapHeader h;
     std::memcpy(&h, buf, sizeof(h));
     const SnapHeader mine = snapHeader(s);
-    if (h.magic != SNAP_MAGIC || h.version != 1) return fail(MC_ERR_ARG, "not a session snapshot");
+    if (h.magic != SNAP_MAGIC || h.version != SNAP_VERSION) return fail(MC_ERR_ARG, "not a session snapshot");
     if (h.prec != mine.prec || h.dyn != mine.dyn || h.grid != mine.grid || h.block != mine.block ||
         h.rows != mine.rows || h.replay != mine.replay || h.nemit != mine.nemit || h.slots != mine.slots ||
         h.cols != mine.cols)
         return fail(MC_ERR_ARG, "snapshot of a different problem or launch configuration");
+    if (h.problem != mine.problem || h.stepsPerLaunch != mine.stepsPerLaunch || h.nsteps != mine.nsteps ||
+        h.maxscat != mine.maxscat || h.maxloop != mine.maxloop || h.cumSize != mine.cumSize || h.seed != mine.seed ||
+        h.dt != mine.dt)
+        return fail(MC_ERR_ARG, "snapshot of a session with another seed, time step, horizon, window or problem");
     if (h.step < 0 || h.step > (int)s->desc.nsteps || (h.parity != 0 && h.parity != 1))
         return fail(MC_ERR_ARG, "corrupt snapshot header");
+    // the parts' sizes follow from the fields compared above, so the whole
+    // buffer is checked before anything of the session changes
+    if (bytes < mc_session_snapshot_bytes(s)) return fail(MC_ERR_ARG, "snapshot buffer too small");
     CK(cudaStreamSynchronize(s->stream));
     s->step = h.step; s->parity = h.parity; s->launches = h.launches; s->sinceCompact = h.sinceCompact;
-    if (bytes < mc_session_snapshot_bytes(s)) return fail(MC_ERR_ARG, "snapshot buffer too small");
     const char* p = (const char*)buf + sizeof(h);
     for (const SnapPart& q : snapParts(s)) {
         CK(cudaMemcpy(q.dev, p, q.bytes, cudaMemcpyHostToDevice));
@@ -2596,6 +2612,10 @@ int mc_solve_noalloc(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, d
     if (p->precision != 32 && p->precision != 64) return fail(MC_ERR_ARG, "precision must be 32 or 64");
     if (p->replay_words || p->replay_offsets || p->log)
         return fail(MC_ERR_UNSUPPORTED, "mc_solve_noalloc: replay streams and trajectory logs are not supported; use mc_solve");
+    // the descriptor is validated as mc_solve validates it, although the
+    // in-place dynamic schedule always runs here
+    if (p->schedule < MC_SCHED_AUTO || p->schedule > MC_SCHED_DYNAMIC) return fail(MC_ERR_ARG, "invalid schedule");
+    if (p->compact_interval < 0) return fail(MC_ERR_ARG, "compact_interval must be >= 0");
     int rc = ensureDevice();
     if (rc) return rc;
     void* scratch = nullptr;

@@ -1312,6 +1312,7 @@ int orc_solve(const orc_material* mp, const orc_domain* dp,
     st.rows = rows;
     st.cols = cols;
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st.threads = nthreads;
     if (stats) *stats = st;
     return 0;
 }

@@ -138,6 +138,7 @@ typedef struct {
     long absorbed;
     long replay_exhausted; /* phonons whose replay stream ran out */
     double seconds;
+    long threads;           /* OpenMP threads the solve ran on */
 } orc_stats;
 
 typedef struct orc_material orc_material;

@@ -56,7 +56,7 @@ class Stats(C.Structure):
                 ("cols", C.c_long), ("phonon_steps", C.c_double), ("events", C.c_long),
                 ("scatters", C.c_long), ("escapes", C.c_long), ("horizon_stops", C.c_long),
                 ("maxscat_stops", C.c_long), ("absorbed", C.c_long),
-                ("replay_exhausted", C.c_long), ("seconds", C.c_double)]
+                ("replay_exhausted", C.c_long), ("seconds", C.c_double), ("threads", C.c_long)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

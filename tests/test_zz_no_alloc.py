@@ -10,7 +10,8 @@ all calls share, so these tests run two different solves back to back (the
 second must not see the first's counters, tally or phonons) and repeat the
 first, each checked against mc_solve with the tolerances of the other GPU
 tests: FP64 flight fields within 1e-12 and FP32 within 1e-10 of each row's
-largest magnitude, event counts identical.
+largest magnitude, event counts identical. Once a first call has loaded the
+kernels, further calls leave the device's free memory unchanged.
 
 The file is named to be collected last.
 """
@@ -82,3 +83,36 @@ def test_noalloc_rejects_problems_above_the_scratch_size():
     # the array is still usable after a refusal
     small = M.MultiProblem(mat, M.FilmDomain.from_cli(1e-7, 1e-7, 100), 5000, 10**6)
     _check(small, 1e-10, dt=0.5e-12, nsteps=200, precision=32, steps_per_launch=200, seed=3)
+
+
+def _free_bytes():
+    import torch
+    return torch.cuda.mem_get_info(0)[0]  # cudaMemGetInfo on the primary context the library uses
+
+
+def test_noalloc_calls_leave_free_device_memory_unchanged():
+    """No device allocation: after a warm-up call of each problem (module
+    loading, the scratch array's first touch), repeated calls leave the
+    free device memory exactly as it was."""
+    mat = M.Material.silicon(300.0)
+    film = M.MultiProblem(mat, M.FilmDomain.from_cli(1e-7, 1e-7, 100), 20000, 10**6)
+    pore = M.MultiProblem(mat, M.PoreCellDomain(5e-7, 2.5e-7), 6000, 10**6)
+    calls = [(film, dict(dt=0.5e-12, nsteps=200, precision=64, steps_per_launch=50, seed=5)),
+             (pore, dict(dt=0.5e-12, nsteps=150, precision=32, steps_per_launch=30, seed=9))]
+    L = _lib.lib()
+    for P, kw in calls:
+        _lib.check(_call(L.mc_solve_noalloc, P, **kw)[0])
+    before = _free_bytes()
+    for _ in range(3):
+        for P, kw in calls:
+            _lib.check(_call(L.mc_solve_noalloc, P, **kw)[0])
+    assert _free_bytes() == before
+
+
+def test_noalloc_validates_the_schedule_as_mc_solve_does():
+    mat = M.Material.silicon(300.0)
+    P = M.MultiProblem(mat, M.FilmDomain.from_cli(1e-7, 1e-7, 20), 2000, 10**6)
+    L = _lib.lib()
+    for fn in (L.mc_solve, L.mc_solve_noalloc):
+        rc, _, _ = _call(fn, P, dt=0.5e-12, nsteps=20, precision=32, schedule=7)
+        assert rc == -1  # MC_ERR_ARG
