@@ -37,6 +37,7 @@ extern "C" {
 #define MC_ERR_NONFINITE (-7)    /* non-finite phonon state                */
 #define MC_ERR_BUSY (-8)         /* admission refused (serving)            */
 #define MC_ERR_TIMEOUT (-9)      /* a bounded device-side wait gave up     */
+#define MC_ERR_CANCELLED (-10)   /* request cancelled (serving)            */
 
 /* Message of the last error on the calling thread. */
 const char* mc_last_error(void);
@@ -328,30 +329,40 @@ size_t mc_batch_state_bytes(mc_batch_h b);
 void mc_batch_destroy(mc_batch_h b);
 
 /* ------------------------------------------------------------ serving */
-/* A request loop on a library thread. Submitted solves are admitted against
- * an HBM budget (phonon state of the rounds in flight at once); every tick
- * advances one round of every admitted solve that fits -- its own
- * Material, Domain, phonon count and Philox key -- in one persistent
- * batched launch, so requests that arrive while others run join the next
- * tick. A round splits its phonons into `groups` batch means; a solve
- * completes when the standard error of kappa = -<q_axis> / gradT_axis is at
- * most target_rel_se of its mean. The first round has the requested
- * phonons; each later round the estimated remainder to the target (at
- * least the requested count, at most a quarter of the budget), and the
- * error pools the rounds' batch means weighted by their phonons. */
+/* A request loop on a library thread (no counterpart in the reference,
+ * whose solves run one at a time to completion). Submitted solves are
+ * admitted against an HBM budget: a solve is admitted when the phonon state
+ * of its first round fits into a free range of the server's state buffer,
+ * and keeps that state resident on the device for the whole round. Rounds
+ * run in windows of steps_per_window dt-steps; every tick advances one
+ * window of every admitted solve -- each with its own Material, Domain,
+ * phonon count and Philox key -- in ONE persistent batched launch, so a
+ * request that arrives while others are on the device joins them at the
+ * next window and their work overlaps. A round splits its phonons into
+ * `groups` batch means; a solve completes when the standard error of
+ * kappa = -<q_axis> / gradT_axis is at most target_rel_se of its mean. The
+ * first round has the requested phonons; each later round the estimated
+ * remainder to the target (at least the requested count, at most a quarter
+ * of the budget), and the error pools the rounds' batch means weighted by
+ * their phonons. State slots are given out first come, first served
+ * (solves between rounds before new requests). A solve's result depends
+ * only on its own request and the server's dt, horizon, window, groups and
+ * stopping rule: the same alone and in any mix. */
 typedef struct mc_server_s* mc_server_h;
 
 typedef struct {
     double dt;              /* time step, s                                 */
     long nsteps;            /* horizon of each round = nsteps * dt          */
     int precision;          /* 32 or 64                                     */
-    size_t hbm_budget;      /* bytes of phonon state admitted at once       */
+    size_t hbm_budget;      /* bytes of phonon state resident at once       */
     int max_active;         /* solves per tick (<= 512)                     */
     int groups;             /* batch means per round, 2..8                  */
     double target_rel_se;   /* e.g. 0.01                                    */
     int min_rounds;         /* rounds before the stopping rule applies     */
     int max_rounds;         /* give up (status MC_ERR_BUSY) after this many */
     int block_size;         /* 0 -> 256                                     */
+    int steps_per_window;   /* dt-steps per tick, a divisor of nsteps; 0: the
+                               largest divisor of nsteps <= nsteps / 8      */
 } mc_server_desc;
 
 typedef struct {
@@ -367,6 +378,7 @@ typedef struct {
     int field;              /* 1: keep the mean field (returned at the end);
                                0: kappa only -- flights are not split over
                                cells, kappa comes from the per-flight sums  */
+    int max_rounds;         /* this request's round limit (0: the server's) */
 } mc_request;
 
 typedef struct {
@@ -374,7 +386,11 @@ typedef struct {
     long rounds, phonons;
     double phonon_steps;
     double t_submit, t_admit, t_done;  /* seconds on the server clock       */
-    int status;             /* MC_OK, or MC_ERR_BUSY if max_rounds ran out  */
+    int status;             /* MC_OK; MC_ERR_BUSY if its max_rounds ran out
+                               or its first round can never fit the budget;
+                               MC_ERR_CANCELLED after mc_server_cancel;
+                               MC_ERR_NONFINITE if its phonons went
+                               non-finite                                   */
 } mc_result;
 
 typedef struct {
@@ -383,8 +399,17 @@ typedef struct {
 } mc_server_counters;
 
 int mc_server_create(const mc_server_desc* d, mc_server_h* out);
-/* Thread-safe; returns at once with a ticket. */
+/* Thread-safe; returns at once with a ticket. A request with invalid
+ * host inputs (null handles, nemit <= 0, an axis outside 0..2, a volume or
+ * gradient that is not finite, a negative max_rounds) is refused with
+ * MC_ERR_ARG and gets no ticket; the requests already submitted are not
+ * affected. */
 int mc_server_submit(mc_server_h s, const mc_request* r, long* ticket);
+/* Cancel a request: a queued one at once, a running one at the next window
+ * boundary (its device state is released then); its result reports
+ * MC_ERR_CANCELLED. Returns 1 if it was cancelled, 0 if it had completed
+ * already, < 0 for an unknown ticket. The other requests are not affected. */
+int mc_server_cancel(mc_server_h s, long ticket);
 /* 1 if done (result and, if field != NULL, the mean field rows x cols are
  * written), 0 if pending, < 0 on error. */
 int mc_server_poll(mc_server_h s, long ticket, mc_result* res, double* field);

@@ -16,7 +16,9 @@ MC_OK = 0
 ERRORS = {
     -1: "invalid argument", -2: "CUDA error", -3: "no CUDA device", -4: "unsupported geometry",
     -5: "I/O error", -6: "replay stream exhausted", -7: "non-finite state", -8: "busy", -9: "device wait timeout",
+    -10: "cancelled",
 }
+MC_ERR_ARG, MC_ERR_BUSY, MC_ERR_CANCELLED = -1, -8, -10
 
 
 class PpedDesc(C.Structure):
@@ -72,13 +74,14 @@ class BatchDesc(C.Structure):
 class ServerDesc(C.Structure):
     _fields_ = [("dt", C.c_double), ("nsteps", C.c_long), ("precision", C.c_int), ("hbm_budget", C.c_size_t),
                 ("max_active", C.c_int), ("groups", C.c_int), ("target_rel_se", C.c_double),
-                ("min_rounds", C.c_int), ("max_rounds", C.c_int), ("block_size", C.c_int)]
+                ("min_rounds", C.c_int), ("max_rounds", C.c_int), ("block_size", C.c_int),
+                ("steps_per_window", C.c_int)]
 
 
 class Request(C.Structure):
     _fields_ = [("mat", C.c_void_p), ("dom", C.c_void_p), ("problem", C.c_int), ("nemit", C.c_long),
                 ("maxscat", C.c_long), ("maxloop", C.c_long), ("seed", C.c_uint64), ("axis", C.c_int),
-                ("volume", C.c_double), ("gradient", C.c_double), ("field", C.c_int)]
+                ("volume", C.c_double), ("gradient", C.c_double), ("field", C.c_int), ("max_rounds", C.c_int)]
 
 
 class Result(C.Structure):
@@ -111,7 +114,8 @@ SYMBOLS = [
     "mc_session_restore",
     "mc_batch_create", "mc_batch_run", "mc_batch_result", "mc_batch_stats", "mc_batch_state_bytes",
     "mc_batch_destroy",
-    "mc_server_create", "mc_server_submit", "mc_server_poll", "mc_server_wait", "mc_server_stats",
+    "mc_server_create", "mc_server_submit", "mc_server_cancel", "mc_server_poll", "mc_server_wait",
+    "mc_server_stats",
     "mc_server_clock", "mc_server_destroy",
 ]
 
@@ -176,6 +180,7 @@ def lib(build_if_missing: bool = True):
     L.mc_server_create.argtypes = [P(ServerDesc), P(C.c_void_p)]
     L.mc_server_submit.argtypes = [C.c_void_p, P(Request), P(C.c_long)]
     L.mc_server_poll.argtypes = [C.c_void_p, C.c_long, P(Result), P(C.c_double)]
+    L.mc_server_cancel.argtypes = [C.c_void_p, C.c_long]
     L.mc_server_wait.argtypes = [C.c_void_p, C.c_long, C.c_double, P(Result), P(C.c_double)]
     L.mc_server_stats.argtypes = [C.c_void_p, P(ServerCounters)]
     L.mc_server_clock.restype = C.c_double

@@ -1657,6 +1657,44 @@ long long allocEmitters(const std::vector<double>& w, long nemitReq, std::vector
     return tot;
 }
 
+// State slots are handed out in multiples of this many (aligned warps).
+constexpr long long SLOT_ALIGN = 64;
+long long slotsFor(long long phonons) { return (phonons + SLOT_ALIGN - 1) / SLOT_ALIGN * SLOT_ALIGN; }
+
+// Free ranges of the server's state buffer: first fit, neighbours merged.
+struct SlotPool {
+    std::map<long long, long long> freeR;  // start -> length
+    void init(long long cap) {
+        freeR.clear();
+        if (cap > 0) freeR[0] = cap;
+    }
+    long long take(long long n) {
+        for (auto it = freeR.begin(); it != freeR.end(); ++it) {
+            if (it->second < n) continue;
+            const long long s = it->first, len = it->second;
+            freeR.erase(it);
+            if (len > n) freeR[s + n] = len - n;
+            return s;
+        }
+        return -1;
+    }
+    void give(long long s, long long n) {
+        auto it = freeR.emplace(s, n).first;
+        auto nx = std::next(it);
+        if (nx != freeR.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            freeR.erase(nx);
+        }
+        if (it != freeR.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                freeR.erase(it);
+            }
+        }
+    }
+};
+
 // One submitted solve.
 struct SrvJob {
     long ticket = 0;
@@ -1678,6 +1716,12 @@ struct SrvJob {
     double grad = 0., volume = 0.;
     std::vector<double> emW;   // emitter weights
     unsigned char image[512];  // host InstD<R> without the per-tick fields
+    // the current round's state slots [slot0, slot0 + slots), -1 between
+    // rounds, and the windows of it already run
+    long long slot0 = -1, slots = 0;
+    int window = 0;
+    int maxRounds = 0;
+    bool cancel = false;
     // pooled batch-mean statistics over rounds of unequal size: round r
     // gives `groups` estimates from N_r / groups phonons each
     long rounds = 0;
@@ -1699,14 +1743,14 @@ struct ServerBase {
     std::mutex mu;
     std::condition_variable cv, cvDone;
     std::deque<SrvJob*> pending;
-    std::vector<SrvJob*> active;
+    std::vector<SrvJob*> active;  // in ticket order
     std::map<long, SrvJob*> jobs;
     long nextTicket = 1;
-    long capacity = 0, inflight = 0;
+    long long capacity = 0;       // phonon slots of the state buffer
+    SlotPool pool;
     bool stop = false;
     mc_server_counters st{};
     std::thread th;
-    std::string err;
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
 
@@ -1721,8 +1765,9 @@ struct ServerT : ServerBase {
     void* state = nullptr;
     unsigned long long* cnt = nullptr;
     unsigned int* status = nullptr;
-    InstD<R>* insts_d = nullptr;
-    long long* islot_d = nullptr;
+    InstD<R>* insts_d = nullptr;   // every solve of a tick
+    InstD<R>* starts_d = nullptr;  // the solves whose round starts in the tick
+    long long* islot_d = nullptr;  // emission ranges of those
     double** accs_d = nullptr;
     double* gsum_d = nullptr;
     SegD* segs_d = nullptr;
@@ -1730,17 +1775,27 @@ struct ServerT : ServerBase {
     unsigned long long* segNext_d = nullptr;
     cudaStream_t stream = nullptr;
     int block = 256, nsm = 0;
-    long maxRound = 0;  // largest round a solve grows to (a server constant)
+    int K = 0, nwin = 1;            // dt-steps per window, windows per round
+    long maxRound = 0;              // largest round a solve grows to (a server constant)
     Params<R> base{};
 
     int init() {
         CK(cudaGetDevice(&dev));
-        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        if (d.steps_per_window < 0 || d.steps_per_window > d.nsteps || (d.steps_per_window > 0 && d.nsteps % d.steps_per_window))
+            return fail(MC_ERR_ARG, "steps_per_window must divide nsteps");
+        K = d.steps_per_window;
+        if (K == 0) {
+            K = (int)std::max(1L, d.nsteps / 8);
+            while (d.nsteps % K) --K;
+        }
+        nwin = (int)(d.nsteps / K);
         using V4 = typename Vec4<R>::T;
         const size_t per = 2 * sizeof(V4) + sizeof(uint4);
-        capacity = (long)(d.hbm_budget / per);
+        capacity = (long long)(d.hbm_budget / per) / SLOT_ALIGN * SLOT_ALIGN;
         if (capacity < 1024) return fail(MC_ERR_ARG, "hbm_budget too small");
-        maxRound = std::max(1L, capacity / 4 - 64);  // never above capacity - 64
+        maxRound = std::max(1LL, capacity / 4 - SLOT_ALIGN);
+        pool.init(capacity);
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
         const size_t cap = (size_t)capacity;
         CK(cudaMalloc(&state, 2 * al(sizeof(V4) * cap) + al(sizeof(uint4) * cap)));
@@ -1751,6 +1806,7 @@ struct ServerT : ServerBase {
         CK(cudaMalloc(&cnt, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
         CK(cudaMalloc(&status, sizeof(unsigned int)));
         CK(cudaMalloc(&insts_d, sizeof(InstD<R>) * d.max_active));
+        CK(cudaMalloc(&starts_d, sizeof(InstD<R>) * d.max_active));
         CK(cudaMalloc(&islot_d, sizeof(long long) * (d.max_active + 1)));
         CK(cudaMalloc(&accs_d, sizeof(double*) * d.max_active));
         CK(cudaMalloc(&gsum_d, sizeof(double) * d.max_active * MAX_GROUPS * 4));
@@ -1762,9 +1818,8 @@ struct ServerT : ServerBase {
         base.live_out = cnt + C_NCOUNTERS + 1;
         base.dt = (R)d.dt;
         base.nsteps = (int)d.nsteps;
-        base.ksteps = (int)d.nsteps;
-        base.insts = insts_d;
-        base.islot = islot_d;
+        base.ksteps = K;
+        base.step0 = 0;
         base.maxGroups = d.groups;
         base.maxRows = 4;
         block = d.block_size > 0 ? d.block_size : 256;
@@ -1776,9 +1831,16 @@ struct ServerT : ServerBase {
     }
 
     ~ServerT() override {
-        void* ps[] = {state, cnt, status, insts_d, islot_d, accs_d, gsum_d, segs_d, home_d, segNext_d};
+        void* ps[] = {state, cnt, status, insts_d, starts_d, islot_d, accs_d, gsum_d, segs_d, home_d, segNext_d};
         for (void* p : ps) if (p) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
+    }
+
+    // Phonons of a request's first round (the emitter rounding of its
+    // requested count), known before anything is uploaded.
+    long long firstRound(const SrvJob* j) const {
+        std::vector<long long> cdf;
+        return allocEmitters(j->req.dom->emWeight, j->req.nemit, cdf);
     }
 
     // Size the job's next round at `want` requested phonons: emitter counts,
@@ -1792,7 +1854,8 @@ struct ServerT : ServerBase {
         InstD<R> I;
         std::memcpy(&I, j->image, sizeof(I));
         I.nemit = j->nemit;
-        const double window = (double)d.nsteps * d.dt;
+        // a flight stays inside one window: the window bounds its amount
+        const double window = (double)K * d.dt;
         // a block's shared field takes at most one field copy's phonons
         const double perCopy = (double)((j->nemit + d.groups - 1) / d.groups);
         for (int r = 0; r < 4; ++r) {
@@ -1832,7 +1895,7 @@ struct ServerT : ServerBase {
         for (double v : D.cellVol) vol += v;
         j->volume = j->req.volume > 0. ? j->req.volume : vol;
         j->grad = j->req.gradient != 0. ? j->req.gradient : D.desc[0].gradT[j->req.axis];
-        if (j->grad == 0.) return fail(MC_ERR_ARG, "no temperature gradient along the kappa axis");
+        if (!(j->grad != 0.) || !std::isfinite(j->grad)) return fail(MC_ERR_ARG, "no temperature gradient along the kappa axis");
         InstD<R> I;
         std::memset(&I, 0, sizeof(I));
         I.vel = P.vel; I.vt = P.vt; I.wthr = P.wthr; I.wguide = P.wguide; I.pthr = P.pthr;
@@ -1850,34 +1913,42 @@ struct ServerT : ServerBase {
         static_assert(sizeof(InstD<R>) <= sizeof(j->image), "instance image");
         std::memcpy(j->image, &I, sizeof(I));
         j->nextReq = j->req.nemit;
+        j->window = 0;
         return setRound(j, j->req.nemit);
     }
 
+    // One window of every running solve: emission of the rounds that start
+    // now, one batched advance launch over all of them, and for the rounds
+    // that end with it the field finish and their batch-mean statistics.
     int tick(const std::vector<SrvJob*>& run) {
         const int n = (int)run.size();
         std::vector<InstD<R>> inst(n);
-        std::vector<long long> islot(n + 1, 0);
         std::vector<double*> accs(n);
+        std::vector<int> starts;
         for (int i = 0; i < n; ++i) {
             SrvJob* j = run[i];
             std::memcpy(&inst[i], j->image, sizeof(InstD<R>));
             inst[i].inst = i;
-            inst[i].slot0 = islot[i];
+            inst[i].slot0 = j->slot0;
             const uint64_t seed = j->req.seed + (uint64_t)j->rounds;
             inst[i].key0 = (uint32_t)seed;
             inst[i].key1 = (uint32_t)(seed >> 32);
-            islot[i + 1] = islot[i] + j->nemit;
             accs[i] = j->acc;
-            const size_t fieldD = (size_t)inst[i].gstride * d.groups + 4 * (size_t)d.groups;
-            CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * fieldD, stream));
+            if (j->window == 0) {
+                starts.push_back(i);
+                const size_t fieldD = (size_t)inst[i].gstride * d.groups + 4 * (size_t)d.groups;
+                CK(cudaMemsetAsync(j->fields, 0, sizeof(double) * fieldD, stream));
+            }
         }
         Params<R> P = base;
         {
             int rc = batchCaps<R>(inst, P);
             if (rc) return rc;
-            for (auto& I : inst) {
+            for (int i = 0; i < n; ++i) {
+                InstD<R>& I = inst[i];
                 if (I.flags & IF_TAL_SHARED) I.gdif = nullptr;
                 if (I.tally == nullptr) I.flags |= IF_NO_FIELD;
+                if (run[i]->window + 1 == nwin) I.flags |= IF_LAST;
             }
         }
         const int tm = batchFieldMode<R>(inst);
@@ -1886,11 +1957,32 @@ struct ServerT : ServerBase {
         const int occ = advanceBatchOccupancy<R>(tm, gen, batchSmemBytes<R>(P), block);
         if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "batched kernel cannot launch with this configuration");
         const int grid = std::min(occ, 64) * nsm;
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), stream));
+        CK(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
+        CK(cudaMemcpyAsync(insts_d, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(accs_d, accs.data(), sizeof(double*) * n, cudaMemcpyHostToDevice, stream));
+        std::vector<InstD<R>> sinst;
+        std::vector<long long> sslot(1, 0);
+        for (int i : starts) {
+            sinst.push_back(inst[i]);
+            sslot.push_back(sslot.back() + run[i]->nemit);
+        }
+        if (!starts.empty()) {
+            // emission of the starting rounds into their own slots
+            CK(cudaMemcpyAsync(starts_d, sinst.data(), sizeof(InstD<R>) * sinst.size(), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(islot_d, sslot.data(), sizeof(long long) * sslot.size(), cudaMemcpyHostToDevice, stream));
+            Params<R> E = P;
+            E.insts = starts_d;
+            E.islot = islot_d;
+            E.ninst = (int)starts.size();
+            E.cap = (unsigned long long)sslot.back();
+            CK(launchEmitBatch<R>(E, stream));
+        }
         std::vector<SegD> segs;
         std::vector<int> home;
-        std::vector<long long> slot0(islot.begin(), islot.end() - 1);
+        std::vector<long long> slot0(n);
         std::vector<long> nem(n);
-        for (int i = 0; i < n; ++i) nem[i] = run[i]->nemit;
+        for (int i = 0; i < n; ++i) { slot0[i] = run[i]->slot0; nem[i] = run[i]->nemit; }
         planSegments(slot0, nem, std::vector<int>(n, d.groups), grid, segs, home);
         if (!segs.empty())
             CK(cudaMemcpyAsync(segs_d, segs.data(), sizeof(SegD) * segs.size(), cudaMemcpyHostToDevice, stream));
@@ -1900,16 +1992,10 @@ struct ServerT : ServerBase {
         P.home = home_d;
         P.segNext = segNext_d;
         P.nseg = (int)segs.size();
-        CK(cudaMemcpyAsync(insts_d, inst.data(), sizeof(InstD<R>) * n, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(islot_d, islot.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, stream));
-        CK(cudaMemcpyAsync(accs_d, accs.data(), sizeof(double*) * n, cudaMemcpyHostToDevice, stream));
-        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (C_NCOUNTERS + 4), stream));
-        CK(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
-        P.cap = (unsigned long long)islot[n];
+        P.insts = insts_d;
         P.ninst = n;
-        P.step0 = 0;
+        P.lastOnly = 1;
         setWindow(P);
-        CK(launchEmitBatch<R>(P, stream));
         CK(launchAdvanceBatch<R>(P, tm, gen, grid, block, stream));
         CK(launchDifPrefix<R>(P, stream));
         CK(launchRoundReduce<R>(P, accs_d, gsum_d, stream));
@@ -1925,6 +2011,7 @@ struct ServerT : ServerBase {
         const int G = d.groups;
         for (int i = 0; i < n; ++i) {
             SrvJob* j = run[i];
+            if (++j->window < nwin) continue;
             j->rounds++;
             // group g holds N / G phonons: kappa_g = -G power q_g / (V gradT)
             const double N = (double)j->nemit;
@@ -1944,6 +2031,7 @@ struct ServerT : ServerBase {
         return MC_OK;
     }
 
+    // Result of a finished solve; frees its device data (outside the lock).
     void complete(SrvJob* j, int status) {
         j->status = status;
         // mean field over the rounds' phonons: (power x N) / sum N x sum of
@@ -1962,7 +2050,6 @@ struct ServerT : ServerBase {
                 }
         }
         freeJobDevice(j);
-        j->tDone = now();
     }
 
     // Phonons of the job's next round: the estimated remainder to reach the
@@ -1977,65 +2064,116 @@ struct ServerT : ServerBase {
         return (long)std::min(need, (double)std::max(maxRound, j->req.nemit));
     }
 
+    // (under the lock) state slots for a round of `phonons`
+    bool takeSlots(SrvJob* j, long long phonons) {
+        const long long n = slotsFor(phonons);
+        const long long s = pool.take(n);
+        if (s < 0) return false;
+        j->slot0 = s;
+        j->slots = n;
+        return true;
+    }
+    void releaseSlots(SrvJob* j) {
+        if (j->slot0 >= 0) pool.give(j->slot0, j->slots);
+        j->slot0 = -1;
+        j->slots = 0;
+    }
+
+    // (under the lock) publish a finished solve
+    void publish(SrvJob* j) {
+        j->tDone = now();
+        j->done = true;
+        st.completed++;
+    }
+
     void loop() override {
         cudaSetDevice(dev);
         for (;;) {
-            std::vector<SrvJob*> toAdmit, run;
+            std::vector<SrvJob*> toAdmit, dropped, run;
+            std::vector<int> droppedRc;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 if (stop) break;
-                // admission: the rounds of the admitted solves fit the budget
-                inflight = 0;
-                for (SrvJob* j : active) inflight += j->nemit + 64;
-                while (!pending.empty() && (int)(active.size() + toAdmit.size()) < d.max_active) {
+                // cancellations of admitted solves take effect between windows
+                std::vector<SrvJob*> keep;
+                for (SrvJob* j : active) {
+                    if (j->cancel) {
+                        releaseSlots(j);
+                        dropped.push_back(j);
+                        droppedRc.push_back(MC_ERR_CANCELLED);
+                    } else {
+                        keep.push_back(j);
+                    }
+                }
+                active.swap(keep);
+                // slots for the next round of the solves between rounds,
+                // oldest first; then new requests while nobody older waits
+                bool blocked = false;
+                for (SrvJob* j : active) {
+                    if (j->slot0 >= 0) continue;
+                    if (!takeSlots(j, j->nemit)) { blocked = true; break; }
+                }
+                while (!blocked && !pending.empty() && (int)(active.size() + toAdmit.size()) < d.max_active) {
                     SrvJob* j = pending.front();
-                    const long need = j->req.nemit + 64;
-                    if (inflight + need > capacity && !(active.empty() && toAdmit.empty())) break;
+                    const long long n = firstRound(j);
+                    if (slotsFor(n) > capacity) {
+                        // can never fit: refused alone
+                        pending.pop_front();
+                        dropped.push_back(j);
+                        droppedRc.push_back(fail(MC_ERR_BUSY, "request larger than the HBM budget"));
+                        continue;
+                    }
+                    if (!takeSlots(j, n)) break;
                     pending.pop_front();
                     toAdmit.push_back(j);
-                    inflight += need;
                 }
-                if (active.empty() && toAdmit.empty()) {
+                if (active.empty() && toAdmit.empty() && dropped.empty()) {
                     cv.wait_for(lk, std::chrono::milliseconds(5));
                     continue;
                 }
             }
-            for (SrvJob* j : toAdmit) {
-                int rc = (j->req.nemit + 64 > capacity) ? fail(MC_ERR_BUSY, "request larger than the HBM budget")
-                                                         : admit(j);
-                std::lock_guard<std::mutex> lk(mu);
-                if (rc) {
-                    freeJobDevice(j);
-                    j->status = rc;
-                    j->done = true;
-                    j->tDone = now();
-                    st.completed++;
-                    cvDone.notify_all();
-                    continue;
-                }
-                j->tAdmit = now();
-                active.push_back(j);
-                st.admitted++;
+            for (size_t k = 0; k < dropped.size(); ++k) complete(dropped[k], droppedRc[k]);
+            std::vector<int> admitRc(toAdmit.size());
+            for (size_t k = 0; k < toAdmit.size(); ++k) {
+                SrvJob* j = toAdmit[k];
+                j->maxRounds = j->req.max_rounds > 0 ? j->req.max_rounds : d.max_rounds;
+                admitRc[k] = admit(j);
+                if (admitRc[k]) complete(j, admitRc[k]);
             }
-            // this tick: the oldest solves whose rounds fit the state buffer
-            long used = 0;
-            for (SrvJob* j : active) {
-                if (used + j->nemit + 64 > capacity) continue;
-                used += j->nemit + 64;
-                run.push_back(j);
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                for (SrvJob* j : dropped) publish(j);
+                for (size_t k = 0; k < toAdmit.size(); ++k) {
+                    SrvJob* j = toAdmit[k];
+                    if (admitRc[k]) {
+                        releaseSlots(j);
+                        publish(j);
+                        continue;
+                    }
+                    j->tAdmit = now();
+                    active.push_back(j);
+                    st.admitted++;
+                }
+                for (SrvJob* j : active)
+                    if (j->slot0 >= 0) run.push_back(j);
+                if (!dropped.empty() || !toAdmit.empty()) cvDone.notify_all();
             }
             if (run.empty()) continue;
             const double tb = now();
-            int rc = tick(run);
-            // each solve's next step (outside the lock: setRound copies)
-            std::vector<int> fate(run.size(), 0);  // 0 next round, 1 converged, 2 gave up, 3 error
+            const int rc = tick(run);
+            // each solve whose round ended: converged, out of rounds, or the
+            // next round sized (outside the lock: setRound copies)
+            std::vector<int> fate(run.size(), 0);  // 0 going on, 1 converged, 2 gave up, 3 error
             for (size_t i = 0; i < run.size(); ++i) {
                 SrvJob* j = run[i];
+                if (rc) { fate[i] = 3; continue; }
+                if (j->window < nwin) continue;
+                j->window = 0;
                 const bool conv = j->rounds >= d.min_rounds && j->se() <= d.target_rel_se * std::fabs(j->kappa());
-                if (rc) fate[i] = 3;
-                else if (conv) fate[i] = 1;
-                else if (j->rounds >= d.max_rounds) fate[i] = 2;
+                if (conv) fate[i] = 1;
+                else if (j->rounds >= j->maxRounds) fate[i] = 2;
                 else {
+                    fate[i] = 4;  // between rounds
                     const long want = nextRound(j);
                     if (want != j->nextReq) {
                         j->nextReq = want;
@@ -2043,6 +2181,9 @@ struct ServerT : ServerBase {
                     }
                 }
             }
+            for (size_t i = 0; i < run.size(); ++i)
+                if (fate[i] >= 1 && fate[i] <= 3)
+                    complete(run[i], fate[i] == 1 ? MC_OK : (fate[i] == 2 ? MC_ERR_BUSY : (rc ? rc : MC_ERR_CUDA)));
             std::lock_guard<std::mutex> lk(mu);
             st.ticks++;
             st.busy_s += now() - tb;
@@ -2051,10 +2192,10 @@ struct ServerT : ServerBase {
             for (SrvJob* j : active) {
                 const bool ran = ri < run.size() && run[ri] == j;
                 const int f = ran ? fate[ri++] : 0;
-                if (f != 0) {
-                    complete(j, f == 1 ? MC_OK : (f == 2 ? MC_ERR_BUSY : (rc ? rc : MC_ERR_CUDA)));
-                    j->done = true;
-                    st.completed++;
+                if (f == 4) releaseSlots(j);
+                if (f >= 1 && f <= 3) {
+                    releaseSlots(j);
+                    publish(j);
                     continue;
                 }
                 keep.push_back(j);
@@ -2723,6 +2864,9 @@ int mc_server_create(const mc_server_desc* d, mc_server_h* out) {
     if (d->groups < 2 || d->groups > MAX_GROUPS) return fail(MC_ERR_ARG, "groups must be in 2..8");
     if (d->max_active < 1 || d->max_active > 512) return fail(MC_ERR_ARG, "max_active must be in 1..512");
     if (!(d->target_rel_se > 0.) || d->max_rounds < 1 || d->min_rounds < 1) return fail(MC_ERR_ARG, "invalid stopping rule");
+    if (d->steps_per_window < 0 || d->steps_per_window > d->nsteps ||
+        (d->steps_per_window > 0 && d->nsteps % d->steps_per_window != 0))
+        return fail(MC_ERR_ARG, "steps_per_window must be 0 or a divisor of nsteps");
     int rc = ensureDevice();
     if (rc) return rc;
     std::unique_ptr<ServerBase> impl;
@@ -2738,8 +2882,11 @@ int mc_server_create(const mc_server_desc* d, mc_server_h* out) {
 
 int mc_server_submit(mc_server_h s, const mc_request* r, long* ticket) {
     if (!s || !r || !ticket) return fail(MC_ERR_ARG, "null argument");
-    if (!r->mat || !r->dom || r->nemit <= 0 || r->maxscat <= 0 || r->maxloop < 0 || r->axis < 0 || r->axis > 2)
+    if (!r->mat || !r->dom || r->nemit <= 0 || r->maxscat <= 0 || r->maxloop < 0 || r->axis < 0 || r->axis > 2 ||
+        r->max_rounds < 0)
         return fail(MC_ERR_ARG, "invalid request");
+    if (!std::isfinite(r->volume) || r->volume < 0. || !std::isfinite(r->gradient))
+        return fail(MC_ERR_ARG, "request volume and gradient must be finite");
     if (r->problem != MC_FLUX && r->problem != MC_MULTI) return fail(MC_ERR_ARG, "kappa needs a flux problem");
     ServerBase* b = s->impl.get();
     SrvJob* j = new SrvJob;
@@ -2753,6 +2900,30 @@ int mc_server_submit(mc_server_h s, const mc_request* r, long* ticket) {
     *ticket = j->ticket;
     b->cv.notify_all();
     return MC_OK;
+}
+
+int mc_server_cancel(mc_server_h s, long ticket) {
+    if (!s) return fail(MC_ERR_ARG, "null server");
+    ServerBase* b = s->impl.get();
+    std::lock_guard<std::mutex> lk(b->mu);
+    auto it = b->jobs.find(ticket);
+    if (it == b->jobs.end()) return fail(MC_ERR_ARG, "unknown ticket");
+    SrvJob* j = it->second;
+    if (j->done) return 0;
+    auto q = std::find(b->pending.begin(), b->pending.end(), j);
+    if (q != b->pending.end()) {
+        // queued: nothing on the device yet
+        b->pending.erase(q);
+        j->status = MC_ERR_CANCELLED;
+        j->tDone = b->now();
+        j->done = true;
+        b->st.completed++;
+        b->cvDone.notify_all();
+        return 1;
+    }
+    j->cancel = true;  // the loop drops it at the next window boundary
+    b->cv.notify_all();
+    return 1;
 }
 
 static int pollLocked(ServerBase* b, long ticket, mc_result* res, double* field) {

@@ -58,7 +58,9 @@ struct SegD {
 // InstD::flags: a batched block stages the fixed-point field / the
 // subdomain images in shared memory; the instance keeps no field (only the
 // per-flight checksums, e.g. for kappa alone)
-enum { IF_TAL_SHARED = 1, IF_SD_SHARED = 2, IF_NO_FIELD = 4 };
+// IF_LAST: this launch's window is the last of the instance's horizon (a
+// served round whose windows started at another launch than the others')
+enum { IF_TAL_SHARED = 1, IF_SD_SHARED = 2, IF_NO_FIELD = 4, IF_LAST = 8 };
 
 template <typename R>
 struct Params {
@@ -136,6 +138,9 @@ struct Params {
     int ninst;
     int maxGroups;  // largest field-copy count of the instances
     int maxRows;    // largest row count of the instances
+    // served windows: the round-end kernels (difference-array prefix, round
+    // reduction) skip the instances without IF_LAST
+    int lastOnly;
     // work segments of a batched advance: each block starts on segment
     // home[block] and moves on to any segment with slots left; segNext[s]
     // counts the slots of segment s already claimed

@@ -213,14 +213,20 @@ __host__ __device__ __forceinline__ long long groupedId(long long local, long lo
     return j * G + g;
 }
 
-// Emission of every instance of a batch: slot n belongs to the instance whose
-// slot range holds it; its phonon id follows from the slot by groupedId.
+// Emission of every instance of a launch: thread n takes phonon n - islot[i]
+// of the instance i whose range [islot[i], islot[i + 1]) holds n, writes it
+// to that instance's state slot I.slot0 + (n - islot[i]) (a batch lays its
+// instances out back to back, so that slot is n; a served round sits in the
+// slots it was given), and its phonon id follows by groupedId.
 template <typename R>
 __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= (long long)P.cap) return;
-    const InstD<R>& I = P.insts[instanceOf(P.islot, P.ninst, n)];
-    const long long id = groupedId(n - I.slot0, I.nemit, I.groups);
+    const int i = instanceOf(P.islot, P.ninst, n);
+    const InstD<R>& I = P.insts[i];
+    const long long local = n - P.islot[i];
+    const long long slot = I.slot0 + local;
+    const long long id = groupedId(local, I.nemit, I.groups);
     Rng<false> g;
     g.init(I.key0, I.key1, (uint32_t)id, &P);
     Phn<R> ph;
@@ -228,9 +234,9 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
     typename Vec4<R>::T a, b;
     uint4 c;
     packPhonon(ph, a, b, c);
-    st4(P.P0out + n, a);
-    st4(P.P1out + n, b);
-    __stcs(P.P2out + n, c);
+    st4(P.P0out + slot, a);
+    st4(P.P1out + slot, b);
+    __stcs(P.P2out + slot, c);
 }
 
 // ----------------------------------------------------------------- advance
@@ -241,8 +247,9 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // regCap). Its live phonons sit at the two ends of its region in the input
 // half: regIn[2b] at the front (their next event falls inside this
 // window), regIn[2b + 1] at the back (no event in it). The block's last
-// warp is the producer: one lane walks the front range, then the back
-// range, in tiles of T = blockDim.x - 32 slots and issues cp.async.bulk
+// warp is the producer: one lane walks the front and back ranges, front
+// tiles spread evenly among the back ones (a different phase per block),
+// in tiles of T = blockDim.x - 32 slots and issues cp.async.bulk
 // copies of each tile (48 B per phonon in FP32: three 16-byte words, one
 // copy per word array) into one of STATIC_STAGES shared-memory stages,
 // completing on the stage's mbarrier. The other T threads (the consumers)
@@ -252,8 +259,8 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // half: phonons whose next event falls inside the next window from the
 // front, the others from the back, positions taken from two shared-memory
 // counters per warp ballot. Stopped phonons are dropped. The warps of a
-// block never wait for one another, warps see phonons of one kind (events
-// first, then plain flights), and no global atomic is involved. Step and
+// block never wait for one another, a tile holds phonons of one kind (events
+// or plain flights), and no global atomic is involved. Step and
 // event counts are summed per thread and added to the block's counters
 // once, at the end.
 constexpr int STATIC_STAGES = 2;
@@ -333,6 +340,9 @@ k_advance(Params<R> P) {
                 min((unsigned long long)P.regIn[2 * blockIdx.x + 1], (unsigned long long)C - nF);
             const long long tF = ((long long)nF + T - 1) / T, tB = ((long long)nB + T - 1) / T;
             const uint32_t perPhonon = (uint32_t)(2 * sizeof(V4) + sizeof(uint4));
+            // Bresenham phase of the front tiles in [0, tF + tB)
+            const long long phase = (long long)((blockIdx.x * 2654435761u) % (unsigned)max(tF + tB, 1LL));
+            long long jF = 0, jB = 0;
             int j = 0;
             for (;; ++j) {
                 const int s = j % STATIC_STAGES;
@@ -348,17 +358,25 @@ k_advance(Params<R> P) {
                     ++j;
                     break;
                 }
+                // front tiles spread evenly among the back tiles, at a phase
+                // that differs from block to block: the blocks of an SM do
+                // not all run their event-heavy tiles (the walker) at once,
+                // so the bulk-copy stream keeps HBM busy throughout
                 long long src;
                 unsigned cnt;
-                if (j < tF) {
-                    src = rbase + (long long)j * T;
-                    cnt = (unsigned)min((long long)T, (long long)nF - (long long)j * T);
+                const long long tot = tF + tB;
+                const long long wantF = tF ? ((long long)(j + 1) * tF + phase) / tot : 0;
+                const bool front = jF < tF && (jB >= tB || wantF > jF);
+                if (front) {
+                    src = rbase + jF * T;
+                    cnt = (unsigned)min((long long)T, (long long)nF - jF * T);
+                    ++jF;
                 } else {
-                    const long long k = j - tF;
-                    src = rbase + C - (long long)nB + k * T;
-                    cnt = (unsigned)min((long long)T, (long long)nB - k * T);
+                    src = rbase + C - (long long)nB + jB * T;
+                    cnt = (unsigned)min((long long)T, (long long)nB - jB * T);
+                    ++jB;
                 }
-                sCnt[s] = cnt | (j >= tF ? STATIC_BACK : 0u);
+                sCnt[s] = cnt | (front ? 0u : STATIC_BACK);
                 unsigned char* st = stage0 + (size_t)s * sbytes;
                 mbarArriveExpectTx(&barFull[s], cnt * perPhonon);
                 bulkLoad(st, P.P0in + src, cnt * (uint32_t)sizeof(V4), &barFull[s]);
@@ -656,8 +674,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
             curInst = S.inst;
         }
         __syncthreads();
+        // a served instance may end its horizon in this window while others
+        // are in the middle of theirs
+        Window<R> Wb = W;
+        Wb.last = W.last || (I->flags & IF_LAST) != 0;
         dynamicLoop<R, false, false, TM, BatchView<R>, GEN>(P, P.segNext + sg, (unsigned long long)S.beg,
-                                              (unsigned long long)S.end, BatchView<R>{&P, smraw, I}, W);
+                                              (unsigned long long)S.end, BatchView<R>{&P, smraw, I}, Wb);
         __syncthreads();
         flushBinding<R>(*I, S.group);
         __syncthreads();
@@ -696,6 +718,7 @@ __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
     const InstD<R>& I = P.insts[blockIdx.x];
     const int r = (int)(blockIdx.y % (unsigned)P.maxRows), grp = (int)(blockIdx.y / (unsigned)P.maxRows);
     if (r >= I.rows || grp >= I.groups || I.gdif == nullptr) return;
+    if (P.lastOnly && !(I.flags & IF_LAST)) return;
     const long long go = (long long)grp * I.gstride;
     const int lane = threadIdx.x;
     double carry = 0.0;
@@ -716,12 +739,14 @@ __global__ void __launch_bounds__(32) k_difprefix(Params<R> P) {
 // End of a served round, block (x, i): gsum[i][g][r] = checksum of row r
 // of field copy g (the batch-mean samples: the amount of every flight of the
 // copy's phonons, equal to the copy's field summed over cells), and, for a
-// solve that keeps its field, acc += the sum of its field copies.
+// solve that keeps its field, acc += the sum of its field copies. With
+// lastOnly, instances whose round goes on are skipped.
 constexpr int MAX_GROUPS = 8;
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_round_reduce(Params<R> P, double* const* accs, double* gsum) {
     const InstD<R>& I = P.insts[blockIdx.y];
+    if (P.lastOnly && !(I.flags & IF_LAST)) return;
     if (blockIdx.x == 0 && threadIdx.x < 4 * MAX_GROUPS) {
         const int g = threadIdx.x >> 2, r = threadIdx.x & 3;
         gsum[(long long)blockIdx.y * MAX_GROUPS * 4 + threadIdx.x] = (g < I.groups && r < I.rows) ? I.csum[threadIdx.x] : 0.0;

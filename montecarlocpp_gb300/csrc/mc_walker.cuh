@@ -579,6 +579,12 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
             if (r < T.nAct) T.csumAdd(r, T.fixedOf(r, s));
     }
     R rem = s;
+    // the lanes that walk: each leaves the loop after its own number of
+    // crossings; they wait for one another after it, so that the event code
+    // that follows runs once for all of them rather than once per exit
+    // (measured: 4.2 of 32 lanes active per instruction on the pore cell
+    // without it, the kernel 2.1x slower)
+    const unsigned walkers = __activemask();
     const int s0 = S.tstride[1], s01 = S.tstride[2];
     for (int guard = 0; guard < 3 * MAX_SHAPE + 4; ++guard) {
         R tmin = rem;
@@ -610,6 +616,7 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
         rem -= tmin;
         if (ax < 0) break;
     }
+    __syncwarp(walkers);
 }
 
 template <typename R>

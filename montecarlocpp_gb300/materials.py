@@ -52,9 +52,21 @@ class SiliconModel:
     C: float = 137.3
 
 
+_DEFAULT_TABLES = None
+
+
 def silicon_tables(model: SiliconModel | None = None):
-    """Return (disp, relax): disp is nw x (2 + 2 np), relax is np x 8."""
-    m = model or SiliconModel()
+    """Return (disp, relax): disp is nw x (2 + 2 np), relax is np x 8 (fresh
+    arrays; the default model's are built once)."""
+    global _DEFAULT_TABLES
+    if model is None:
+        if _DEFAULT_TABLES is None:
+            _DEFAULT_TABLES = _silicon_tables(SiliconModel())
+        return tuple(x.copy() for x in _DEFAULT_TABLES)
+    return _silicon_tables(model)
+
+
+def _silicon_tables(m: SiliconModel):
     np_ = len(m.branches)
     wmax = max(b.omega_max(m.kmax) for b in m.branches)
     dw = wmax / m.nw

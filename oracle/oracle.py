@@ -287,12 +287,22 @@ def solve(mat, dom, problem=MULTI, nemit=1000, maxscat=1000, maxloop=0, dt=0.0,
     return out.reshape(rows, dom.cols, order="F"), st.as_dict(), extras
 
 
-def record_to_replay(record):
-    """Turn recorded per-phonon words into (flat words, offsets)."""
+def record_to_replay(record, pad=0, seed=12345):
+    """Turn recorded per-phonon words into (flat words, offsets). `pad`
+    extra words (a fixed pseudo-random sequence) follow each phonon's
+    record, so that a replay whose trajectory parts from the recorded one
+    (an FP32 rounding flips a discrete choice) can run on past it."""
     rw, rc = record
+    rc = np.asarray(rc, dtype=np.int64)
     offsets = np.zeros(len(rc) + 1, dtype=np.int64)
-    offsets[1:] = np.cumsum(rc)
-    words = np.concatenate([rw[i, :rc[i]] for i in range(len(rc))]) if len(rc) else np.zeros(0, np.uint32)
+    offsets[1:] = np.cumsum(rc + pad)
+    extra = np.random.default_rng(seed).integers(0, 2**32, size=pad, dtype=np.uint64).astype(np.uint32)
+    parts = []
+    for i in range(len(rc)):
+        parts.append(rw[i, :rc[i]])
+        if pad:
+            parts.append(extra)
+    words = np.concatenate(parts) if parts else np.zeros(0, np.uint32)
     return words.astype(np.uint32), offsets
 
 
