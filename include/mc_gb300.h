@@ -56,6 +56,21 @@ int mc_material_create(const double* disp, long nw, long np, const double* relax
 /* Material(disp, relax, T) reading the two files
  * (montecarlo/material.cpp:158-186). */
 int mc_material_load(const char* disp_path, const char* relax_path, double T, mc_material_h* out);
+/* Material(disp, relax, T[t]) for n temperatures at once (no counterpart
+ * in the reference, which builds one Material per run; it serves batches
+ * and request streams of many temperatures): the temperature-dependent
+ * tables of montecarlo/material.cpp:116-161 -- relaxation times, the
+ * energy, flux and scattering pdfs, their sums and the inverse-CDF
+ * thresholds -- are built on the GPU in one launch. out[t] is, bit for bit,
+ * the material mc_material_create(disp, nw, np, relax, T[t]) returns: both
+ * builds evaluate the same FP64 formulas in the same order. Synchronous. */
+int mc_material_create_many(const double* disp, long nw, long np, const double* relax, const double* T, int n,
+                            mc_material_h* out);
+/* The integer inverse-CDF thresholds the kernels sample (no counterpart in
+ * the reference, whose Boost discrete distributions hold their own
+ * tables): scattering bins (nw) and branches (nw x np), flux bins and
+ * branches; threshold = ceil(cdf * 2^32). Any pointer may be NULL. */
+int mc_material_thresholds(mc_material_h m, uint64_t* swthr, uint64_t* spthr, uint64_t* fwthr, uint64_t* fpthr);
 /* energySum, fluxSum, scatSum, cond (montecarlo/material.h:55,62-64). */
 int mc_material_sums(mc_material_h m, double out[4]);
 /* vel and tau tables, nw x np row-major (montecarlo/material.cpp:246-256). */

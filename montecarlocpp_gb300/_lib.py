@@ -106,7 +106,7 @@ class ServerCounters(C.Structure):
 SYMBOLS = [
     "mc_last_error", "mc_version",
     "mc_material_create", "mc_material_load", "mc_material_sums", "mc_material_tables",
-    "mc_material_destroy",
+    "mc_material_destroy", "mc_material_create_many", "mc_material_thresholds",
     "mc_domain_create", "mc_domain_create_shapes", "mc_domain_cols", "mc_domain_cell_volumes", "mc_domain_destroy",
     "mc_solve", "mc_solve_noalloc", "mc_solve_replicas", "mc_check_bounded_wait",
     "mc_session_create", "mc_session_emit", "mc_session_advance", "mc_session_result",
@@ -145,6 +145,9 @@ def lib(build_if_missing: bool = True):
     L.mc_material_create.argtypes = [P(C.c_double), C.c_long, C.c_long, P(C.c_double), C.c_double, P(C.c_void_p)]
     L.mc_material_load.argtypes = [C.c_char_p, C.c_char_p, C.c_double, P(C.c_void_p)]
     L.mc_material_sums.argtypes = [C.c_void_p, P(C.c_double)]
+    L.mc_material_create_many.argtypes = [P(C.c_double), C.c_long, C.c_long, P(C.c_double), P(C.c_double), C.c_int,
+                                          P(C.c_void_p)]
+    L.mc_material_thresholds.argtypes = [C.c_void_p] + [P(C.c_uint64)] * 4
     L.mc_material_tables.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
     L.mc_material_destroy.argtypes = [C.c_void_p]
     L.mc_domain_create.argtypes = [P(PpedDesc), C.c_int, P(PairDesc), C.c_int, P(C.c_void_p)]

@@ -30,6 +30,7 @@
 
 #include "../../include/mc_gb300.h"
 #include "mc_launch.h"
+#include "mc_matbuild.h"
 
 using namespace mcg;
 
@@ -131,37 +132,21 @@ M3 rotZTo(const V3& nIn) {
     return r;
 }
 
-// Integer inverse-CDF thresholds: T_i = ceil(cdf_i * 2^32), so that for a
-// 32-bit word x, x < T_i exactly when x / 2^32 < cdf_i in FP64.
-unsigned long long thrOf(double cdf) {
-    double t = std::ceil(std::ldexp(cdf, 32));
-    if (t < 0.) t = 0.;
-    if (t > 4294967296.0) t = 4294967296.0;
-    return (unsigned long long)t;
-}
-
 // Two-level discrete distribution (montecarlo/material.cpp:123-147) as
-// FP64 cumulative tables.
+// integer inverse-CDF thresholds (cdfThreshold): the bins by their
+// running sum over the bins' totals, the branches of a bin by theirs.
 void buildThresholds(const std::vector<double>& pdf, long nw, long np, std::vector<unsigned long long>& wthr,
                      std::vector<unsigned long long>& pthr) {
-    std::vector<double> rowSum(nw), pre(nw);
-    double acc = 0.;
-    for (long w = 0; w < nw; ++w) {
-        double s = 0.;
-        for (long p = 0; p < np; ++p) s += pdf[w * np + p];
-        rowSum[w] = s;
-        acc += s;
-        pre[w] = acc;
-    }
-    wthr.resize(nw);
-    for (long w = 0; w < nw; ++w) wthr[w] = thrOf(pre[w] / acc);
+    std::vector<double> rowSum(nw);
     pthr.assign(nw * np, 4294967296ull);
+    for (long w = 0; w < nw; ++w) rowSum[w] = branchThresholds(pdf.data(), w, np, pthr.data());
+    double acc = 0.;
+    for (long w = 0; w < nw; ++w) acc += rowSum[w];
+    wthr.resize(nw);
+    double pre = 0.;
     for (long w = 0; w < nw; ++w) {
-        if (!(rowSum[w] > 0.)) continue;
-        double a = 0.;
-        std::vector<double> pp(np);
-        for (long p = 0; p < np; ++p) { a += pdf[w * np + p]; pp[p] = a; }
-        for (long p = 0; p < np; ++p) pthr[w * np + p] = thrOf(pp[p] / a);
+        pre += rowSum[w];
+        wthr[w] = cdfThreshold(pre / acc);
     }
 }
 
@@ -203,27 +188,21 @@ int buildMaterial(const double* disp, long nw, long np, const double* relax, dou
             dos[w * np + p] = disp[w * nc + 3 + 2 * p];
         }
     }
-    for (long p = 0; p < np; ++p) {
-        std::vector<double> tinv(nw, 0.);
-        for (int j = 0; j < 2; ++j) {
-            const double* c = relax + p * 8 + 4 * j;
-            if (c[0] < 0.) { delete m; return fail(MC_ERR_ARG, "Scattering times cannot be negative"); }
-            if (c[0] <= DMIN) continue;
-            double tp = std::pow(T, c[2]), ex = std::exp(-c[3] / T);
-            for (long w = 0; w < nw; ++w) tinv[w] += c[0] * std::pow(m->omega[w], c[1]) * tp * ex;
-        }
-        for (long w = 0; w < nw; ++w) m->tau[w * np + p] = 1. / tinv[w];
-    }
+    for (long p = 0; p < np; ++p)
+        for (int j = 0; j < 2; ++j)
+            if (relax[p * 8 + 4 * j] < 0.) { delete m; return fail(MC_ERR_ARG, "Scattering times cannot be negative"); }
+    // the temperature-dependent tables with the host/device formulas of
+    // mc_matbuild.h (the device build of many temperatures gives the same bits)
+    for (long w = 0; w < nw; ++w)
+        for (long p = 0; p < np; ++p) m->tau[w * np + p] = 1. / tauInverse(relax, p, m->omega[w], T);
     for (long i = 0; i < nw * np; ++i)
         if (!std::isfinite(m->tau[i])) { delete m; return fail(MC_ERR_ARG, "Scattering time model produced infinite values"); }
     for (long i = 0; i < nw * np; ++i)
         if (!(m->vel[i] > DMIN)) { delete m; return fail(MC_ERR_ARG, "Velocity must be nonzero"); }
     std::vector<double> epdf(nw * np), fpdf(nw * np), spdf(nw * np);
-    double xs = HBAR / (KB * T), es = 0., fs = 0., ss = 0., k = 0.;
+    double es = 0., fs = 0., ss = 0., k = 0.;
     for (long w = 0; w < nw; ++w) {
-        double x = xs * m->omega[w];
-        double q = x / (2. * std::sinh(x / 2.));
-        double dedT = KB * (std::fabs(x) < DEPS ? 1. - x * x / 12. : q * q);
+        const double dedT = dEdT(m->omega[w], T);
         for (long p = 0; p < np; ++p) {
             long i = w * np + p;
             epdf[i] = dedT * dos[i] * domega[w];
@@ -466,7 +445,7 @@ void setThresholds(EmitterD& E, const std::vector<double>& w) {
     double acc = 0.;
     for (double x : w) acc += x;
     double pre = 0.;
-    for (size_t i = 0; i < w.size(); ++i) { pre += w[i]; E.thr[i] = thrOf(pre / acc); }
+    for (size_t i = 0; i < w.size(); ++i) { pre += w[i]; E.thr[i] = cdfThreshold(pre / acc); }
 }
 
 }  // namespace
@@ -2420,6 +2399,104 @@ int mc_material_load(const char* dp, const char* rp, double T, mc_material_h* ou
     if ((long)a.size() < 2 + nw * (2 + 2 * np) || (long)b.size() < 8 * np)
         return fail(MC_ERR_ARG, "Array extraction failed");
     return buildMaterial(a.data() + 2, nw, np, b.data(), T, out);
+}
+
+int mc_material_create_many(const double* disp, long nw, long np, const double* relax, const double* T, int n,
+                            mc_material_h* out) {
+    if (!disp || !relax || !T || !out || n <= 0 || nw <= 0 || np <= 0 || np > 255 || nw > 65535)
+        return fail(MC_ERR_ARG, "invalid arguments");
+    for (int t = 0; t < n; ++t)
+        if (!(T[t] > 0.)) return fail(MC_ERR_ARG, "temperature must be positive");
+    for (long p = 0; p < np; ++p)
+        for (int j = 0; j < 2; ++j)
+            if (relax[p * 8 + 4 * j] < 0.) return fail(MC_ERR_ARG, "Scattering times cannot be negative");
+    int rc = ensureDevice();
+    if (rc) return rc;
+    const long nt = nw * np, nc = 2 + 2 * np;
+    std::vector<double> omega(nw), domega(nw), vel(nt), dos(nt);
+    for (long w = 0; w < nw; ++w) {
+        omega[w] = disp[w * nc];
+        domega[w] = disp[w * nc + 1];
+        for (long p = 0; p < np; ++p) {
+            vel[w * np + p] = disp[w * nc + 2 + 2 * p];
+            dos[w * np + p] = disp[w * nc + 3 + 2 * p];
+        }
+    }
+    // one device allocation: inputs, then per temperature the outputs and
+    // the pdf scratch
+    const size_t nIn = 2 * (size_t)nw + 2 * (size_t)nt + 8 * (size_t)np + (size_t)n;
+    const size_t nD = (size_t)n * ((size_t)nt + 4 + 3 * (size_t)nt + 2 * (size_t)nw);
+    const size_t nU = (size_t)n * (2 * (size_t)nw + 2 * (size_t)nt);
+    void* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, sizeof(double) * (nIn + nD) + sizeof(unsigned long long) * nU + sizeof(int) * n);
+    if (e != cudaSuccess) return cudaFail(e, "cudaMalloc");
+    std::unique_ptr<void, void (*)(void*)> hold(buf, [](void* q) { cudaFree(q); });
+    MatBuildArgs A;
+    A.nw = nw; A.np = np;
+    double* in = (double*)buf;
+    A.omega = in; in += nw;
+    A.domega = in; in += nw;
+    A.vel = in; in += nt;
+    A.dos = in; in += nt;
+    A.relax = in; in += 8 * np;
+    A.T = in; in += n;
+    A.tau = in; in += (size_t)n * nt;
+    A.sums = in; in += (size_t)n * 4;
+    A.scratch = in; in += (size_t)n * 3 * nt;
+    A.rows = in; in += (size_t)n * 2 * nw;
+    unsigned long long* u = (unsigned long long*)in;
+    A.swthr = u; u += (size_t)n * nw;
+    A.fwthr = u; u += (size_t)n * nw;
+    A.spthr = u; u += (size_t)n * nt;
+    A.fpthr = u; u += (size_t)n * nt;
+    A.status = (int*)u;
+    CK(cudaMemcpy((void*)A.omega, omega.data(), sizeof(double) * nw, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)A.domega, domega.data(), sizeof(double) * nw, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)A.vel, vel.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)A.dos, dos.data(), sizeof(double) * nt, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)A.relax, relax, sizeof(double) * 8 * np, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((void*)A.T, T, sizeof(double) * n, cudaMemcpyHostToDevice));
+    CK(launchBuildMaterials(A, n, nullptr));
+    std::vector<double> tau((size_t)n * nt), sums((size_t)n * 4);
+    std::vector<unsigned long long> thr(nU);
+    std::vector<int> status(n);
+    CK(cudaMemcpy(tau.data(), A.tau, sizeof(double) * tau.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sums.data(), A.sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(thr.data(), A.swthr, sizeof(unsigned long long) * nU, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(status.data(), A.status, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int t = 0; t < n; ++t) {
+        if (status[t]) return fail(MC_ERR_ARG, "Scattering time model produced infinite values or a velocity is zero");
+        if (!(sums[4 * t + 1] > 0.) || !(sums[4 * t + 2] > 0.)) return fail(MC_ERR_ARG, "material has no phonons to draw");
+    }
+    for (int t = 0; t < n; ++t) {
+        mc_material_s* m = new mc_material_s;
+        m->nw = nw; m->np = np; m->T = T[t];
+        m->omega = omega;
+        m->vel = vel;
+        m->tau.assign(tau.begin() + (size_t)t * nt, tau.begin() + (size_t)(t + 1) * nt);
+        m->energySum = sums[4 * t]; m->fluxSum = sums[4 * t + 1]; m->scatSum = sums[4 * t + 2];
+        m->cond = sums[4 * t + 3];
+        const unsigned long long* sw = thr.data() + (size_t)t * nw;
+        const unsigned long long* fw = thr.data() + (size_t)n * nw + (size_t)t * nw;
+        const unsigned long long* sp = thr.data() + 2 * (size_t)n * nw + (size_t)t * nt;
+        const unsigned long long* fp = thr.data() + 2 * (size_t)n * nw + (size_t)n * nt + (size_t)t * nt;
+        m->swthr.assign(sw, sw + nw);
+        m->fwthr.assign(fw, fw + nw);
+        m->spthr.assign(sp, sp + nt);
+        m->fpthr.assign(fp, fp + nt);
+        out[t] = m;
+    }
+    return MC_OK;
+}
+
+int mc_material_thresholds(mc_material_h m, uint64_t* swthr, uint64_t* spthr, uint64_t* fwthr, uint64_t* fpthr) {
+    if (!m) return fail(MC_ERR_ARG, "null argument");
+    const size_t nw = (size_t)m->nw, nt = (size_t)m->nw * m->np;
+    if (swthr) std::memcpy(swthr, m->swthr.data(), 8 * nw);
+    if (spthr) std::memcpy(spthr, m->spthr.data(), 8 * nt);
+    if (fwthr) std::memcpy(fwthr, m->fwthr.data(), 8 * nw);
+    if (fpthr) std::memcpy(fpthr, m->fpthr.data(), 8 * nt);
+    return MC_OK;
 }
 
 int mc_material_sums(mc_material_h m, double out[4]) {

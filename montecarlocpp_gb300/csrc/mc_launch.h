@@ -40,6 +40,21 @@ template <typename R>
 cudaError_t launchRoundReduce(const Params<R>& p, double* const* accs, double* gsum,
                               cudaStream_t s);
 
+// device build of the temperature-dependent Material tables of n
+// temperatures (mc_material_create_many); all arrays device memory, per
+// temperature t at offset t * (nw, nw * np, 4) of each output
+struct MatBuildArgs {
+    long nw, np;
+    const double *omega, *domega, *vel, *dos, *relax, *T;
+    double* tau;
+    double* sums;     // energySum, fluxSum, scatSum, cond
+    unsigned long long *swthr, *spthr, *fwthr, *fpthr;
+    double* scratch;  // 3 nw np per temperature
+    double* rows;     // 2 nw per temperature
+    int* status;      // 1: a non-finite relaxation time or a zero velocity
+};
+cudaError_t launchBuildMaterials(const MatBuildArgs& a, int n, cudaStream_t s);
+
 // the bounded-wait self-check (mc_check_bounded_wait)
 cudaError_t launchWaitCheck(unsigned* status, unsigned long long limitNs, unsigned long long* waitedNs,
                             cudaStream_t s);

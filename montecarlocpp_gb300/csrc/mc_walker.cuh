@@ -583,7 +583,9 @@ __device__ __forceinline__ void fly(Phn<R>& ph, const SdomD<R>& S, const R a[3],
     // crossings; they wait for one another after it, so that the event code
     // that follows runs once for all of them rather than once per exit
     // (measured: 4.2 of 32 lanes active per instruction on the pore cell
-    // without it, the kernel 2.1x slower)
+    // without it, the kernel 2.1x slower; a walk that shares all lanes'
+    // segments out over the warp gained a further 2% only, for spilled
+    // registers)
     const unsigned walkers = __activemask();
     const int s0 = S.tstride[1], s01 = S.tstride[2];
     for (int guard = 0; guard < 3 * MAX_SHAPE + 4; ++guard) {

@@ -55,6 +55,39 @@ class Material:
     def silicon(cls, T=300.0, model=None):
         return cls(T=T, tables=silicon_tables(model))
 
+    @classmethod
+    def many(cls, temperatures, tables=None):
+        """Material(disp, relax, T) for every T of `temperatures`, the
+        temperature-dependent tables built on the GPU in one launch
+        (mc_material_create_many); each equals Material(T=T, tables=...)
+        bit for bit. tables: (disp, relax), default the silicon model."""
+        d, r = (np.ascontiguousarray(x, dtype=np.float64) for x in (tables or silicon_tables()))
+        Ts = np.ascontiguousarray(temperatures, dtype=np.float64)
+        hs = (C.c_void_p * len(Ts))()
+        _lib.check(_lib.lib().mc_material_create_many(_dp(d), d.shape[0], (d.shape[1] - 2) // 2, _dp(r), _dp(Ts),
+                                                      len(Ts), hs))
+        out = []
+        for h, T in zip(hs, Ts):
+            m = cls.__new__(cls)
+            m.h = C.c_void_p(h)
+            m.nw, m.np = d.shape[0], (d.shape[1] - 2) // 2
+            m.T = float(T)
+            m._sums = np.zeros(4)
+            _lib.check(_lib.lib().mc_material_sums(m.h, _dp(m._sums)))
+            out.append(m)
+        return out
+
+    def thresholds(self):
+        """Inverse-CDF thresholds (scattering bins, scattering branches, flux
+        bins, flux branches) as uint64 arrays."""
+        sw = np.zeros(self.nw, dtype=np.uint64)
+        sp = np.zeros((self.nw, self.np), dtype=np.uint64)
+        fw = np.zeros(self.nw, dtype=np.uint64)
+        fp = np.zeros((self.nw, self.np), dtype=np.uint64)
+        u = lambda a: a.ctypes.data_as(C.POINTER(C.c_uint64))
+        _lib.check(_lib.lib().mc_material_thresholds(self.h, u(sw), u(sp), u(fw), u(fp)))
+        return sw, sp, fw, fp
+
     def temp(self):
         return self.T
 

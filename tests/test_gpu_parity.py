@@ -5,8 +5,10 @@ Tolerances (stated per test):
 * trajectories, FP64 flight: loop index, subdomains, face hit, cell, nscat,
   w, p identical; positions within 1e-12 of the domain size; times 1e-12
   relative;
-* trajectories, FP32 flight: the same discrete fields identical; positions
-  within 1e-5 of the domain size;
+* trajectories, FP32 flight: the same discrete fields identical except in
+  as many trajectories as the measured FP32 discrete-mismatch rate allows
+  (test_gpu_statistics.mismatch_allowance); positions within 1e-5 of the
+  domain size;
 * fields, FP64 flight: within 1e-9 of each row's largest magnitude;
 * statistics: kappa within 3 standard errors of the oracle.
 """
@@ -16,6 +18,7 @@ import pytest
 
 import montecarlocpp_gb300 as M
 from oracle import oracle as O
+from test_gpu_statistics import mismatch_allowance
 
 pytestmark = pytest.mark.gpu
 
@@ -114,8 +117,11 @@ def test_fp32_trajectories(name, gmat, omat):
     kind, nemit, dt, nsteps = CASES[name]
     (oo, ost, olog), (go, gst, glog) = run_pair(gmat, omat, dom, kind, nemit, dt, nsteps, 32, 50)
     # FP32 directions carry ~1e-7 relative rounding; a wall reached at a
-    # grazing angle a turns a transverse error d into d / a along the wall
-    bad, _ = compare_logs(olog, glog, dom.max_dim(), 1e-5, allow_mismatch=1, pos_quantile=0.99, pos_cap=1e-3)
+    # grazing angle a turns a transverse error d into d / a along the wall.
+    # Trajectories that part from the FP64 ones: at most as many as the
+    # measured FP32 mismatch rate over this horizon allows
+    allow = mismatch_allowance(name, dt * nsteps, len(olog[1]))
+    bad, _ = compare_logs(olog, glog, dom.max_dim(), 1e-5, allow_mismatch=allow, pos_quantile=0.99, pos_cap=1e-3)
     # the per-result FP32 error of the field against the FP64 oracle
     assert field_err(oo, go) < 5e-3
 
@@ -133,7 +139,8 @@ def test_replay_of_reference_stream(prec, tol, gmat, omat):
     if prec == 64:
         compare_logs(olog, glog, dom.max_dim(), tol)
     else:
-        compare_logs(olog, glog, dom.max_dim(), tol, allow_mismatch=1, pos_quantile=0.99, pos_cap=1e-3)
+        allow = mismatch_allowance("film", 0.5e-12 * 300, len(olog[1]))
+        compare_logs(olog, glog, dom.max_dim(), tol, allow_mismatch=allow, pos_quantile=0.99, pos_cap=1e-3)
     if prec == 64:
         assert gst["events"] == ost["events"]
         assert field_err(oo, go) < 1e-9

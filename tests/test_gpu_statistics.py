@@ -25,7 +25,7 @@ Mismatch rate: the fraction of FP32 trajectories whose discrete fields
 (cells, subdomains, faces, event counts, scatter counts, frequency bins,
 branches) differ from the FP64 oracle's at or before a horizon, with both
 fed the same uniform words (replay of the oracle's mt19937 stream), on
-10^4 phonons of the in-plane film and of the pore cell.
+10^4 phonons of the in-plane film, the pore cell and the cross-plane film.
 """
 
 import numpy as np
@@ -145,30 +145,43 @@ def slab_index(dom, nslab=16):
 
 
 # ----------------------------------------------------------- mismatch rate
-HORIZON_STEPS = (250, 500, 1000, 2000)
-# Measured FP32 discrete-mismatch rates (fraction of 10^4 trajectories that
-# diverged from the FP64 trajectory at or before each horizon, same words),
-# the allowance of the FP32 trajectory comparisons in test_gpu_parity.py.
+# Measured FP32 discrete-mismatch rates: the fraction of trajectories that
+# parted from the FP64 trajectory of the same uniform words at or before
+# each horizon, the larger of two measurements on 10^4 phonons each (replay
+# of the oracle's mt19937 stream over 2000 and over 4000 steps of 0.5 ps;
+# the bench's `precision.discrete_mismatch` measures the same against the
+# FP64 kernels over the whole 4000-step horizon). A rate measured as zero
+# is taken as 1 / 10^4. Keys: the horizon in ns. These rates set the
+# allowance of every FP32 trajectory comparison (test_gpu_parity.py).
 MISMATCH_RATE = {
-    "film": {250: 0.002, 500: 0.004, 1000: 0.008, 2000: 0.016},
-    "pore": {250: 0.003, 500: 0.006, 1000: 0.012, 2000: 0.024},
+    "film": {0.125: 1e-4, 0.25: 2e-4, 0.5: 1.4e-3, 1.0: 6.5e-3, 1.5: 2.0e-2, 2.0: 4.3e-2},
+    "pore": {0.125: 1e-4, 0.25: 1e-4, 0.5: 4e-4, 1.0: 1.1e-3, 1.5: 1.6e-3, 2.0: 3.1e-3},
+    "cross": {0.25: 1e-4, 0.5: 1e-4, 1.0: 1e-4, 2.0: 1e-4},
+}
+MISMATCH_CASES = {  # domain, dt, dt-steps of each measured horizon
+    "film": (lambda: M.FilmDomain.from_cli(1e-7, 1e-7, 100), 0.5e-12, (250, 500, 1000, 2000)),
+    "pore": (lambda: M.PoreCellDomain(5e-7, 2.5e-7), 0.5e-12, (250, 500, 1000, 2000)),
+    "cross": (lambda: M.CrossPlaneFilmDomain(1e-7, 1e-7, 20), 1e-12, (250, 500, 1000, 2000)),
 }
 
 
-def mismatch_allowance(name, nsteps, n):
-    """Trajectories of n that may differ at horizon nsteps: the 99.9%
-    quantile of Binomial(n, measured rate) (the rate of the next measured
-    horizon at or above nsteps)."""
+def mismatch_allowance(name, horizon_s, n):
+    """Trajectories of n that may differ over a horizon of horizon_s
+    seconds: the 99.9% quantile of Binomial(n, measured rate), the rate of
+    the first measured horizon at or beyond it (the film's for domains
+    without a measurement of their own)."""
     from scipy import stats
-    rates = MISMATCH_RATE[name]
-    h = min([x for x in rates if x >= nsteps] or [max(rates)])
+    rates = MISMATCH_RATE.get(name, MISMATCH_RATE["film"])
+    ns = horizon_s * 1e9
+    h = min([x for x in rates if x >= ns * (1 - 1e-9)] or [max(rates)])
     return int(stats.binom.ppf(0.999, n, rates[h]))
 
 
-@pytest.mark.parametrize("name", ["film", "pore"])
+@pytest.mark.parametrize("name", list(MISMATCH_CASES))
 def test_fp32_discrete_mismatch_rate(name, gmat, omat):
-    dom = {"film": M.FilmDomain.from_cli(1e-7, 1e-7, 100), "pore": M.PoreCellDomain(5e-7, 2.5e-7)}[name]
-    n, dt, nsteps, cap = 10_000, 0.5e-12, max(HORIZON_STEPS), 320
+    make, dt, horizons = MISMATCH_CASES[name]
+    dom = make()
+    n, nsteps, cap = 10_000, max(horizons), 320
     od = O.ODomain(dom)
     _, ost, ex = O.solve(omat, od, O.MULTI, nemit=n, maxscat=10**6, dt=dt, horizon=dt * nsteps, rng=O.RNG_MT,
                          nchunk=16, seed=3, record_cap=4096, log_cap=cap, log_phonons=n)
@@ -181,11 +194,11 @@ def test_fp32_discrete_mismatch_rate(name, gmat, omat):
             replay=O.record_to_replay(ex["record"], pad=4096), log_cap=cap, log_phonons=n)
     assert P.stats["status"] == 0
     tdiv = divergence_times(olog, P.log)
-    rates = mismatch_rate(tdiv, [h * dt for h in HORIZON_STEPS])
-    print(f"{name}: FP32 mismatch rate at {HORIZON_STEPS} steps: {rates}")
-    for h, r in zip(HORIZON_STEPS, rates):
+    rates = mismatch_rate(tdiv, [h * dt for h in horizons])
+    print(f"{name}: FP32 mismatch rate at {horizons} steps of {dt:g} s: {rates}")
+    for h, r in zip(horizons, rates):
         # the measured rate, with the binomial spread of 10^4 trajectories
-        assert r * n <= mismatch_allowance(name, h, n), (h, r)
+        assert r * n <= mismatch_allowance(name, h * dt, n), (h, r)
     # the FP64 path replays the same words without a single mismatch
     P.solve(dt=dt, nsteps=nsteps, precision=64, steps_per_launch=100, replay=O.record_to_replay(ex["record"]),
             log_cap=cap, log_phonons=n)
