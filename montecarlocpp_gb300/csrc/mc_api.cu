@@ -1017,8 +1017,9 @@ int setupSession(mc_session_s* S) {
     const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
     S->tm = S->desc.tally_mode;
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
-    S->block = S->desc.block_size > 0 ? S->desc.block_size : 256;
-    if (S->block % 32 || S->block > 256) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    const int maxBlock = S->dyn ? 256 : MC_STATIC_CONSUMERS;
+    S->block = S->desc.block_size > 0 ? S->desc.block_size : maxBlock;
+    if (S->block % 32 || S->block > maxBlock) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
     // static schedule with a shared 1-D field along one axis in every
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
@@ -1032,9 +1033,10 @@ int setupSession(mc_session_s* S) {
     // FP32 lean flights tally into a carry-free copy of the field (exact
     // while a block runs at most 65536 of them per launch, checked below)
     const bool split = S->lean >= 0 && sizeof(R) == 4;
+    P.tabGlobal = (!S->dyn && MC_STATIC_TABLES_GLOBAL) ? 1 : 0;
     {
         const SmemLayout L = singleLayout<R>((int)m.nw, (int)m.np, (int)D.sd.size(), S->rows, (int)D.cols,
-                                             S->tm == TM_SHARED, split);
+                                             S->tm == TM_SHARED, split, !P.tabGlobal);
         S->smem = L.total;
         setSingleLayout(P, L);
         // static schedule: the state stages after the tables

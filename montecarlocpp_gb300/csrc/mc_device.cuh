@@ -94,6 +94,7 @@ struct Params {
     // (setBatchLayout)
     int smVt, smWthr, smGuide, smSd, smTal, smStage;
     int smSplit;       // carry-free lean-flight field, 0 if none
+    int tabGlobal;     // 1: vel * tau and the guide table read from global memory
     int smVel;  // batched launches: their layout's vel table (0 otherwise)
     uint32_t key0, key1;
     // state (ping-pong halves chosen by the host)

@@ -32,19 +32,20 @@ template <typename R, int TM>
 __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned char* smraw) {
     const int nt = P.nw * P.np;
     const int nsdShared = P.nsd;
-    const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED);
+    const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED, false, !P.tabGlobal);
     R* vel = reinterpret_cast<R*>(smraw + L.vel);
-    R* vt = reinterpret_cast<R*>(smraw + L.vt);
+    R* vt = P.tabGlobal ? const_cast<R*>(P.vt) : reinterpret_cast<R*>(smraw + L.vt);
     unsigned long long* wthr = reinterpret_cast<unsigned long long*>(smraw + L.wthr);
-    uint16_t* wguide = reinterpret_cast<uint16_t*>(smraw + L.guide);
+    uint16_t* wguide = P.tabGlobal ? const_cast<uint16_t*>(P.wguide) : reinterpret_cast<uint16_t*>(smraw + L.guide);
     long long* tal = reinterpret_cast<long long*>(smraw + L.tal);
     InstD<R>* I = reinterpret_cast<InstD<R>*>(smraw + L.inst);
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         vel[i] = P.vel[i];
-        vt[i] = P.vt[i];
+        if (!P.tabGlobal) vt[i] = P.vt[i];
     }
     for (int i = threadIdx.x; i < P.nw; i += blockDim.x) wthr[i] = P.wthr[i];
-    for (int i = threadIdx.x; i < GUIDE; i += blockDim.x) wguide[i] = P.wguide[i];
+    if (!P.tabGlobal)
+        for (int i = threadIdx.x; i < GUIDE; i += blockDim.x) wguide[i] = P.wguide[i];
     const SdomD<R>* sd = P.sd;
     if (nsdShared) {
         const int nw4 = (int)(sizeof(SdomD<R>) * nsdShared / 4);
@@ -262,9 +263,9 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // or plain flights), and no global atomic is involved. Step and
 // event counts are summed per thread and added to the block's counters
 // once, at the end.
-constexpr int STATIC_STAGES = 2;
+constexpr int STATIC_STAGES = MC_STATIC_STAGES;
 constexpr int STATIC_PRODUCER_THREADS = 32;
-constexpr int STATIC_MAX_THREADS = 256 + STATIC_PRODUCER_THREADS;
+constexpr int STATIC_MAX_THREADS = MC_STATIC_CONSUMERS + STATIC_PRODUCER_THREADS;
 constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
 constexpr unsigned STATIC_BACK = 1u << 30;    // stage tag: a tile of the back range
 // bounded waits: a bulk copy lands within microseconds; the producer may

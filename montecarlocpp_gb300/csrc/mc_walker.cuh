@@ -24,14 +24,14 @@ struct SmemLayout {
     size_t vel = 0, vt = 0, wthr = 0, guide = 0, sd = 0, inst = 0, tal = 0, split = 0, total = 0;
     template <typename R>
     __host__ __device__ void init(int nw, int np, int nsdShared, int rows, int cols, bool sharedTally,
-                                  bool splitTally = false) {
+                                  bool splitTally = false, bool tabShared = true) {
         auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
         const size_t nt = (size_t)nw * np;
         vel = 0;
         vt = vel + sizeof(R) * nt;
-        wthr = al(vt + sizeof(R) * nt);
+        wthr = al(vt + (tabShared ? sizeof(R) * nt : 0));
         guide = al(wthr + sizeof(unsigned long long) * (size_t)nw);
-        sd = al(guide + sizeof(uint16_t) * GUIDE);
+        sd = al(guide + (tabShared ? sizeof(uint16_t) * GUIDE : 0));
         inst = al(sd + sizeof(SdomD<R>) * (size_t)nsdShared);
         tal = al(inst + sizeof(InstD<R>));
         total = tal + (sharedTally ? sizeof(long long) * talEntries(rows, cols) : 0);
@@ -48,9 +48,9 @@ struct SmemLayout {
 // splitTally: the lean flights' carry-free field (below) after the tally.
 template <typename R>
 __host__ __device__ inline SmemLayout singleLayout(int nw, int np, int nsd, int rows, int cols, bool sharedTally,
-                                                   bool splitTally = false) {
+                                                   bool splitTally = false, bool tabShared = true) {
     SmemLayout L;
-    L.init<R>(nw, np, nsd, rows, cols, sharedTally, splitTally);
+    L.init<R>(nw, np, nsd, rows, cols, sharedTally, splitTally, tabShared);
     return L;
 }
 
@@ -111,6 +111,19 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 // producer warp) per SM: three, which its shared-memory stages also fit.
 #ifndef MC_MIN_BLOCKS_STATIC_F32
 #define MC_MIN_BLOCKS_STATIC_F32 3
+#endif
+// The static kernel's consumer threads per block at most (and its default
+// block size), its shared-memory stages of the state stream, and whether it
+// reads the vel * tau and guide tables (used at scatters only) from global
+// memory instead of staging them, which leaves room for more stages.
+#ifndef MC_STATIC_CONSUMERS
+#define MC_STATIC_CONSUMERS 256
+#endif
+#ifndef MC_STATIC_STAGES
+#define MC_STATIC_STAGES 2
+#endif
+#ifndef MC_STATIC_TABLES_GLOBAL
+#define MC_STATIC_TABLES_GLOBAL 0
 #endif
 
 template <typename R>
@@ -285,11 +298,15 @@ struct ParamView {
     __device__ __forceinline__ R tqinv(int r) const { return P->tqinv[r]; }
     __device__ __forceinline__ const SdomD<R>* sd() const { return reinterpret_cast<const SdomD<R>*>(sm + P->smSd); }
     __device__ __forceinline__ const R* vel() const { return reinterpret_cast<const R*>(sm); }
-    __device__ __forceinline__ const R* vt() const { return reinterpret_cast<const R*>(sm + P->smVt); }
+    __device__ __forceinline__ const R* vt() const {
+        return P->tabGlobal ? P->vt : reinterpret_cast<const R*>(sm + P->smVt);
+    }
     __device__ __forceinline__ const unsigned long long* wthr() const {
         return reinterpret_cast<const unsigned long long*>(sm + P->smWthr);
     }
-    __device__ __forceinline__ const uint16_t* wguide() const { return reinterpret_cast<const uint16_t*>(sm + P->smGuide); }
+    __device__ __forceinline__ const uint16_t* wguide() const {
+        return P->tabGlobal ? P->wguide : reinterpret_cast<const uint16_t*>(sm + P->smGuide);
+    }
     __device__ __forceinline__ const unsigned long long* pthr() const { return P->pthr; }
     __device__ __forceinline__ uint32_t key0() const { return P->key0; }
     __device__ __forceinline__ uint32_t key1() const { return P->key1; }
