@@ -230,7 +230,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     W = dict(WORKLOAD)
-    sample = int(os.environ.get("MC_REF_SAMPLE", 200_000))
+    sample = int(os.environ.get("MC_REF_SAMPLE", 1_000_000))
     for _ in range(args.warmup):
         cpu_baseline(W, sample)
     vals = []
@@ -432,7 +432,7 @@ def main():
         line["served"] = sv
     if rank == 0 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = cpu_baseline(W, int(os.environ.get("MC_CPU_SAMPLE", 400_000)))
+            line["cpu_baseline"] = cpu_baseline(W, int(os.environ.get("MC_CPU_SAMPLE", 4_000_000)))
             if "precision" in line:
                 # the reference computes in FP64: the GPU's FP64 flight beside the FP32 headline
                 line["precision"]["fp64_vs_cpu"] = (line["precision"]["fp64_phonon_steps_per_s"] /
@@ -957,7 +957,7 @@ def discrete_mismatch(n=10_000, nsteps=4000, dt=0.5e-12, cap=1024, seed=5):
     return out
 
 
-def bench_pore_cpu(sample=100_000):
+def bench_pore_cpu(sample=1_000_000):
     """CPU baseline of config 2: the oracle on a sample of the pore cell's
     phonons (50^3 grid, full 4000-step horizon)."""
     import montecarlocpp_gb300 as M
