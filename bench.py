@@ -624,7 +624,7 @@ def bench_batched(stream, reps=2, plain=True):
     return out
 
 
-def plain_on_requests(reqs, doms, mats, done, done_idx, nsteps, sample=8, cap=10_000_000, warm=20, timed=200):
+def plain_on_requests(reqs, doms, mats, done, done_idx, nsteps, sample=32, cap=10_000_000, warm=20, timed=200):
     """The plain single-instance kernel (one dt-step per launch, full FP64
     field) on a sample of the completed requests: its phonon-steps/s on each
     request's own geometry and temperature, and the time it would take for

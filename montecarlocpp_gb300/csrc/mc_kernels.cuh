@@ -264,6 +264,12 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // event counts are summed per thread and added to the block's counters
 // once, at the end.
 constexpr int STATIC_STAGES = MC_STATIC_STAGES;
+// 1: the consumers walk the front range with lane refill from global
+// memory and the stream carries the back range only; 0: both ranges go
+// through the stream, front tiles first, one phonon per lane
+#ifndef MC_STATIC_FRONT_DYNAMIC
+#define MC_STATIC_FRONT_DYNAMIC 0
+#endif
 constexpr int STATIC_PRODUCER_THREADS = 32;
 constexpr int STATIC_MAX_THREADS = MC_STATIC_CONSUMERS + STATIC_PRODUCER_THREADS;
 constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
@@ -309,6 +315,7 @@ k_advance(Params<R> P) {
     __shared__ unsigned sCnt[STATIC_STAGES];
     __shared__ unsigned sOut[2];
     __shared__ int sStop;
+    __shared__ unsigned long long sFront;
     const int T = (int)blockDim.x - STATIC_PRODUCER_THREADS;
     const int nCw = T >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -327,6 +334,7 @@ k_advance(Params<R> P) {
         }
         sStop = 0;
         sOut[0] = sOut[1] = 0u;
+        sFront = 0ull;
         mbarInitFence();
     }
     __syncthreads();
@@ -338,7 +346,10 @@ k_advance(Params<R> P) {
             const unsigned long long nF = min((unsigned long long)P.regIn[2 * blockIdx.x], (unsigned long long)C);
             const unsigned long long nB =
                 min((unsigned long long)P.regIn[2 * blockIdx.x + 1], (unsigned long long)C - nF);
-            const long long tF = ((long long)nF + T - 1) / T, tB = ((long long)nB + T - 1) / T;
+            // with the front range walked by the consumers straight from
+            // global memory, the stream carries the back range only
+            const long long tF = MC_STATIC_FRONT_DYNAMIC ? 0 : ((long long)nF + T - 1) / T;
+            const long long tB = ((long long)nB + T - 1) / T;
             const uint32_t perPhonon = (uint32_t)(2 * sizeof(V4) + sizeof(uint4));
             long long jF = 0, jB = 0;
             int j = 0;
@@ -392,6 +403,69 @@ k_advance(Params<R> P) {
         W.init(P);
         const unsigned lt = (1u << lane) - 1u;
         unsigned long long nSteps = 0, nEvents = 0;
+        if constexpr (MC_STATIC_FRONT_DYNAMIC != 0) {
+            // The front range (phonons with an event in this window) first,
+            // walked with lane refill straight from global memory while the
+            // producer already streams the back range: a lane whose phonon
+            // is done takes the next one, so no warp waits for its slowest
+            // lane as it would with one phonon per lane per tile.
+            const unsigned long long nF = min((unsigned long long)P.regIn[2 * blockIdx.x], (unsigned long long)C);
+            Walker<R, REPLAY, LOG, TM, ParamView<R, TM>, true, GEN> wk;
+            bool have = false;
+            bool drained = nF == 0;
+            for (int guard = 0; guard < (1 << 30); ++guard) {
+                const unsigned idle = __ballot_sync(0xFFFFFFFFu, !have);
+                if (!drained && idle) {
+                    unsigned long long b = 0;
+                    if (lane == 0) b = atomicAdd(&sFront, (unsigned long long)__popc(idle));
+                    b = __shfl_sync(0xFFFFFFFFu, b, 0);
+                    if (b + __popc(idle) >= nF) drained = true;
+                    if (!have) {
+                        const unsigned long long my = b + __popc(idle & lt);
+                        if (my < nF) {
+                            const long long src = rbase + (long long)my;
+                            V4 A0, A1;
+                            const uint4 A2 = __ldcs(P.P2in + src);
+                            ld4(P.P0in + src, A0);
+                            ld4(P.P1in + src, A1);
+                            wk.load(P, V, W, A0, A1, A2);
+                            have = true;
+                        }
+                    }
+                }
+                if (__ballot_sync(0xFFFFFFFFu, have) == 0) {
+                    if (drained) break;
+                    continue;
+                }
+                bool fin = false, alive = false, soon = false;
+                V4 A0, A1;
+                uint4 A2;
+                if (have && wk.iterate(P, W)) {
+                    fin = true;
+                    alive = wk.finishInto(P, W, nSteps, nEvents);
+                    soon = wk.tnext < W.next;
+                    if (alive) wk.pack(A0, A1, A2);
+                    have = false;
+                }
+                const unsigned mf = __ballot_sync(0xFFFFFFFFu, fin && alive && soon);
+                const unsigned mb = __ballot_sync(0xFFFFFFFFu, fin && alive && !soon);
+                if (mf | mb) {
+                    unsigned bf = 0, bb = 0;
+                    if (lane == 0) {
+                        if (mf) bf = atomicAdd(&sOut[0], (unsigned)__popc(mf));
+                        if (mb) bb = atomicAdd(&sOut[1], (unsigned)__popc(mb));
+                    }
+                    bf = __shfl_sync(0xFFFFFFFFu, bf, 0);
+                    bb = __shfl_sync(0xFFFFFFFFu, bb, 0);
+                    if (fin && alive) {
+                        const long long o = soon ? rbase + bf + __popc(mf & lt) : rbase + C - 1 - (bb + __popc(mb & lt));
+                        st4(P.P0out + o, A0);
+                        st4(P.P1out + o, A1);
+                        __stcs(P.P2out + o, A2);
+                    }
+                }
+            }
+        }
         for (int j = 0;; ++j) {
             const int s = j % STATIC_STAGES;
             const uint32_t use = (uint32_t)(j / STATIC_STAGES);
@@ -484,8 +558,13 @@ k_advance(Params<R> P) {
 // keeps its lanes busy by refilling finished lanes whenever at least REFILL
 // of them are idle, so a long phonon no longer holds up its warp. Survivors
 // are written back in place; dead slots get PROP_DEAD (skipped until the
-// host compacts).
-constexpr int REFILL = 8;
+// host compacts). Refilling as soon as one lane is idle measured fastest on
+// the film over a whole horizon (90.2 ms against 93.1 at 4, 98.3 at 8, 109
+// at 16): an idle lane costs more than the refill's shared atomic and loads.
+#ifndef MC_REFILL
+#define MC_REFILL 1
+#endif
+constexpr int REFILL = MC_REFILL;
 
 template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool GEN = false>
 __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
@@ -508,11 +587,13 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
             if (!have) {
                 const unsigned long long my = b + __popc(idle & lt);
                 if (my < qend) {
+                    // all three words at once (one memory round trip, not
+                    // two); a dead slot's position and direction go unused
                     typename Vec4<R>::T A0, A1;
-                    uint4 A2 = __ldcs(P.P2in + my);
+                    const uint4 A2 = __ldcs(P.P2in + my);
+                    ld4(P.P0in + my, A0);
+                    ld4(P.P1in + my, A1);
                     if (!(A2.y & PROP_DEAD)) {
-                        ld4(P.P0in + my, A0);
-                        ld4(P.P1in + my, A1);
                         wk.load(P, I, W, A0, A1, A2);
                         have = true;
                         slot = my;

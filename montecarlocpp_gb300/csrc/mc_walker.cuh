@@ -856,6 +856,7 @@ struct Walker {
     R budget;
     R tnext;       // time to the next event after the window end
     int nev;       // events in this window
+    int nsc;       // relaxation-time scatters in this window
     int stop;      // 0 alive, else the counter of the stop reason
     // the replay stream's position persists across events; a Philox stream
     // is set up afresh at each event from (key, phonon id, event index)
@@ -883,6 +884,7 @@ struct Walker {
         iv = R(1) / v;
         stop = 0;
         nev = 0;
+        nsc = 0;
         tnext = R(0);
     }
 
@@ -1028,7 +1030,7 @@ struct Walker {
             ph.scatNext = drawScatNext<R>(g, I.vt()[ph.w * I.np() + ph.p]);
             v = I.vel()[ph.w * I.np() + ph.p];
             iv = R(1) / v;
-            blkCount(C_SCATTERS, 1);
+            ++nsc;
         } else if (kind == F_SPEC) {  // montecarlo/boundary.cpp:283-287
             R nd = (F->n[0] * ph.d[0] + F->n[1] * ph.d[1]) + F->n[2] * ph.d[2];
             for (int j = 0; j < 3; ++j) ph.d[j] -= R(2) * nd * F->n[j];
@@ -1137,6 +1139,9 @@ struct Walker {
         const bool alive = close(P, W, st);
         blkCount(C_PHONON_STEPS, (unsigned)st);
         blkCount(C_EVENTS, (unsigned)nev);
+        // counted per window rather than per scatter: one block-counter add
+        // per phonon instead of one per event
+        if (nsc) blkCount(C_SCATTERS, (unsigned)nsc);
         return alive;
     }
 
@@ -1148,6 +1153,7 @@ struct Walker {
         const bool alive = close(P, W, st);
         steps += (unsigned)st;
         events += (unsigned)nev;
+        if (nsc) blkCount(C_SCATTERS, (unsigned)nsc);
         return alive;
     }
 
