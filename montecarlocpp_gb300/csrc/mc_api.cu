@@ -896,13 +896,17 @@ int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vma
     for (size_t i = 0; i < nt; ++i) { vel[i] = (R)m.vel[i]; vt[i] = (R)(m.vel[i] * m.tau[i]); }
     vmax = 0.;
     for (size_t i = 0; i < nt; ++i) vmax = std::max(vmax, m.vel[i]);
+    // every table 16-byte aligned (the kernels stage them by bulk copies)
+    auto al16 = [](char* b) { return (char*)(((uintptr_t)b + 15) & ~(uintptr_t)15); };
     P.vel = (R*)base; base += sizeof(R) * nt;
+    base = al16(base);
     P.vt = (R*)base; base += sizeof(R) * nt;
-    base = (char*)(((uintptr_t)base + 15) & ~(uintptr_t)15);
+    base = al16(base);
     P.wthr = (unsigned long long*)base; base += 8 * m.nw;
     P.pthr = (unsigned long long*)base; base += 8 * nt;
     P.fwthr = (unsigned long long*)base; base += 8 * m.nw;
     P.fpthr = (unsigned long long*)base; base += 8 * nt;
+    base = al16(base);
     P.wguide = (const uint16_t*)base; base += 2 * GUIDE;
     CK(cudaMemcpy((void*)P.vel, vel.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
     CK(cudaMemcpy((void*)P.vt, vt.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));

@@ -85,6 +85,15 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// Programmatic dependent launch (sm_90+). A kernel launched with the
+// programmatic stream-serialization attribute may start while the kernel
+// before it in the stream is still running; gridDepWait blocks until that
+// kernel has completed and its memory writes are visible (a no-op without
+// such a predecessor), gridDepTrigger lets the next such kernel be scheduled
+// as this one's blocks exit.
+__device__ __forceinline__ void gridDepWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void gridDepTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Named barrier `id` over `nthreads` threads (a multiple of 32) that also
 // returns the OR of `pred` over them: every participant gets the same answer.
 __device__ __forceinline__ bool barOr(int id, int nthreads, bool pred) {

@@ -26,10 +26,39 @@
 
 namespace mcg {
 
+// One constant table into shared memory: its 16-byte-aligned body by a
+// bulk copy (the TMA engine, completing on a block mbarrier), the rest
+// element by element by all threads. A table whose source or destination
+// is not 16-byte aligned is copied by the threads whole.
+template <typename T>
+struct TableCopy {
+    T* dst;
+    const T* src;
+    int n;
+    uint32_t body;  // bytes the bulk copy takes
+    __device__ __forceinline__ TableCopy(T* d, const T* s, int count) : dst(d), src(s), n(count) {
+        const bool aligned = MC_TABLE_BULK && count > 0 && (((uintptr_t)s | (uintptr_t)smemAddr(d)) & 15) == 0;
+        body = aligned ? (uint32_t)((sizeof(T) * (size_t)count) & ~(size_t)15) : 0u;
+    }
+    // thread 0: the bulk copy, after the barrier expects its bytes
+    __device__ __forceinline__ void issue(uint64_t* bar) const {
+        if (body) bulkLoad(dst, src, body, bar);
+    }
+    __device__ __forceinline__ void rest() const {
+        for (int i = (int)(body / sizeof(T)) + (int)threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+    }
+};
+
+// A bounded wait on the table copies of stageTables (they complete in
+// microseconds; the limit only keeps a broken copy from hanging the block)
+constexpr uint64_t TABLE_COPY_WAIT_NS = 1000000000ull;
+
 // Instance descriptor of a single-instance launch, around the tables it
-// staged in shared memory.
+// staged in shared memory. The tables go in by bulk copies, so a block's
+// staging costs about one round trip rather than one per loop iteration.
 template <typename R, int TM>
 __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned char* smraw) {
+    __shared__ uint64_t barTab;
     const int nt = P.nw * P.np;
     const int nsdShared = P.nsd;
     const SmemLayout L = singleLayout<R>(P.nw, P.np, P.nsd, P.rows, P.cols, TM == TM_SHARED, false, !P.tabGlobal);
@@ -39,21 +68,28 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
     uint16_t* wguide = P.tabGlobal ? const_cast<uint16_t*>(P.wguide) : reinterpret_cast<uint16_t*>(smraw + L.guide);
     long long* tal = reinterpret_cast<long long*>(smraw + L.tal);
     InstD<R>* I = reinterpret_cast<InstD<R>*>(smraw + L.inst);
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        vel[i] = P.vel[i];
-        if (!P.tabGlobal) vt[i] = P.vt[i];
+    const TableCopy<R> cVel(vel, P.vel, nt);
+    const TableCopy<R> cVt(vt, P.vt, P.tabGlobal ? 0 : nt);
+    const TableCopy<uint16_t> cGuide(wguide, P.wguide, P.tabGlobal ? 0 : GUIDE);
+    const TableCopy<unsigned long long> cWthr(wthr, P.wthr, P.nw);
+    const TableCopy<uint32_t> cSd(reinterpret_cast<uint32_t*>(smraw + L.sd), reinterpret_cast<const uint32_t*>(P.sd),
+                                  (int)(sizeof(SdomD<R>) * nsdShared / 4));
+    const SdomD<R>* sd = nsdShared ? reinterpret_cast<const SdomD<R>*>(smraw + L.sd) : P.sd;
+    if (threadIdx.x == 0) {
+        mbarInit(&barTab, 1);
+        mbarInitFence();
+        mbarArriveExpectTx(&barTab, cVel.body + cVt.body + cGuide.body + cWthr.body + cSd.body);
+        cVel.issue(&barTab);
+        cVt.issue(&barTab);
+        cGuide.issue(&barTab);
+        cWthr.issue(&barTab);
+        cSd.issue(&barTab);
     }
-    for (int i = threadIdx.x; i < P.nw; i += blockDim.x) wthr[i] = P.wthr[i];
-    if (!P.tabGlobal)
-        for (int i = threadIdx.x; i < GUIDE; i += blockDim.x) wguide[i] = P.wguide[i];
-    const SdomD<R>* sd = P.sd;
-    if (nsdShared) {
-        const int nw4 = (int)(sizeof(SdomD<R>) * nsdShared / 4);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(smraw + L.sd);
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(P.sd);
-        for (int i = threadIdx.x; i < nw4; i += blockDim.x) dst[i] = src[i];
-        sd = reinterpret_cast<const SdomD<R>*>(smraw + L.sd);
-    }
+    cVel.rest();
+    cVt.rest();
+    cGuide.rest();
+    cWthr.rest();
+    cSd.rest();
     if (TM == TM_SHARED) {
         const int nz = (int)talEntries(P.rows, P.cols);
         for (int i = threadIdx.x; i < nz; i += blockDim.x) tal[i] = 0;
@@ -77,6 +113,8 @@ __device__ __forceinline__ InstD<R>* stageTables(const Params<R>& P, unsigned ch
         I->groups = 1; I->gstride = 0; I->flags = 0;
         for (int r = 0; r < 4; ++r) { I->tqinv[r] = P.tqinv[r]; I->tq[r] = P.tq[r]; }
     }
+    __syncthreads();  // the barrier's initialisation seen by every thread
+    if (!mbarWait(&barTab, 0u, TABLE_COPY_WAIT_NS)) atomicOr(P.status, (unsigned)S_TIMEOUT);
     return I;
 }
 
@@ -264,12 +302,6 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // event counts are summed per thread and added to the block's counters
 // once, at the end.
 constexpr int STATIC_STAGES = MC_STATIC_STAGES;
-// 1: the consumers walk the front range with lane refill from global
-// memory and the stream carries the back range only; 0: both ranges go
-// through the stream, front tiles first, one phonon per lane
-#ifndef MC_STATIC_FRONT_DYNAMIC
-#define MC_STATIC_FRONT_DYNAMIC 0
-#endif
 constexpr int STATIC_PRODUCER_THREADS = 32;
 constexpr int STATIC_MAX_THREADS = MC_STATIC_CONSUMERS + STATIC_PRODUCER_THREADS;
 constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
@@ -315,10 +347,10 @@ k_advance(Params<R> P) {
     __shared__ unsigned sCnt[STATIC_STAGES];
     __shared__ unsigned sOut[2];
     __shared__ int sStop;
-    __shared__ unsigned long long sFront;
     const int T = (int)blockDim.x - STATIC_PRODUCER_THREADS;
     const int nCw = T >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if constexpr (MC_PDL != 0) gridDepTrigger();
     InstD<R>* I = stageTables<R, TM>(P, smraw);
     ParamView<R, TM> V;
     V.init(P, smraw);
@@ -334,10 +366,12 @@ k_advance(Params<R> P) {
         }
         sStop = 0;
         sOut[0] = sOut[1] = 0u;
-        sFront = 0ull;
         mbarInitFence();
     }
     __syncthreads();
+    // the tables are constant; the state, the region counts and the field
+    // belong to the previous launch until it has completed
+    if constexpr (MC_PDL != 0) gridDepWait();
 
     if (warp == nCw) {
         // ---------------------------------------------------- producer
@@ -346,9 +380,7 @@ k_advance(Params<R> P) {
             const unsigned long long nF = min((unsigned long long)P.regIn[2 * blockIdx.x], (unsigned long long)C);
             const unsigned long long nB =
                 min((unsigned long long)P.regIn[2 * blockIdx.x + 1], (unsigned long long)C - nF);
-            // with the front range walked by the consumers straight from
-            // global memory, the stream carries the back range only
-            const long long tF = MC_STATIC_FRONT_DYNAMIC ? 0 : ((long long)nF + T - 1) / T;
+            const long long tF = ((long long)nF + T - 1) / T;
             const long long tB = ((long long)nB + T - 1) / T;
             const uint32_t perPhonon = (uint32_t)(2 * sizeof(V4) + sizeof(uint4));
             long long jF = 0, jB = 0;
@@ -403,69 +435,6 @@ k_advance(Params<R> P) {
         W.init(P);
         const unsigned lt = (1u << lane) - 1u;
         unsigned long long nSteps = 0, nEvents = 0;
-        if constexpr (MC_STATIC_FRONT_DYNAMIC != 0) {
-            // The front range (phonons with an event in this window) first,
-            // walked with lane refill straight from global memory while the
-            // producer already streams the back range: a lane whose phonon
-            // is done takes the next one, so no warp waits for its slowest
-            // lane as it would with one phonon per lane per tile.
-            const unsigned long long nF = min((unsigned long long)P.regIn[2 * blockIdx.x], (unsigned long long)C);
-            Walker<R, REPLAY, LOG, TM, ParamView<R, TM>, true, GEN> wk;
-            bool have = false;
-            bool drained = nF == 0;
-            for (int guard = 0; guard < (1 << 30); ++guard) {
-                const unsigned idle = __ballot_sync(0xFFFFFFFFu, !have);
-                if (!drained && idle) {
-                    unsigned long long b = 0;
-                    if (lane == 0) b = atomicAdd(&sFront, (unsigned long long)__popc(idle));
-                    b = __shfl_sync(0xFFFFFFFFu, b, 0);
-                    if (b + __popc(idle) >= nF) drained = true;
-                    if (!have) {
-                        const unsigned long long my = b + __popc(idle & lt);
-                        if (my < nF) {
-                            const long long src = rbase + (long long)my;
-                            V4 A0, A1;
-                            const uint4 A2 = __ldcs(P.P2in + src);
-                            ld4(P.P0in + src, A0);
-                            ld4(P.P1in + src, A1);
-                            wk.load(P, V, W, A0, A1, A2);
-                            have = true;
-                        }
-                    }
-                }
-                if (__ballot_sync(0xFFFFFFFFu, have) == 0) {
-                    if (drained) break;
-                    continue;
-                }
-                bool fin = false, alive = false, soon = false;
-                V4 A0, A1;
-                uint4 A2;
-                if (have && wk.iterate(P, W)) {
-                    fin = true;
-                    alive = wk.finishInto(P, W, nSteps, nEvents);
-                    soon = wk.tnext < W.next;
-                    if (alive) wk.pack(A0, A1, A2);
-                    have = false;
-                }
-                const unsigned mf = __ballot_sync(0xFFFFFFFFu, fin && alive && soon);
-                const unsigned mb = __ballot_sync(0xFFFFFFFFu, fin && alive && !soon);
-                if (mf | mb) {
-                    unsigned bf = 0, bb = 0;
-                    if (lane == 0) {
-                        if (mf) bf = atomicAdd(&sOut[0], (unsigned)__popc(mf));
-                        if (mb) bb = atomicAdd(&sOut[1], (unsigned)__popc(mb));
-                    }
-                    bf = __shfl_sync(0xFFFFFFFFu, bf, 0);
-                    bb = __shfl_sync(0xFFFFFFFFu, bb, 0);
-                    if (fin && alive) {
-                        const long long o = soon ? rbase + bf + __popc(mf & lt) : rbase + C - 1 - (bb + __popc(mb & lt));
-                        st4(P.P0out + o, A0);
-                        st4(P.P1out + o, A1);
-                        __stcs(P.P2out + o, A2);
-                    }
-                }
-            }
-        }
         for (int j = 0;; ++j) {
             const int s = j % STATIC_STAGES;
             const uint32_t use = (uint32_t)(j / STATIC_STAGES);

@@ -12,6 +12,29 @@ static cudaError_t prepare(K fn, size_t smem) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
+// A static-kernel launch; with MC_PDL, programmatic dependent launch: the
+// kernel may begin while the previous kernel of the stream finishes (it
+// waits for it before touching shared state, griddepcontrol.wait).
+template <typename K, typename R>
+static cudaError_t launchStatic(K fn, const Params<R>& p, int grid, int threads, size_t smem, cudaStream_t s) {
+    if constexpr (MC_PDL != 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, fn, p);
+    } else {
+        fn<<<grid, threads, smem, s>>>(p);
+        return cudaGetLastError();
+    }
+}
+
 // GEN: the kernels that also take subdomains other than the Parallelepiped,
 // continuation slots and Inter faces paired more than once.
 template <typename R, bool DYN, bool REPLAY, bool LOG, int TM, bool GEN = false>
@@ -20,7 +43,8 @@ static cudaError_t advanceOne(const Params<R>& p, int grid, int block, size_t sm
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
     // the static kernel adds its producer warp to the `block` consumers
-    fn<<<grid, DYN ? block : block + STATIC_PRODUCER_THREADS, smem, s>>>(p);
+    if (!DYN) return launchStatic(fn, p, grid, block + STATIC_PRODUCER_THREADS, smem, s);
+    fn<<<grid, block, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -44,8 +68,7 @@ cudaError_t launchAdvanceLean<MC_REAL>(const Params<MC_REAL>& p, int lean, int g
                         : k_advance<MC_REAL, false, false, TM_SHARED, 2>;
     cudaError_t e = prepare(fn, smem);
     if (e != cudaSuccess) return e;
-    fn<<<grid, block + STATIC_PRODUCER_THREADS, smem, s>>>(p);
-    return cudaGetLastError();
+    return launchStatic(fn, p, grid, block + STATIC_PRODUCER_THREADS, smem, s);
 }
 
 template <>

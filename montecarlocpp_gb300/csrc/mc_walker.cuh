@@ -28,7 +28,7 @@ struct SmemLayout {
         auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
         const size_t nt = (size_t)nw * np;
         vel = 0;
-        vt = vel + sizeof(R) * nt;
+        vt = al(vel + sizeof(R) * nt);
         wthr = al(vt + (tabShared ? sizeof(R) * nt : 0));
         guide = al(wthr + sizeof(unsigned long long) * (size_t)nw);
         sd = al(guide + (tabShared ? sizeof(uint16_t) * GUIDE : 0));
@@ -124,6 +124,18 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 #endif
 #ifndef MC_STATIC_TABLES_GLOBAL
 #define MC_STATIC_TABLES_GLOBAL 0
+#endif
+// Programmatic dependent launch of the static kernel: launch k + 1's blocks
+// stage their tables and initialise their barriers while launch k's last
+// blocks finish, and wait for launch k to complete before they touch the
+// state, the region counts or the field.
+#ifndef MC_PDL
+#define MC_PDL 1
+#endif
+// Constant tables staged by bulk copies (else by the threads, one element
+// per thread per loop iteration).
+#ifndef MC_TABLE_BULK
+#define MC_TABLE_BULK 1
 #endif
 
 template <typename R>
