@@ -174,7 +174,8 @@ typedef struct {
     int precision;          /* 32: FP32 flight, 64: FP64 flight; tallies FP64 */
     uint64_t seed;          /* Philox key                                  */
     int steps_per_launch;   /* K dt-steps per advance launch (>= 1)        */
-    int block_size;         /* 0 -> 256                                    */
+    int block_size;         /* 0 -> 256 (static schedule, FP32 flight: 768
+                               consumer threads and a producer warp)       */
     int grid_blocks;        /* 0 -> resident blocks x SMs                  */
     int tally_mode;         /* MC_TALLY_*                                  */
     /* replay: per-phonon 32-bit words, offsets has nemit+1 entries (host) */

@@ -1021,9 +1021,11 @@ int setupSession(mc_session_s* S) {
     const size_t tallyB = smemTallyBytes(S->rows, (int)D.cols);
     S->tm = S->desc.tally_mode;
     if (S->tm == MC_TALLY_AUTO) S->tm = tallyB <= 32 * 1024 ? TM_SHARED : TM_GLOBAL;
-    const int maxBlock = S->dyn ? 256 : MC_STATIC_CONSUMERS;
+    const int maxBlock = S->dyn ? 256 : staticConsumers<R>();
     S->block = S->desc.block_size > 0 ? S->desc.block_size : maxBlock;
-    if (S->block % 32 || S->block > maxBlock) return fail(MC_ERR_ARG, "block_size must be a multiple of 32, <= 256");
+    if (S->block % 32 || S->block > maxBlock)
+        return fail(MC_ERR_ARG, S->dyn || sizeof(R) == 8 ? "block_size must be a multiple of 32, <= 256"
+                                                         : "block_size must be a multiple of 32, <= 768");
     // static schedule with a shared 1-D field along one axis in every
     // subdomain (and no replay or log): the kernel with the lean flight
     S->lean = -1;
@@ -1035,7 +1037,8 @@ int setupSession(mc_session_s* S) {
         if (same) S->lean = k;
     }
     // FP32 lean flights tally into a carry-free copy of the field (exact
-    // while a block runs at most 65536 of them per launch, checked below)
+    // while a block runs at most SPLIT_MAX_FLIGHTS of them per launch,
+    // checked below)
     const bool split = S->lean >= 0 && sizeof(R) == 4;
     P.tabGlobal = (!S->dyn && MC_STATIC_TABLES_GLOBAL) ? 1 : 0;
     {
@@ -1054,7 +1057,7 @@ int setupSession(mc_session_s* S) {
                            : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
-    if (split && (S->nemit + S->grid - 1) / S->grid > 65536) {
+    if (split && (S->nemit + S->grid - 1) / S->grid > SPLIT_MAX_FLIGHTS) {
         // too many phonons per block for the carry-free copy: the walker
         // for every phonon
         S->lean = -1;
@@ -1136,12 +1139,13 @@ int emitT(mc_session_s* S) {
 
 // Fixed-point quantum of the tallies for one row. `flight` bounds what one
 // phonon adds in a window (the window itself for time rows, vmax x window
-// for displacement rows). FP32 flight: 2^-30 of it, so that every flight's
-// amount converts to a 32-bit integer; a block's sums (at most `perBlock`
-// phonons x 2^30) stay inside int64. FP64 flight: 2^-61 of perBlock x
-// flight, converted to 64 bits.
+// for displacement rows). FP32 flight: 2^-29 of it, so that every flight's
+// amount converts to a 32-bit integer with a bit to spare for the lean
+// flights' carry-free field; a block's sums (at most `perBlock` phonons x
+// 2^29) stay inside int64. FP64 flight: 2^-61 of perBlock x flight,
+// converted to 64 bits.
 double tallyQuantum(bool f32, double flight, double perBlock) {
-    return f32 ? std::ldexp(flight * 1.0001, -30) : std::ldexp(perBlock * flight * 1.0001, -61);
+    return f32 ? std::ldexp(flight * 1.0001, -29) : std::ldexp(perBlock * flight * 1.0001, -61);
 }
 
 template <typename R>

@@ -181,7 +181,7 @@ __device__ __forceinline__ void closeBlock(const Params<R>& P, const InstD<R>& I
         const unsigned* lo = reinterpret_cast<const unsigned*>(base + P.smSplit);
         const int* hi = reinterpret_cast<const int*>(lo) + nz;
         for (int e = threadIdx.x; e < nz; e += blockDim.x) {
-            const long long v = (long long)hi[e] * 65536 + (long long)lo[e];
+            const long long v = (long long)hi[e] * (1LL << SPLIT_LOW_BITS) + (long long)lo[e];
             if (v != 0) I.tal[e] += v;
         }
         __syncthreads();
@@ -303,7 +303,16 @@ __global__ void __launch_bounds__(256) k_emit_batch(Params<R> P) {
 // once, at the end.
 constexpr int STATIC_STAGES = MC_STATIC_STAGES;
 constexpr int STATIC_PRODUCER_THREADS = 32;
-constexpr int STATIC_MAX_THREADS = MC_STATIC_CONSUMERS + STATIC_PRODUCER_THREADS;
+// consumer threads per block at most (the default block size) and threads
+// per block at most, by flight precision
+template <typename R>
+__host__ __device__ constexpr int staticConsumers() {
+    return sizeof(R) == 4 ? MC_STATIC_CONSUMERS : MC_STATIC_CONSUMERS_F64;
+}
+template <typename R>
+__host__ __device__ constexpr int staticMaxThreads() {
+    return staticConsumers<R>() + STATIC_PRODUCER_THREADS;
+}
 constexpr unsigned STATIC_END = 0xFFFFFFFFu;  // stage marker: no more tiles
 constexpr unsigned STATIC_BACK = 1u << 30;    // stage tag: a tile of the back range
 // bounded waits: a bulk copy lands within microseconds; the producer may
@@ -338,7 +347,7 @@ inline void setSingleLayout(Params<R>& P, const SmemLayout& L) {
 // the front range, for a back-range phonon that does meet an event, and in
 // the window that ends the horizon.
 template <typename R, bool REPLAY, bool LOG, int TM, int LEAN, bool GEN = false>
-__global__ void __launch_bounds__(STATIC_MAX_THREADS, sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
+__global__ void __launch_bounds__(staticMaxThreads<R>(), sizeof(R) == 4 ? MC_MIN_BLOCKS_STATIC_F32 : 2)
 k_advance(Params<R> P) {
     static_assert(LEAN < 0 || (!REPLAY && !LOG && TM == TM_SHARED), "the lean flight needs a plain shared-field launch");
     using V4 = typename Vec4<R>::T;

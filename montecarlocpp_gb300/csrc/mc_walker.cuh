@@ -107,17 +107,27 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 #ifndef MC_MIN_BLOCKS_F32
 #define MC_MIN_BLOCKS_F32 3
 #endif
-// Resident blocks of the static kernel (256 consumer threads and one
-// producer warp) per SM: three, which its shared-memory stages also fit.
+// Resident blocks of the FP32 static kernel per SM: one block of 768
+// consumer threads and a producer warp. Three blocks of 256 consumers (the
+// same warps per SM) measured 4 % slower over a whole horizon: each block
+// streams its own region, and an SM whose first block finished early ran
+// its last block with a third of the warps (blocks' finishing times spread
+// over 20 % of a launch); one block per SM shares its tiles among all the
+// SM's warps, so they finish together.
 #ifndef MC_MIN_BLOCKS_STATIC_F32
-#define MC_MIN_BLOCKS_STATIC_F32 3
+#define MC_MIN_BLOCKS_STATIC_F32 1
 #endif
 // The static kernel's consumer threads per block at most (and its default
-// block size), its shared-memory stages of the state stream, and whether it
-// reads the vel * tau and guide tables (used at scatters only) from global
-// memory instead of staging them, which leaves room for more stages.
+// block size) in FP32 and in FP64 flight (two resident blocks of 256 leave
+// the FP64 walker its registers), its shared-memory stages of the state
+// stream, and whether it reads the vel * tau and guide tables (used at
+// scatters only) from global memory instead of staging them, which leaves
+// room for more stages.
 #ifndef MC_STATIC_CONSUMERS
-#define MC_STATIC_CONSUMERS 256
+#define MC_STATIC_CONSUMERS 768
+#endif
+#ifndef MC_STATIC_CONSUMERS_F64
+#define MC_STATIC_CONSUMERS_F64 256
 #endif
 #ifndef MC_STATIC_STAGES
 #define MC_STATIC_STAGES 2
@@ -151,7 +161,7 @@ struct Phn {
 };
 
 // Fixed-point amount of a flight. FP32 flight: the quantum gives the
-// largest single flight 2^30 units, so one 32-bit round-to-nearest
+// largest single flight 2^29 units, so one 32-bit round-to-nearest
 // conversion suffices (|v| < 2^31); sums are kept in 64 bits. FP64 flight:
 // 64-bit conversion against a quantum sized for a block's total.
 __device__ __forceinline__ int toFixed(float v) { return __float2int_rn(v); }
@@ -371,11 +381,17 @@ struct BatchView {
 
 // Field accumulation for one flight of one instance.
 // SPLIT (FP32 lean flights only): adds go to a carry-free copy of the
-// shared field instead -- the low 16 bits of the amount into one 32-bit
+// shared field instead -- the low 15 bits of the amount into one 32-bit
 // word, the rest (arithmetic shift) into another, both without a returned
-// value. A lean flight adds to an entry at most once and a block runs at
-// most regCap <= 65536 of them per launch, so neither word can overflow;
-// closeBlock folds the copy into the 64-bit field.
+// value. A lean flight adds to an entry at most once, |amount| <= 2^29, and
+// a block runs at most regCap <= 131072 of them per launch, so neither word
+// can overflow (131072 x (2^15 - 1) < 2^32 unsigned; 131072 x 2^14 = 2^31
+// signed); closeBlock folds the copy into the 64-bit field.
+constexpr int SPLIT_LOW_BITS = 15;
+constexpr unsigned SPLIT_LOW_MASK = (1u << SPLIT_LOW_BITS) - 1u;
+// lean flights per block per launch the carry-free copy holds exactly
+constexpr long long SPLIT_MAX_FLIGHTS = 131072;
+
 template <typename R, int TM, typename IA, bool SPLIT = false>
 struct Tally {
     IA V;
@@ -399,8 +415,8 @@ struct Tally {
     // [c * talStride(rows) + r]
     __device__ __forceinline__ void splitAdd(int e, Fix v) const {
         unsigned* lo = V.split();
-        atomicAdd(lo + e, (unsigned)v & 0xFFFFu);
-        atomicAdd(reinterpret_cast<int*>(lo) + V.entries() + e, (int)(v >> 16));
+        atomicAdd(lo + e, (unsigned)v & SPLIT_LOW_MASK);
+        atomicAdd(reinterpret_cast<int*>(lo) + V.entries() + e, (int)(v >> SPLIT_LOW_BITS));
     }
     __device__ __forceinline__ void atomShared(int r, int col, Fix v) const {
         if constexpr (SPLIT) splitAdd(col * talStride(V.rows()) + rowBase + r, v);
