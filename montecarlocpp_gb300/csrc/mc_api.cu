@@ -1057,9 +1057,17 @@ int setupSession(mc_session_s* S) {
                            : advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
     if (occ <= 0) return fail(MC_ERR_UNSUPPORTED, "advance kernel cannot launch with this configuration");
     S->grid = S->desc.grid_blocks > 0 ? S->desc.grid_blocks : occ * nsm;
+    if (split && S->desc.grid_blocks == 0 && (S->nemit + S->grid - 1) / S->grid > SPLIT_MAX_FLIGHTS) {
+        // whole waves of resident blocks rather than more phonons per block
+        // than the carry-free copy holds (a partial last wave would run its
+        // few blocks alone)
+        const long long need = (S->nemit + SPLIT_MAX_FLIGHTS - 1) / SPLIT_MAX_FLIGHTS;
+        const long long wave = (long long)occ * nsm;
+        S->grid = (int)((need + wave - 1) / wave * wave);
+    }
     if (split && (S->nemit + S->grid - 1) / S->grid > SPLIT_MAX_FLIGHTS) {
-        // too many phonons per block for the carry-free copy: the walker
-        // for every phonon
+        // too many phonons per block of a requested grid for the carry-free
+        // copy: the walker for every phonon
         S->lean = -1;
         P.smSplit = 0;
         occ = advanceOccupancy<R>(S->dyn, S->replay, S->logging, S->tm, S->gen, S->block, S->smem);
@@ -1139,13 +1147,14 @@ int emitT(mc_session_s* S) {
 
 // Fixed-point quantum of the tallies for one row. `flight` bounds what one
 // phonon adds in a window (the window itself for time rows, vmax x window
-// for displacement rows). FP32 flight: 2^-29 of it, so that every flight's
-// amount converts to a 32-bit integer with a bit to spare for the lean
-// flights' carry-free field; a block's sums (at most `perBlock` phonons x
-// 2^29) stay inside int64. FP64 flight: 2^-61 of perBlock x flight,
-// converted to 64 bits.
+// for displacement rows). FP32 flight: 2^-27 of it, so that every flight's
+// amount converts to a 32-bit integer with room for the lean flights'
+// carry-free field (2^18 flights per block); a block's sums (at most
+// `perBlock` phonons x 2^27) stay inside int64. The quantum is 7.5e-9 of
+// the largest flight, below the FP32 flight's own rounding. FP64 flight:
+// 2^-61 of perBlock x flight, converted to 64 bits.
 double tallyQuantum(bool f32, double flight, double perBlock) {
-    return f32 ? std::ldexp(flight * 1.0001, -29) : std::ldexp(perBlock * flight * 1.0001, -61);
+    return f32 ? std::ldexp(flight * 1.0001, -27) : std::ldexp(perBlock * flight * 1.0001, -61);
 }
 
 template <typename R>

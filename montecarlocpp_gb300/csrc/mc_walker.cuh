@@ -161,7 +161,7 @@ struct Phn {
 };
 
 // Fixed-point amount of a flight. FP32 flight: the quantum gives the
-// largest single flight 2^29 units, so one 32-bit round-to-nearest
+// largest single flight 2^27 units, so one 32-bit round-to-nearest
 // conversion suffices (|v| < 2^31); sums are kept in 64 bits. FP64 flight:
 // 64-bit conversion against a quantum sized for a block's total.
 __device__ __forceinline__ int toFixed(float v) { return __float2int_rn(v); }
@@ -381,16 +381,17 @@ struct BatchView {
 
 // Field accumulation for one flight of one instance.
 // SPLIT (FP32 lean flights only): adds go to a carry-free copy of the
-// shared field instead -- the low 15 bits of the amount into one 32-bit
+// shared field instead -- the low 14 bits of the amount into one 32-bit
 // word, the rest (arithmetic shift) into another, both without a returned
-// value. A lean flight adds to an entry at most once, |amount| <= 2^29, and
-// a block runs at most regCap <= 131072 of them per launch, so neither word
-// can overflow (131072 x (2^15 - 1) < 2^32 unsigned; 131072 x 2^14 = 2^31
-// signed); closeBlock folds the copy into the 64-bit field.
-constexpr int SPLIT_LOW_BITS = 15;
+// value. A lean flight adds to an entry at most once, |amount| < 2^27, and
+// a block runs at most regCap <= 2^18 of them per launch, so neither word
+// can overflow (2^18 x (2^14 - 1) < 2^32 unsigned; 2^18 x 2^13 = 2^31
+// signed, reached only by the most negative amounts); closeBlock folds the
+// copy into the 64-bit field.
+constexpr int SPLIT_LOW_BITS = 14;
 constexpr unsigned SPLIT_LOW_MASK = (1u << SPLIT_LOW_BITS) - 1u;
 // lean flights per block per launch the carry-free copy holds exactly
-constexpr long long SPLIT_MAX_FLIGHTS = 131072;
+constexpr long long SPLIT_MAX_FLIGHTS = 262144;
 
 template <typename R, int TM, typename IA, bool SPLIT = false>
 struct Tally {

@@ -444,3 +444,23 @@ def test_static_regions_in_unusual_launch_shapes(nemit, block, grid, prec, gmat)
     assert ss["status"] == 0
     tol = 1e-12 if prec == 64 else 1e-5
     assert field_err(d, s) < tol
+
+
+def test_static_lean_kernel_with_more_phonons_than_one_wave_holds(gmat):
+    """4.2e7 phonons of the in-plane film: more per resident block than the
+    lean flights' carry-free field holds in one launch (2^18 on 152 SMs), so
+    the per-step kernel runs whole extra waves of blocks. The trajectories
+    equal the dynamic schedule's (counters) and the fields agree to FP32
+    flight precision."""
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 100)
+    P = M.MultiProblem(gmat, dom, 42_000_000, 10**6)
+    kw = dict(dt=0.5e-12, nsteps=12, precision=32, seed=23)
+    s = P.solve(steps_per_launch=1, schedule=1, **kw)
+    ss = dict(P.stats)
+    d = P.solve(steps_per_launch=12, schedule=2, **kw)
+    sd = dict(P.stats)
+    assert ss["status"] == 0 and sd["status"] == 0
+    for k in ("events", "scatters", "absorbed", "escapes"):
+        assert ss[k] == sd[k], k
+    assert abs(ss["phonon_steps"] - sd["phonon_steps"]) <= 1e-5 * sd["phonon_steps"] + 1
+    assert field_err(d, s) < 1e-5
