@@ -976,8 +976,9 @@ int setupSession(mc_session_s* S) {
     if (rc) return rc;
     rc = uploadDomain<R>(D, m.fluxSum, S->desc.nemit, &S->dom_d, &S->em_d, &S->cdf_d, P, S->nemit, S->power);
     if (rc) return rc;
-    // counters: C_NCOUNTERS + two (front, back) live-count pairs
-    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 4)));
+    // counters: C_NCOUNTERS + two (front, back) live-count pairs + the
+    // dynamic launches' slot counter
+    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 5)));
     CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
     S->rows = (int)problemRows(S->desc.problem, S->desc.cum_size);
     CK(cudaMalloc(&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L)));
@@ -992,6 +993,7 @@ int setupSession(mc_session_s* S) {
     P.key0 = (uint32_t)S->desc.seed;
     P.key1 = (uint32_t)(S->desc.seed >> 32);
     P.counters = S->cnt_d;
+    P.qglobal = (sizeof(R) == 4 && MC_DYN_GLOBAL_QUEUE) ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
     P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;
@@ -1190,6 +1192,10 @@ int advanceT(mc_session_s* S, int nl, int* done) {
             P.live_in = cur;
             P.live_out = cur + 1;
             CK(cudaMemsetAsync(cur + 1, 0, sizeof(unsigned long long), S->stream));
+            // one launch-wide slot counter only for long windows: a claim
+            // per refilled lane is then rare enough for one address
+            if (P.wKeff < MC_DYN_QUEUE_MIN_STEPS) P.qglobal = nullptr;
+            if (P.qglobal) CK(cudaMemsetAsync(P.qglobal, 0, sizeof(unsigned long long), S->stream));
             CK(launchAdvance<R>(P, true, S->replay, S->logging, S->tm, S->gen, S->grid, S->block, S->smem,
                                 S->stream));
             S->launches++;
@@ -2289,7 +2295,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     const size_t oP0 = take(sizeof(V4) * n);
     const size_t oP1 = take(sizeof(V4) * n);
     const size_t oP2 = take(sizeof(uint4) * n);
-    const size_t oCnt = take(sizeof(unsigned long long) * (C_NCOUNTERS + 4));
+    const size_t oCnt = take(sizeof(unsigned long long) * (C_NCOUNTERS + 5));
     const size_t oStatus = take(sizeof(unsigned int));
     const size_t oTally = take(sizeof(double) * nval);
     const size_t oCsum = take(sizeof(double) * 4);
@@ -2365,6 +2371,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     P.key0 = (uint32_t)S->desc.seed;
     P.key1 = (uint32_t)(S->desc.seed >> 32);
     P.counters = S->cnt_d;
+    P.qglobal = (sizeof(R) == 4 && MC_DYN_GLOBAL_QUEUE) ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
     P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;

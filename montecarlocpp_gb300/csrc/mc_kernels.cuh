@@ -606,7 +606,11 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
     if (lane == 0 && x) atomicAdd(&P.live_out[0], x);
 }
 
-// Block b owns the live slots [b C, (b + 1) C) of the launch.
+// Every block claims slots of [0, n) from the launch-wide counter
+// P.qglobal, so blocks (and the SMs they run on) keep taking phonons until
+// none is left and finish within about one phonon's work of one another;
+// without it (FP64 flight, whose tally quantum bounds what one block adds),
+// block b owns the live slots [b C, (b + 1) C).
 template <typename R, bool REPLAY, bool LOG, int TM, bool GEN = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
     extern __shared__ __align__(128) unsigned char smraw[];
@@ -618,12 +622,18 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k
     Window<R> W;
     W.init(P);
     const unsigned long long n = P.live_in[0];
-    const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
-    const unsigned long long qbeg = min((unsigned long long)blockIdx.x * chunk, n);
-    const unsigned long long qend = min(qbeg + chunk, n);
+    unsigned long long* q = &qnext;
+    unsigned long long qbeg = 0, qend = n;
+    if (sizeof(R) == 8 || P.qglobal == nullptr) {
+        const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
+        qbeg = min((unsigned long long)blockIdx.x * chunk, n);
+        qend = min(qbeg + chunk, n);
+    } else {
+        q = P.qglobal;
+    }
     ParamView<R, TM> V;
     V.init(P, smraw);
-    dynamicLoop<R, REPLAY, LOG, TM, ParamView<R, TM>, GEN>(P, &qnext, qbeg, qend, V, W);
+    dynamicLoop<R, REPLAY, LOG, TM, ParamView<R, TM>, GEN>(P, q, qbeg, qend, V, W);
     closeBlock<R, TM>(P, *I);
 }
 

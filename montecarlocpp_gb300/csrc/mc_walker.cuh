@@ -142,6 +142,15 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 #ifndef MC_PDL
 #define MC_PDL 1
 #endif
+// FP32 single-instance dynamic launches claim slots from one launch-wide
+// counter (else each block from its own share).
+#ifndef MC_DYN_GLOBAL_QUEUE
+#define MC_DYN_GLOBAL_QUEUE 1
+#endif
+// dt-steps per window from which a launch uses that counter
+#ifndef MC_DYN_QUEUE_MIN_STEPS
+#define MC_DYN_QUEUE_MIN_STEPS 1024
+#endif
 // Constant tables staged by bulk copies (else by the threads, one element
 // per thread per loop iteration).
 #ifndef MC_TABLE_BULK
