@@ -464,3 +464,23 @@ def test_static_lean_kernel_with_more_phonons_than_one_wave_holds(gmat):
         assert ss[k] == sd[k], k
     assert abs(ss["phonon_steps"] - sd["phonon_steps"]) <= 1e-5 * sd["phonon_steps"] + 1
     assert field_err(d, s) < 1e-5
+
+
+def test_launch_wide_slot_counter_matches_static_schedule(gmat):
+    """FP32 flight with windows of 2000 dt-steps: the fused kernel's blocks
+    claim slots from one launch-wide counter (windows of 1024 steps or more)
+    while the static schedule streams block-owned regions through the same
+    windows. Same phonons and windows, same trajectories: equal counters;
+    the fields differ only by the order of the FP64 adds of the blocks'
+    fixed-point fields."""
+    dom = M.FilmDomain.from_cli(1e-7, 1e-7, 100)
+    P = M.MultiProblem(gmat, dom, 300_000, 10**6)
+    kw = dict(dt=0.5e-12, nsteps=2000, precision=32, steps_per_launch=2000, seed=29)
+    a = P.solve(schedule=2, **kw)
+    sa = dict(P.stats)
+    c = P.solve(schedule=1, **kw)
+    sc = dict(P.stats)
+    for k in ("events", "scatters", "absorbed", "escapes", "horizon_stops", "phonon_steps"):
+        assert sa[k] == sc[k], k
+    assert sa["status"] == sc["status"] == 0
+    assert field_err(a, c) < 1e-12
