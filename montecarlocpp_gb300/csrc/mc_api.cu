@@ -993,7 +993,7 @@ int setupSession(mc_session_s* S) {
     P.key0 = (uint32_t)S->desc.seed;
     P.key1 = (uint32_t)(S->desc.seed >> 32);
     P.counters = S->cnt_d;
-    P.qglobal = (sizeof(R) == 4 && MC_DYN_GLOBAL_QUEUE) ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
+    P.qglobal = MC_DYN_GLOBAL_QUEUE ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
     P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;
@@ -2371,7 +2371,7 @@ int placeSession(mc_session_s* S, char* base, size_t cap) {
     P.key0 = (uint32_t)S->desc.seed;
     P.key1 = (uint32_t)(S->desc.seed >> 32);
     P.counters = S->cnt_d;
-    P.qglobal = (sizeof(R) == 4 && MC_DYN_GLOBAL_QUEUE) ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
+    P.qglobal = MC_DYN_GLOBAL_QUEUE ? S->cnt_d + C_NCOUNTERS + 4 : nullptr;
     P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;

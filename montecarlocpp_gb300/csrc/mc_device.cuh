@@ -106,9 +106,9 @@ struct Params {
     // from the back, so that warps see phonons of one kind
     const unsigned long long* live_in;
     unsigned long long* live_out;
-    // single-instance dynamic launches in FP32 flight: the launch-wide slot
-    // counter every block claims from (zeroed before each launch); null:
-    // each block claims from its own share of the slots
+    // single-instance dynamic launches of long windows: the launch-wide
+    // slot counter every block claims from (zeroed before each launch);
+    // null: each block claims from its own share of the slots
     unsigned long long* qglobal;
     unsigned long long cap;
     // static schedule: block b of the (fixed) grid owns the slots

@@ -544,10 +544,13 @@ k_advance(Params<R> P) {
 #endif
 constexpr int REFILL = MC_REFILL;
 
+// cap (with the block's shared counter `claimed`): a block stops claiming
+// once it holds that many slots (0: no limit).
 template <typename R, bool REPLAY, bool LOG, int TM, typename IA, bool GEN = false>
 __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long long* qnext,
                                             unsigned long long qbeg, unsigned long long qend,
-                                            const IA& I, const Window<R>& W) {
+                                            const IA& I, const Window<R>& W,
+                                            unsigned long long cap = 0, unsigned long long* claimed = nullptr) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     Walker<R, REPLAY, LOG, TM, IA, false, GEN> wk;
@@ -559,7 +562,10 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
         const unsigned idle = __ballot_sync(0xFFFFFFFFu, !have);
         if (!drained && (idle == 0xFFFFFFFFu || __popc(idle) >= REFILL)) {
             unsigned long long b = 0;
-            if (lane == 0) b = qbeg + atomicAdd(qnext, (unsigned long long)__popc(idle));
+            if (lane == 0) {
+                const bool full = cap != 0 && atomicAdd(claimed, (unsigned long long)__popc(idle)) >= cap;
+                b = full ? qend : qbeg + atomicAdd(qnext, (unsigned long long)__popc(idle));
+            }
             b = __shfl_sync(0xFFFFFFFFu, b, 0);
             if (b + __popc(idle) >= qend) drained = true;
             if (!have) {
@@ -609,31 +615,33 @@ __device__ __forceinline__ void dynamicLoop(const Params<R>& P, unsigned long lo
 // Every block claims slots of [0, n) from the launch-wide counter
 // P.qglobal, so blocks (and the SMs they run on) keep taking phonons until
 // none is left and finish within about one phonon's work of one another;
-// without it (FP64 flight, whose tally quantum bounds what one block adds),
-// block b owns the live slots [b C, (b + 1) C).
+// without it (short windows), block b owns the live slots [b C, (b + 1) C).
+// In FP64 flight the tally quantum bounds a block's sum for C phonons with
+// 4x headroom, so a block claims at most 2 C slots.
 template <typename R, bool REPLAY, bool LOG, int TM, bool GEN = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? MC_MIN_BLOCKS_F32 : 2) k_advance_dyn(Params<R> P) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ unsigned long long qnext;
+    __shared__ unsigned long long qnext, claimed;
     InstD<R>* I = stageTables<R, TM>(P, smraw);
     blkZero();
-    if (threadIdx.x == 0) qnext = 0;
+    if (threadIdx.x == 0) qnext = claimed = 0;
     __syncthreads();
     Window<R> W;
     W.init(P);
     const unsigned long long n = P.live_in[0];
+    const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
     unsigned long long* q = &qnext;
-    unsigned long long qbeg = 0, qend = n;
-    if (sizeof(R) == 8 || P.qglobal == nullptr) {
-        const unsigned long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    unsigned long long qbeg = 0, qend = n, cap = 0;
+    if (P.qglobal == nullptr) {
         qbeg = min((unsigned long long)blockIdx.x * chunk, n);
         qend = min(qbeg + chunk, n);
     } else {
         q = P.qglobal;
+        if (sizeof(R) == 8) cap = 2 * chunk;
     }
     ParamView<R, TM> V;
     V.init(P, smraw);
-    dynamicLoop<R, REPLAY, LOG, TM, ParamView<R, TM>, GEN>(P, q, qbeg, qend, V, W);
+    dynamicLoop<R, REPLAY, LOG, TM, ParamView<R, TM>, GEN>(P, q, qbeg, qend, V, W, cap, &claimed);
     closeBlock<R, TM>(P, *I);
 }
 

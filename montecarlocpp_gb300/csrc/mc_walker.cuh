@@ -142,8 +142,8 @@ constexpr int MAX_EVENTS_PER_LAUNCH = 1 << 22;
 #ifndef MC_PDL
 #define MC_PDL 1
 #endif
-// FP32 single-instance dynamic launches claim slots from one launch-wide
-// counter (else each block from its own share).
+// Single-instance dynamic launches of long windows claim slots from one
+// launch-wide counter (else each block from its own share).
 #ifndef MC_DYN_GLOBAL_QUEUE
 #define MC_DYN_GLOBAL_QUEUE 1
 #endif
