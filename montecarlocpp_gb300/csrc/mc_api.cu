@@ -857,6 +857,7 @@ struct mc_session_s {
     bool timing = false;
     // device buffers
     void* state = nullptr;       // two halves
+    bool statePooled = false;    // from the stream-ordered pool (freed on the stream)
     size_t stateBytes = 0;
     void* tables = nullptr;
     void* dom_d = nullptr;
@@ -881,6 +882,24 @@ struct mc_session_s {
     Params<float> p32{};
     Params<double> p64{};
 };
+
+// Session state from the device's default stream-ordered memory pool; the
+// pool keeps freed memory for reuse by this process instead of returning it
+// at each synchronisation (a process setting, not a device one).
+#ifndef MC_STATE_POOL
+#define MC_STATE_POOL 1
+#endif
+static void keepPooledMemory() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    });
+}
 
 namespace {
 
@@ -1090,7 +1109,17 @@ int setupSession(mc_session_s* S) {
     const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
     S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
     S->slots = (long long)n;
-    CK(cudaMalloc(&S->state, 2 * half));
+    if (MC_STATE_POOL) {
+        // the state from the device's stream-ordered pool, which keeps what
+        // a finished session freed for the next one: a session's largest
+        // buffer then costs neither a fresh mapping nor a device-wide
+        // synchronisation when it is freed
+        keepPooledMemory();
+        CK(cudaMallocAsync(&S->state, 2 * half, S->stream));
+        S->statePooled = true;
+    } else {
+        CK(cudaMalloc(&S->state, 2 * half));
+    }
     char* sb = (char*)S->state;
     V4* h0[2]; V4* h1[2]; uint4* h2[2];
     for (int h = 0; h < 2; ++h) {
@@ -1293,7 +1322,11 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
 
 void freeSession(mc_session_s* S) {
     if (!S) return;
-    void* ps[] = {S->state, S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
+    if (S->state) {
+        if (S->statePooled) cudaFreeAsync(S->state, S->stream);
+        else cudaFree(S->state);
+    }
+    void* ps[] = {S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
                   S->rwords_d, S->roff_d, S->rcur_d, S->log_d, S->logcnt_d, S->reg_d};
     for (void* p : ps) if (p) cudaFree(p);
     if (S->ev0) cudaEventDestroy(S->ev0);
