@@ -857,7 +857,7 @@ struct mc_session_s {
     bool timing = false;
     // device buffers
     void* state = nullptr;       // two halves
-    bool statePooled = false;    // from the stream-ordered pool (freed on the stream)
+    bool pooled = false;         // buffers from the stream-ordered pool (freed on the stream)
     size_t stateBytes = 0;
     void* tables = nullptr;
     void* dom_d = nullptr;
@@ -883,12 +883,9 @@ struct mc_session_s {
     Params<double> p64{};
 };
 
-// Session state from the device's default stream-ordered memory pool; the
-// pool keeps freed memory for reuse by this process instead of returning it
-// at each synchronisation (a process setting, not a device one).
-#ifndef MC_STATE_POOL
-#define MC_STATE_POOL 1
-#endif
+// The device's default stream-ordered memory pool keeps freed memory for
+// reuse by this process instead of returning it at each synchronisation (a
+// process setting, not a device one).
 static void keepPooledMemory() {
     static std::once_flag once;
     std::call_once(once, [] {
@@ -901,15 +898,36 @@ static void keepPooledMemory() {
     });
 }
 
+// A session's device buffers come from the pool on the session's stream
+// (stream != null), so that creating and destroying sessions costs neither
+// driver allocations nor the device-wide synchronisation of cudaFree;
+// batches and servers keep plain allocations (stream == null).
+#ifndef MC_SESSION_POOL
+#define MC_SESSION_POOL 1
+#endif
+static cudaError_t devAlloc(void** p, size_t bytes, cudaStream_t pool) {
+    if (pool) {
+        keepPooledMemory();
+        return cudaMallocAsync(p, bytes, pool);
+    }
+    return cudaMalloc(p, bytes);
+}
+// host to device, in stream order on the pool's stream (from pageable
+// memory the call returns once the host buffer has been staged)
+static cudaError_t devUpload(void* dst, const void* src, size_t bytes, cudaStream_t pool) {
+    if (pool) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, pool);
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+}
+
 namespace {
 
 // Material tables in the flight precision, thresholds, guide table: one
 // device allocation; fills the table pointers of P.
 template <typename R>
-int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vmax) {
+int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vmax, cudaStream_t pool = nullptr) {
     const size_t nt = (size_t)m.nw * m.np;
     size_t tb = 2 * sizeof(R) * nt + sizeof(unsigned long long) * (2 * m.nw + 2 * nt) + 2 * GUIDE + 128;
-    CK(cudaMalloc(buf, tb));
+    CK(devAlloc(buf, tb, pool));
     char* base = (char*)*buf;
     std::vector<R> vel(nt), vt(nt);
     for (size_t i = 0; i < nt; ++i) { vel[i] = (R)m.vel[i]; vt[i] = (R)(m.vel[i] * m.tau[i]); }
@@ -927,12 +945,12 @@ int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vma
     P.fpthr = (unsigned long long*)base; base += 8 * nt;
     base = al16(base);
     P.wguide = (const uint16_t*)base; base += 2 * GUIDE;
-    CK(cudaMemcpy((void*)P.vel, vel.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((void*)P.vt, vt.data(), sizeof(R) * nt, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((void*)P.wthr, m.swthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((void*)P.pthr, m.spthr.data(), 8 * nt, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((void*)P.fwthr, m.fwthr.data(), 8 * m.nw, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy((void*)P.fpthr, m.fpthr.data(), 8 * nt, cudaMemcpyHostToDevice));
+    CK(devUpload((void*)P.vel, vel.data(), sizeof(R) * nt, pool));
+    CK(devUpload((void*)P.vt, vt.data(), sizeof(R) * nt, pool));
+    CK(devUpload((void*)P.wthr, m.swthr.data(), 8 * m.nw, pool));
+    CK(devUpload((void*)P.pthr, m.spthr.data(), 8 * nt, pool));
+    CK(devUpload((void*)P.fwthr, m.fwthr.data(), 8 * m.nw, pool));
+    CK(devUpload((void*)P.fpthr, m.fpthr.data(), 8 * nt, pool));
     {
         // guide table: first bin whose threshold exceeds k * 2^32 / GUIDE
         std::vector<uint16_t> g(GUIDE);
@@ -942,7 +960,7 @@ int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vma
             while (i < m.nw - 1 && x >= m.swthr[i]) ++i;
             g[k] = (uint16_t)i;
         }
-        CK(cudaMemcpy((void*)P.wguide, g.data(), 2 * GUIDE, cudaMemcpyHostToDevice));
+        CK(devUpload((void*)P.wguide, g.data(), 2 * GUIDE, pool));
     }
     P.nw = (int)m.nw;
     P.np = (int)m.np;
@@ -953,11 +971,11 @@ int uploadMaterial(const mc_material_s& m, void** buf, Params<R>& P, double& vma
 // count (montecarlo/problem.cpp:315-342); fills P.sd / em / emitCdf.
 template <typename R>
 int uploadDomain(const mc_domain_s& D, double fluxSum, long nemitReq, void** sd_d, EmitterD** em_d,
-                 long long** cdf_d, Params<R>& P, long& nemit, double& power) {
+                 long long** cdf_d, Params<R>& P, long& nemit, double& power, cudaStream_t pool = nullptr) {
     std::vector<SdomD<R>> sd(D.sd.size());
     for (size_t i = 0; i < sd.size(); ++i) castSdom(D.sd[i], sd[i], sizeof(R) == 4);
-    CK(cudaMalloc(sd_d, sizeof(SdomD<R>) * sd.size()));
-    CK(cudaMemcpy(*sd_d, sd.data(), sizeof(SdomD<R>) * sd.size(), cudaMemcpyHostToDevice));
+    CK(devAlloc(sd_d, sizeof(SdomD<R>) * sd.size(), pool));
+    CK(devUpload(*sd_d, sd.data(), sizeof(SdomD<R>) * sd.size(), pool));
     P.sd = (const SdomD<R>*)*sd_d;
     P.nsd = (int)sd.size();
     const long ne = (long)D.em.size();
@@ -976,10 +994,10 @@ int uploadDomain(const mc_domain_s& D, double fluxSum, long nemitReq, void** sd_
     power = wsum / (double)tot * fluxSum / 4.;
     for (long i = 0; i < ne; ++i)
         if (!(D.emWeight[i] > 0.)) return fail(MC_ERR_ARG, "No phonons to emit");
-    CK(cudaMalloc(em_d, sizeof(EmitterD) * ne));
-    CK(cudaMemcpy(*em_d, D.em.data(), sizeof(EmitterD) * ne, cudaMemcpyHostToDevice));
-    CK(cudaMalloc(cdf_d, sizeof(long long) * ne));
-    CK(cudaMemcpy(*cdf_d, cdf.data(), sizeof(long long) * ne, cudaMemcpyHostToDevice));
+    CK(devAlloc((void**)em_d, sizeof(EmitterD) * ne, pool));
+    CK(devUpload(*em_d, D.em.data(), sizeof(EmitterD) * ne, pool));
+    CK(devAlloc((void**)cdf_d, sizeof(long long) * ne, pool));
+    CK(devUpload(*cdf_d, cdf.data(), sizeof(long long) * ne, pool));
     P.em = *em_d;
     P.emitCdf = *cdf_d;
     P.nem = (int)ne;
@@ -991,16 +1009,18 @@ int setupSession(mc_session_s* S) {
     const mc_material_s& m = *S->mat;
     const mc_domain_s& D = *S->dom;
     Params<R> P{};
-    int rc = uploadMaterial<R>(m, &S->tables, P, S->vmax);
+    cudaStream_t pool = MC_SESSION_POOL ? S->stream : nullptr;
+    S->pooled = pool != nullptr;
+    int rc = uploadMaterial<R>(m, &S->tables, P, S->vmax, pool);
     if (rc) return rc;
-    rc = uploadDomain<R>(D, m.fluxSum, S->desc.nemit, &S->dom_d, &S->em_d, &S->cdf_d, P, S->nemit, S->power);
+    rc = uploadDomain<R>(D, m.fluxSum, S->desc.nemit, &S->dom_d, &S->em_d, &S->cdf_d, P, S->nemit, S->power, pool);
     if (rc) return rc;
     // counters: C_NCOUNTERS + two (front, back) live-count pairs + the
     // dynamic launches' slot counter
-    CK(cudaMalloc(&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 5)));
-    CK(cudaMalloc(&S->status_d, sizeof(unsigned int)));
+    CK(devAlloc((void**)&S->cnt_d, sizeof(unsigned long long) * (C_NCOUNTERS + 5), pool));
+    CK(devAlloc((void**)&S->status_d, sizeof(unsigned int), pool));
     S->rows = (int)problemRows(S->desc.problem, S->desc.cum_size);
-    CK(cudaMalloc(&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L)));
+    CK(devAlloc((void**)&S->tally_d, sizeof(double) * (size_t)S->rows * std::max(D.cols, 1L), pool));
     P.problem = S->desc.problem; P.rows = S->rows; P.cols = (int)D.cols;
     P.cumStep = cumStepOf(S->desc.problem, S->desc.maxscat, S->desc.cum_size);
     P.nemit = S->nemit;
@@ -1016,7 +1036,7 @@ int setupSession(mc_session_s* S) {
     P.cap = (unsigned long long)S->nemit;
     P.status = S->status_d;
     P.tally = S->tally_d;
-    CK(cudaMalloc(&S->csum_d, sizeof(double) * 4));
+    CK(devAlloc((void**)&S->csum_d, sizeof(double) * 4, pool));
     P.csum = S->csum_d;
     // replay
     if (S->replay) {
@@ -1025,17 +1045,17 @@ int setupSession(mc_session_s* S) {
         if (off[0] != 0 || nw < 0) return fail(MC_ERR_ARG, "replay offsets must start at 0");
         for (long i = 0; i < S->nemit; ++i)
             if (off[i + 1] < off[i]) return fail(MC_ERR_ARG, "replay offsets must not decrease");
-        CK(cudaMalloc(&S->rwords_d, sizeof(uint32_t) * std::max(nw, 1LL)));
-        if (nw) CK(cudaMemcpy(S->rwords_d, S->desc.replay_words, sizeof(uint32_t) * nw, cudaMemcpyHostToDevice));
-        CK(cudaMalloc(&S->roff_d, sizeof(long long) * (S->nemit + 1)));
-        CK(cudaMemcpy(S->roff_d, off, sizeof(long long) * (S->nemit + 1), cudaMemcpyHostToDevice));
-        CK(cudaMalloc(&S->rcur_d, sizeof(uint32_t) * S->nemit));
+        CK(devAlloc((void**)&S->rwords_d, sizeof(uint32_t) * std::max(nw, 1LL), pool));
+        if (nw) CK(devUpload(S->rwords_d, S->desc.replay_words, sizeof(uint32_t) * nw, pool));
+        CK(devAlloc((void**)&S->roff_d, sizeof(long long) * (S->nemit + 1), pool));
+        CK(devUpload(S->roff_d, off, sizeof(long long) * (S->nemit + 1), pool));
+        CK(devAlloc((void**)&S->rcur_d, sizeof(uint32_t) * S->nemit, pool));
         P.rwords = S->rwords_d; P.roff = S->roff_d; P.rcur = S->rcur_d;
     }
     if (S->logging) {
         long long ln = std::min<long long>(S->desc.log_phonons, S->nemit);
-        CK(cudaMalloc(&S->log_d, sizeof(double) * 12 * (size_t)ln * S->desc.log_cap + 8));
-        CK(cudaMalloc(&S->logcnt_d, sizeof(int) * (size_t)std::max(ln, 1LL)));
+        CK(devAlloc((void**)&S->log_d, sizeof(double) * 12 * (size_t)ln * S->desc.log_cap + 8, pool));
+        CK(devAlloc((void**)&S->logcnt_d, sizeof(int) * (size_t)std::max(ln, 1LL), pool));
         P.log = S->log_d; P.logcap = S->desc.log_cap; P.logn = ln; P.logcount = S->logcnt_d;
     }
     // launch configuration
@@ -1101,7 +1121,7 @@ int setupSession(mc_session_s* S) {
     if (!S->dyn) {
         const long long C = (S->nemit + S->grid - 1) / S->grid;
         n = (size_t)C * (size_t)S->grid;
-        CK(cudaMalloc(&S->reg_d, sizeof(unsigned) * 4 * (size_t)S->grid));
+        CK(devAlloc((void**)&S->reg_d, sizeof(unsigned) * 4 * (size_t)S->grid, pool));
         P.regCap = C;
     }
     using V4 = typename Vec4<R>::T;
@@ -1109,17 +1129,7 @@ int setupSession(mc_session_s* S) {
     const size_t half = 2 * al(sizeof(V4) * n) + al(sizeof(uint4) * n);
     S->stateBytes = 2 * (sizeof(V4) * 2 + sizeof(uint4)) * n;
     S->slots = (long long)n;
-    if (MC_STATE_POOL) {
-        // the state from the device's stream-ordered pool, which keeps what
-        // a finished session freed for the next one: a session's largest
-        // buffer then costs neither a fresh mapping nor a device-wide
-        // synchronisation when it is freed
-        keepPooledMemory();
-        CK(cudaMallocAsync(&S->state, 2 * half, S->stream));
-        S->statePooled = true;
-    } else {
-        CK(cudaMalloc(&S->state, 2 * half));
-    }
+    CK(devAlloc(&S->state, 2 * half, pool));
     char* sb = (char*)S->state;
     V4* h0[2]; V4* h1[2]; uint4* h2[2];
     for (int h = 0; h < 2; ++h) {
@@ -1322,13 +1332,13 @@ int resultImpl(mc_session_s* S, double* out, mc_stats* st) {
 
 void freeSession(mc_session_s* S) {
     if (!S) return;
-    if (S->state) {
-        if (S->statePooled) cudaFreeAsync(S->state, S->stream);
-        else cudaFree(S->state);
-    }
-    void* ps[] = {S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
+    void* ps[] = {S->state, S->tables, S->dom_d, S->em_d, S->cdf_d, S->cnt_d, S->status_d, S->tally_d, S->csum_d,
                   S->rwords_d, S->roff_d, S->rcur_d, S->log_d, S->logcnt_d, S->reg_d};
-    for (void* p : ps) if (p) cudaFree(p);
+    for (void* p : ps) {
+        if (!p) continue;
+        if (S->pooled) cudaFreeAsync(p, S->stream);
+        else cudaFree(p);
+    }
     if (S->ev0) cudaEventDestroy(S->ev0);
     if (S->ev1) cudaEventDestroy(S->ev1);
     if (S->ownStream && S->stream) cudaStreamDestroy(S->stream);
