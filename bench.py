@@ -380,7 +380,10 @@ def main():
                 "traffic": None, "peak_source": peak_kind, "kernel": "k_advance<float>", "launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": bytes_launch}
 
-    # e2e through mc_solve (host buffers)
+    # e2e through mc_solve (host buffers), after one untimed call (the first
+    # call of a process grows the stream-ordered memory pool its sessions
+    # draw from)
+    prob.solve(dt=W["dt"], nsteps=W["nsteps"], precision=32, steps_per_launch=K, seed=seed)
     e2e_steps, e2e_t = 0.0, 0.0
     for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
@@ -910,9 +913,15 @@ def bench_cross_plane(reps=5):
     steps = st["phonon_steps"] * reps
     ms = e0.elapsed_time(e1)
     sess.close()
-    t0 = time.perf_counter()
-    out = prob.solve(dt=W["dt"], nsteps=W["nsteps"], precision=64, steps_per_launch=W["nsteps"], seed=0)
-    e2e_s = time.perf_counter() - t0
+    # mc_solve end to end: the median of five calls after one untimed call
+    # (the first call of a process grows the stream-ordered memory pool)
+    prob.solve(dt=W["dt"], nsteps=W["nsteps"], precision=64, steps_per_launch=W["nsteps"], seed=0)
+    e2e = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        out = prob.solve(dt=W["dt"], nsteps=W["nsteps"], precision=64, steps_per_launch=W["nsteps"], seed=0)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e))
     vols = M.problem._handle(dom).cell_volumes()
     kappa = -float(np.sum(out[1] * vols) / np.sum(vols)) / (-2.0 / 1e-7)
     res = {"workload": "cross-plane film 100 nm, isothermal walls 301 / 299 K, 20 cells, 1e5 phonons, "
