@@ -283,7 +283,14 @@ int mc_solve_noalloc(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, d
 /* ---------------------------------------------- device-resident session */
 typedef struct mc_session_s* mc_session_h;
 
-/* Allocate the phonon structure of arrays and tables on the device. */
+/* Allocate the phonon structure of arrays and tables on the device. A
+ * session's buffers come from the device's default stream-ordered memory
+ * pool (cudaMallocAsync on the session stream, freed with cudaFreeAsync by
+ * mc_session_destroy); the library raises that pool's release threshold so
+ * that freed memory stays with the process for the next session, and
+ * creating or destroying a session never synchronises the device. A caller
+ * that wants the memory back calls cudaMemPoolTrimTo on the default pool.
+ * mc_solve uses a session. */
 int mc_session_create(mc_material_h m, mc_domain_h d, const mc_problem_desc* p, mc_session_h* out);
 /* Emit all phonons (reset tally, counters and time). Asynchronous. */
 int mc_session_emit(mc_session_h s);
