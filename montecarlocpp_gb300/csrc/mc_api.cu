@@ -905,6 +905,14 @@ static void keepPooledMemory() {
 #ifndef MC_SESSION_POOL
 #define MC_SESSION_POOL 1
 #endif
+// whether the current device has stream-ordered memory pools (else
+// sessions allocate with cudaMalloc)
+static bool poolsSupported() {
+    int dev = 0, ok = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&ok, cudaDevAttrMemoryPoolsSupported, dev) != cudaSuccess) return false;
+    return ok != 0;
+}
 static cudaError_t devAlloc(void** p, size_t bytes, cudaStream_t pool) {
     if (pool) {
         keepPooledMemory();
@@ -1009,7 +1017,7 @@ int setupSession(mc_session_s* S) {
     const mc_material_s& m = *S->mat;
     const mc_domain_s& D = *S->dom;
     Params<R> P{};
-    cudaStream_t pool = MC_SESSION_POOL ? S->stream : nullptr;
+    cudaStream_t pool = (MC_SESSION_POOL && poolsSupported()) ? S->stream : nullptr;
     S->pooled = pool != nullptr;
     int rc = uploadMaterial<R>(m, &S->tables, P, S->vmax, pool);
     if (rc) return rc;
