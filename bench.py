@@ -741,7 +741,7 @@ def bench_served(rate=200.0, duration=60.0, drain=30.0, nsteps=4000, seed=0, bud
             "incomplete_at_cutoff": n_inc, "cutoff_s": t_cut - c0,
             "solves_per_s": solves_per_s, "p50_s": pct(50), "p99_s": pct(99),
             "p99_s_lower_bound_with_incomplete": float(np.percentile(censored, 99)) if censored else None,
-            "steps_per_window": steps_per_window or "default (nsteps / 8)",
+            "steps_per_window": steps_per_window or "default (nsteps / 2)",
             "ticks": st["ticks"], "busy_s": st["busy_s"], "span_s": span,
             "phonon_steps_per_s": st["phonon_steps"] / max(st["busy_s"], 1e-9),
             "phonon_steps_per_solve": (sum(r["phonon_steps"] for r in done) / len(done)) if done else None,

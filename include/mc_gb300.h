@@ -385,7 +385,7 @@ typedef struct {
     int max_rounds;         /* give up (status MC_ERR_BUSY) after this many */
     int block_size;         /* 0 -> 256                                     */
     int steps_per_window;   /* dt-steps per tick, a divisor of nsteps; 0: the
-                               largest divisor of nsteps <= nsteps / 8      */
+                               largest divisor of nsteps <= nsteps / 2      */
 } mc_server_desc;
 
 typedef struct {

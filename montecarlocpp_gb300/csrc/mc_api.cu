@@ -1840,7 +1840,11 @@ struct ServerT : ServerBase {
             return fail(MC_ERR_ARG, "steps_per_window must divide nsteps");
         K = d.steps_per_window;
         if (K == 0) {
-            K = (int)std::max(1L, d.nsteps / 8);
+            // two windows per round: measured on the served stream against an
+            // eighth and a quarter of the horizon, it gave both the most
+            // solves/s at saturation and the lowest latencies below it (each
+            // tick's emission, flush and reduction cost less per phonon-step)
+            K = (int)std::max(1L, d.nsteps / 2);
             while (d.nsteps % K) --K;
         }
         nwin = (int)(d.nsteps / K);
